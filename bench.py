@@ -1,0 +1,439 @@
+"""Benchmark of the LIC volume ray-cast hot path (one JSON line on stdout).
+
+Workload (default): the mid-size configuration with lighting and precision — a 256^3 field of a
+uniform drift plus 8 seeded Gaussian vortices, dense uint8 noise (frequency 4.0) with
+central-difference gradients, Heun streamlines L = 40 each way at step 0.005, Gaussian filter,
+1024^2 image, ray spacing 1/256, gradient Phong lighting, FP16 field storage (FP32 and BF16 are
+measured alongside).  A step is one frame.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`value` is device throughput in Gsample-steps/s (one LIC integration step at one ray sample),
+whole job over all ranks; `e2e` is the same metric through the C ABI with host buffers
+(field + noise upload, preprocessing, render, image download inside the timed region).
+`--impl reference` times the CPU restatement of the reference's path (the reference itself is
+GLSL and cannot run without an OpenGL stack) on all host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Gsample-steps/s & frames/s, fwd and fwd+adjoint, at RMSE<=1e-3 vs FP64 oracle"
+UNIT = "Gsample-steps/s"
+L2_FLUSH_BYTES = 256 << 20
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--storage", default="f16", choices=["f32", "f16", "bf16"])
+    ap.add_argument("--sampler", default="cell", choices=["gather", "cell", "texture"])
+    ap.add_argument("--size", type=int, default=256)
+    ap.add_argument("--image", type=int, default=1024)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------------------------
+# distributed plumbing (one process per GPU; replicas of the same workload, no data exchange)
+# ---------------------------------------------------------------------------------------------
+class Dist:
+    def __init__(self, init: bool = True):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1 and init:
+            import torch
+            import torch.distributed as dist
+
+            torch.cuda.set_device(self.local)
+            dist.init_process_group("nccl")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ---------------------------------------------------------------------------------------------
+class Clocks:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(prefix="vvlic_clocks_", suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        with open(self.path) as fh:
+            for line in fh:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for name, val in zip(names, r[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+# ---------------------------------------------------------------------------------------------
+def bytes_per_texel(storage: str) -> int:
+    return 16 if storage == "f32" else 8
+
+
+def algorithmic_bytes(stats, params, storage: str, lit: bool, pixels: int) -> float:
+    """Cacheless trilinear-gather model: 8*(k*s_F + s_N) per sample-step, 8*s_F per sample for
+    the compositing fetch, 16 B per output pixel."""
+    k = {0: 1, 1: 2, 2: 4}[params.integrator]
+    sF = bytes_per_texel(storage)
+    sN = 4 if lit else 1
+    return stats.sample_steps * 8 * (k * sF + sN) + stats.samples * 8 * sF + pixels * 16
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def load_traffic(workload_key: str):
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as fh:
+        d = json.load(fh)
+    e = d.get(workload_key)
+    return None if e is None else e.get("bytes_per_launch")
+
+
+def make_workload(args):
+    from vectorvisualization_gb300 import workloads as wl
+
+    return wl.c2(size=args.size, image=args.image, storage=args.storage)
+
+
+def cpu_sample(w, seconds: float, threads: int = 0, rows_offset: int = 0):
+    """FP32 OpenMP CPU restatement on a stratified row subset sized to ~`seconds`."""
+    from oracle import pyoracle
+    from vectorvisualization_gb300 import capi
+
+    rgba = pyoracle.round_storage(pyoracle.encode_field(w.field), w.storage)
+    noise = w.noise if w.noise_mode == capi.NOISE_SCALAR else pyoracle.noise_gradients(w.noise, w.noise_mode)
+    sc = pyoracle.Scene(rgba, noise, w.tf_rgba, w.tf_opac, filter_table=w.filter_table)
+    H = w.height
+    # probe one row, then size the stratified subset
+    probe_row = [H // 2 + rows_offset % max(1, H // 2)]
+    t0 = time.perf_counter()
+    _, s = sc.render(w.params, w.views[0], w.width, H, rows=probe_row, precision=32, threads=threads)
+    dt = max(time.perf_counter() - t0, 1e-3)
+    nrows = int(max(1, min(H, seconds / dt)))
+    stride = max(1, H // nrows)
+    rows = list(range((rows_offset % stride), H, stride))[:nrows]
+    t0 = time.perf_counter()
+    img, smp = sc.render(w.params, w.views[0], w.width, H, rows=rows, precision=32, threads=threads)
+    dt = time.perf_counter() - t0
+    steps = float(smp.astype(np.float64).sum()) * (w.params.steps_forward + w.params.steps_backward)
+    return {"rate": steps / dt / 1e9, "seconds": dt, "rows": rows, "img": img, "sample_steps": steps,
+            "threads": pyoracle.max_threads() if threads <= 0 else threads}
+
+
+def run_reference(args, dist: Dist):
+    """CPU restatement of the reference path, all host threads, bounded sample per step."""
+    if dist.rank != 0:
+        return 0
+    w = make_workload(args)
+    per_step = max(1.0, min(args.cpu_seconds, 20.0))
+    for i in range(args.warmup):
+        cpu_sample(w, per_step / 4, rows_offset=i)
+    rates, secs, steps = [], 0.0, 0.0
+    res = None
+    for i in range(args.steps):
+        res = cpu_sample(w, per_step, rows_offset=i + args.warmup)
+        rates.append(res["rate"])
+        secs += res["seconds"]
+        steps += res["sample_steps"]
+    value = steps / secs / 1e9
+    full_frame_steps = None
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": secs / args.steps * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded SplitMix64 vortex field and noise)",
+        "config": {**w.describe(), "cpu_rows_per_step": len(res["rows"]) if res else 0},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": res["threads"] if res else 0, "kind": "port",
+                         "sample": f"{len(res['rows']) if res else 0} stratified rows of the {w.width}x{w.height} "
+                                   f"frame per step (FP32 OpenMP restatement of the GLSL path; the reference "
+                                   f"itself runs only through OpenGL)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    del full_frame_steps
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args, dist: Dist):
+    import torch
+
+    from vectorvisualization_gb300 import build, capi, workloads as wl
+
+    build.build()
+    dev = dist.local
+    torch.cuda.set_device(dev)
+    w = make_workload(args)
+    lit = w.params.illum == capi.ILLUM_GRADIENT
+    ctx = capi.Context(dev)
+    vid = wl.setup_context(ctx, w)
+    p = w.params
+    p.sampler = capi.SAMPLER[args.sampler]
+    ctx.set_params(p)
+    stream = torch.cuda.Stream(device=dev)
+    sh = stream.cuda_stream
+    W, H = w.width, w.height
+    out = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+
+    def frame():
+        ctx.render_device(vid, out.data_ptr(), W, H, None, sh)
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            frame()
+    stream.synchronize()
+    st0 = ctx.stats()
+
+    clocks = Clocks(dev)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    t_wall0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            flush.zero_()  # L2 flush between frames, outside the event pair
+            starts[k].record(stream)
+            frame()
+            ends[k].record(stream)
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter() - t_wall0
+    dist.barrier()
+    clk = clocks.stop()
+    times = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    st = ctx.stats()
+    assert st.sample_steps == st0.sample_steps
+    kernel_ms = sum(times)
+    steps_rank = st.sample_steps * args.steps
+    total_steps = dist.sum(float(steps_rank))
+    max_ms = dist.max(kernel_ms)
+    value = total_steps / (max_ms / 1e3) / 1e9
+    ms_per_step = max_ms / args.steps
+
+    peak, peak_kind = load_peaks()
+    alg = algorithmic_bytes(st, p, w.storage, lit, W * H)
+    achieved = alg / (ms_per_step / 1e3) / 1e9
+    key = f"c2/{w.storage}/{args.sampler}/{args.size}/{args.image}"
+    traffic = load_traffic(key)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "peak_kind": peak_kind,
+                "algorithmic_bytes_per_launch": alg,
+                "model": "8*(k*s_F+s_N) B per sample-step + 8*s_F per sample + 16 B per pixel"}
+
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": dist.world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_per_step,
+        "frames_per_s": 1e3 / ms_per_step * dist.world,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded SplitMix64 vortex field and noise; the reference ships no datasets)",
+        "config": {**w.describe(), "sampler": args.sampler,
+                   "l2": "flushed between frames (256 MiB write); inputs > L2",
+                   "sample_steps_per_frame": int(st.sample_steps), "samples_per_frame": int(st.samples),
+                   "rays": int(st.rays), "parallelism": f"replicas x{dist.world}"},
+        "wall_ms_per_step": t_wall / args.steps * 1e3,
+        "roofline": roofline,
+        "gpu_launches": args.steps,
+        "clocks": clk,
+    }
+
+    # reduced / full precision storage alongside (same frame, same sampler)
+    if not args.no_variants and dist.rank == 0:
+        variants = {}
+        for storage in ("f32", "f16", "bf16"):
+            if storage == w.storage:
+                variants[storage] = {"gss": value / dist.world, "ms": ms_per_step}
+                continue
+            vid2 = ctx.upload_field(w.field, storage=storage)
+            with torch.cuda.stream(stream):
+                frame2 = lambda: ctx.render_device(vid2, out.data_ptr(), W, H, None, sh)  # noqa: E731
+                frame2()
+                stream.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                flush.zero_()
+                e0.record(stream)
+                frame2()
+                e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+            s2 = ctx.stats()
+            variants[storage] = {"gss": s2.sample_steps / (ms / 1e3) / 1e9, "ms": ms}
+            ctx.free_volume(vid2)
+        line["storage_variants"] = variants
+
+    # end to end through the C ABI with host buffers
+    if not args.no_e2e:
+        field_h = torch.from_numpy(np.ascontiguousarray(w.field)).pin_memory()
+        noise_h = torch.from_numpy(np.ascontiguousarray(w.noise)).pin_memory()
+        img_h = torch.empty((H, W, 4), dtype=torch.float32).pin_memory()
+        lib = capi.load()
+        nz, ny, nx = w.field.shape[:3]
+        mz, my, mx = w.noise.shape
+        e2e_steps = max(1, min(args.steps, 3))
+        e2e_vid = None
+
+        def e2e_step():
+            nonlocal e2e_vid
+            if e2e_vid is not None:
+                ctx.free_volume(e2e_vid)
+            v = capi._I(0)
+            ctx._check(lib.vvlic_upload_field(ctx.h, field_h.data_ptr(), capi.DTYPE_FLOAT32, nx, ny, nz, None,
+                                              capi.STORAGE[w.storage], capi.C.byref(v)), "upload_field")
+            e2e_vid = v.value
+            ctx._check(lib.vvlic_upload_noise(ctx.h, noise_h.data_ptr(), mx, my, mz, w.noise_mode), "upload_noise")
+            ctx._check(lib.vvlic_render(ctx.h, e2e_vid, img_h.data_ptr(), W, H), "render")
+
+        e2e_step()
+        dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            e2e_step()
+        t = time.perf_counter() - t0
+        t = dist.max(t)
+        s3 = ctx.stats()
+        line["e2e"] = {"value": dist.sum(float(s3.sample_steps * e2e_steps)) / t / 1e9, "unit": UNIT,
+                       "h2d_bytes_per_step": int(field_h.numel() * 4 + noise_h.numel()),
+                       "d2h_bytes_per_step": int(img_h.numel() * 4),
+                       "ms_per_step": t / e2e_steps * 1e3,
+                       "includes": "field upload+encode, noise upload+gradients, cell layouts, render, image download"}
+        ctx.free_volume(e2e_vid)
+
+    # CPU baseline (rank 0, N=1 only): the FP32 OpenMP restatement on a bounded sample
+    if not args.no_cpu and dist.rank == 0 and dist.world == 1:
+        res = cpu_sample(w, args.cpu_seconds)
+        gpu_rows = out.cpu().numpy()[res["rows"]]
+        line["cpu_baseline"] = {
+            "value": res["rate"], "unit": UNIT, "cores": res["threads"], "kind": "port",
+            "sample": f"{len(res['rows'])} stratified rows of the {W}x{H} frame ({res['seconds']:.1f} s, "
+                      f"FP32 OpenMP restatement of the reference GLSL path)",
+            "rmse_gpu_vs_cpu_rows": float(np.sqrt(np.mean((gpu_rows.astype(np.float64) - res["img"]) ** 2))),
+        }
+    ctx.close()
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse()
+    # the reference arm runs on rank 0 only and needs no process group
+    dist = Dist(init=args.impl == "ours")
+    try:
+        if args.impl == "reference":
+            return run_reference(args, dist)
+        return run_ours(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,298 @@
+/*
+ * vvlic.h — C ABI of the GB300 3D line-integral-convolution (LIC) volume ray-caster.
+ *
+ * This is the drop-in boundary for the voLIC renderer's LIC hot path.  In the reference
+ * (VectorVisualization) that path is the GLSL program composed by Renderer::loadGLSLShader
+ * (renderer.cpp:807-871: inc_header.glsl + inc_lic.glsl + inc_illum.glsl + lic3d_fragment.glsl),
+ * fed through the Renderer C++ API (renderer.h:28-125) and the GL uniform interface
+ * (inc_header.glsl:22-63).  Every entry point below names the reference interface it replaces.
+ *
+ * Conventions
+ *   - Every function returns a vvlic_status; nothing throws across the boundary.
+ *   - Host buffers are owned by the caller; device buffers created by upload calls are owned by
+ *     the context and freed by vvlic_destroy / vvlic_free_volume.
+ *   - A context is bound to one CUDA device and must be used from one host thread at a time.
+ *     Different contexts are independent.
+ *   - `stream` arguments are cudaStream_t passed as void*; NULL means the legacy default stream.
+ *   - Images are RGBA float32, row-major, row 0 = bottom row (the GL window convention),
+ *     premultiplied colour exactly as the reference's gl_FragColor = dest.
+ */
+#ifndef VVLIC_H_
+#define VVLIC_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VVLIC_ABI_VERSION 1
+
+/* Largest streamline length per direction (stepsForward / stepsBackward). */
+#define VVLIC_MAX_STEPS 256
+/* Number of entries of the transfer-function tables (TransferEdit::_numEntries, transferEdit.cpp:61). */
+#define VVLIC_TF_ENTRIES 256
+
+typedef int32_t vvlic_status;
+enum {
+  VVLIC_OK = 0,
+  VVLIC_ERR_INVALID_ARGUMENT = 1,
+  VVLIC_ERR_OUT_OF_MEMORY = 2,
+  VVLIC_ERR_CUDA = 3,
+  VVLIC_ERR_NO_DEVICE = 4,
+  VVLIC_ERR_NOT_READY = 5,     /* a required input (field, noise, TF, filter) was never set */
+  VVLIC_ERR_TIMEOUT = 6,       /* a bounded device-side wait gave up */
+  VVLIC_ERR_UNSUPPORTED = 7,
+  VVLIC_ERR_BAD_HANDLE = 8,
+  VVLIC_ERR_IO = 9,
+  VVLIC_ERR_FORMAT = 10
+};
+
+/* Raw vector data types of a .raw file (reader.h DataType: DATRAW_FLOAT, DATRAW_UCHAR). */
+enum { VVLIC_DTYPE_FLOAT32 = 0, VVLIC_DTYPE_UINT8 = 1 };
+
+/* Device storage precision of the encoded field (RGBA per voxel).  The reference stores RGBA16F
+ * (VectorDataSet::createTextureIterp(..., true), 3DLIC.cpp:707 -> dataset.cpp:326-331). */
+enum { VVLIC_STORAGE_F32 = 0, VVLIC_STORAGE_F16 = 1, VVLIC_STORAGE_BF16 = 2 };
+
+/* How the kernels read the field:
+ *   GATHER  - 8 texel loads per trilinear from the x-fastest RGBA array;
+ *   CELL    - corner-packed cells: the 8 corners of every trilinear cell stored contiguously
+ *             (8x the memory, one or two vector loads per trilinear);
+ *   TEXTURE - hardware-filtered cudaTextureObject (8-bit fixed-point weights). */
+enum { VVLIC_SAMPLER_GATHER = 0, VVLIC_SAMPLER_CELL = 1, VVLIC_SAMPLER_TEXTURE = 2 };
+
+/* Noise texture preparation (NoiseDataSet::createTexture, dataset.cpp:1176-1344).
+ *   SCALAR  - noise value only (the reference without -g, read as the noise value, see quirks);
+ *   SOBEL   - -g with the 3x3x3 Sobel gradients (gradient.h:37 SOBEL 1);
+ *   CENTRAL - -g with the central-difference branch (gradient.cpp SOBEL 0). */
+enum { VVLIC_NOISE_SCALAR = 0, VVLIC_NOISE_GRAD_SOBEL = 1, VVLIC_NOISE_GRAD_CENTRAL = 2 };
+
+/* Streamline integrator.  HEUN is the reference's singleLICstep (inc_lic.glsl:93-145);
+ * EULER and RK4 are extensions with the same step size and first-same-as-last field reuse. */
+enum { VVLIC_EULER = 0, VVLIC_HEUN = 1, VVLIC_RK4 = 2 };
+
+/* Shading model: the #define variant of inc_illum.glsl (inc_header.glsl:3-8). */
+enum { VVLIC_ILLUM_NONE = 0, VVLIC_ILLUM_GRADIENT = 1, VVLIC_ILLUM_ZOECKLER = 2, VVLIC_ILLUM_MALLO = 3 };
+
+/* Transfer-function index: lic3d_fragment.glsl:54 uses the encoded z direction (.b);
+ * the slicing and vector-field shaders use the magnitude (.a). */
+enum { VVLIC_TF_INDEX_DIR_Z = 0, VVLIC_TF_INDEX_MAGNITUDE = 1 };
+
+/* Wrap mode of the 1D filter-kernel lookup: the reference sets GL_CLAMP (dataset.cpp:1499),
+ * whose LINEAR filter blends the outermost taps 50% with the (zero) border colour. */
+enum { VVLIC_KERNEL_CLAMP_BORDER = 0, VVLIC_KERNEL_CLAMP_EDGE = 1 };
+
+/* Analytic filter shapes for vvlic_make_filter_table.  BOX is LICFilter::createBoxFilter
+ * (dataset.cpp:1405-1413); the others stand in for the kernel PNGs the reference loads. */
+enum { VVLIC_FILTER_BOX = 0, VVLIC_FILTER_TRIANGLE = 1, VVLIC_FILTER_COS2 = 2, VVLIC_FILTER_GAUSSIAN = 3 };
+
+/* Projection of vvlic_view. */
+enum { VVLIC_PERSPECTIVE = 0, VVLIC_ORTHOGRAPHIC = 1 };
+
+/* Reproduced reference behaviours that differ from what the code evidently intends.
+ *   LUMINANCE_NOISE    without gradients the noise texture is GL_LUMINANCE whose .a samples
+ *                      as 1.0, so the LIC is flat (dataset.cpp:1291-1318, inc_lic.glsl:148).
+ *   UNIFORM_SCALE_BUG  setRenderVolParams writes scaleInv into the scaleVol uniform and leaves
+ *                      scaleVolInv at 0 whenever the shading variant uses scaleVolInv
+ *                      (renderer.cpp:941-944); the light direction then ignores the sample
+ *                      position.
+ *   GRAD_NOISE_NO_FREQ the gradient-noise fetch freqSamplingGrad ignores freqScale
+ *                      (inc_lic.glsl:124-131).
+ * VVLIC_QUIRKS_REFERENCE is what the reference actually computes. */
+enum {
+  VVLIC_QUIRK_LUMINANCE_NOISE = 1u << 0,
+  VVLIC_QUIRK_UNIFORM_SCALE_BUG = 1u << 1,
+  VVLIC_QUIRK_GRAD_NOISE_NO_FREQ = 1u << 2
+};
+#define VVLIC_QUIRKS_REFERENCE (VVLIC_QUIRK_UNIFORM_SCALE_BUG | VVLIC_QUIRK_GRAD_NOISE_NO_FREQ)
+
+/* Render parameters.  The first block is the reference's LICParams (types.h:91-109, defaults in
+ * its constructor); the rest are the shader #define variants and GL state the reference sets
+ * elsewhere.  Fill with vvlic_params_default() and change what you need. */
+typedef struct vvlic_params {
+  /* LICParams */
+  float step_size_vol;    /* stepSizeVol: ray sample spacing in texture units (1/128) */
+  float gradient_scale;   /* gradientScale: LIC intensity scale (30) */
+  float illum_scale;      /* illumScale (1) */
+  float freq_scale;       /* freqScale: noise frequency (1) */
+  int32_t num_iterations; /* numIterations: bound of each of the two nested ray loops (255) */
+  int32_t steps_forward;  /* stepsForward L_f (32) */
+  int32_t steps_backward; /* stepsBackward L_b (32) */
+  float step_size_lic;    /* stepSizeLIC h (0.01) */
+  /* variants */
+  int32_t integrator;     /* VVLIC_EULER / HEUN / RK4 (HEUN) */
+  int32_t illum;          /* VVLIC_ILLUM_* (NONE) */
+  int32_t tf_index;       /* VVLIC_TF_INDEX_* (DIR_Z) */
+  int32_t speed_of_flow;  /* SPEED_OF_FLOW define: scale steps by the magnitude (0) */
+  int32_t low_res;        /* Renderer::_lowRes preview overrides, renderer.cpp:947-966 (0) */
+  int32_t scalar_gate;    /* freqSampling's scalar gate, inc_lic.glsl:143 (0 = off) */
+  float gate_lo, gate_hi; /* gate bounds (0.1, 0.3) */
+  float eye_dist_factor;  /* (logEyeDist*0.5 + 0.3) with the never-written logEyeDist = 0 (0.3) */
+  float alpha_threshold;  /* early ray termination on the sample's src.a (0.95) */
+  uint32_t quirks;        /* VVLIC_QUIRK_* bits (VVLIC_QUIRKS_REFERENCE) */
+  /* light (GL_LIGHT0 as set up by init/updateLightPos, 3DLIC.cpp:736, renderer.cpp:431-466) */
+  float light_pos[3];     /* object-space point light ((0.5, 0.5, 1.5)) */
+  float spec_exp;         /* GL_SPOT_EXPONENT = Illumination specular exponent (40) */
+  float light_diffuse[3]; /* (1,1,1) */
+  float light_specular[3];/* (1,1,1) */
+  float light_ambient[3]; /* (0,0,0) */
+  /* kernel selection (no reference counterpart) */
+  int32_t sampler;        /* VVLIC_SAMPLER_* (CELL) */
+  int32_t reserved[7];
+} vvlic_params;
+
+/* View.  PERSPECTIVE follows Camera::setCamera (camera.cpp:56-67) followed by
+ * glTranslatef(-center) (renderer.cpp:146): gluPerspective(fovy, aspect, near, far),
+ * translate(pan), translate(0,0,-distance), rotate(quaternion).  ORTHOGRAPHIC (no reference
+ * counterpart) casts parallel rays along `dir`; the image spans center +- right +- up in object
+ * space.  Object space is the reference's: the volume is the box [0, extent] with the largest
+ * physical side 1. */
+typedef struct vvlic_view {
+  int32_t projection;
+  float quat[4];          /* camera rotation (x, y, z, w), Transform::_q; identity (0,0,0,1) */
+  float distance;         /* Camera::_dist (4) */
+  float pan[3];           /* Camera::_pos ((0,0,0)) */
+  float fovy_deg;         /* 35 */
+  float aspect;           /* <= 0: image width / height */
+  float ortho_center[3];
+  float ortho_right[3];
+  float ortho_up[3];
+  float ortho_dir[3];
+} vvlic_view;
+
+typedef struct vvlic_ctx vvlic_ctx;
+
+/* Per-render statistics of the last render call on a context. */
+typedef struct vvlic_stats {
+  uint64_t samples;       /* ray samples whose LIC was computed */
+  uint64_t sample_steps;  /* samples * (L_f + L_b): the throughput unit */
+  uint64_t rays;          /* pixels whose ray hit the volume */
+  float kernel_ms;        /* device time of the render kernel (CUDA events) */
+} vvlic_stats;
+
+/* ---- defaults and helpers (no device work) ------------------------------------------- */
+
+/* LICParams() defaults (types.h:91-99) plus the reference's shader variant defaults. */
+void vvlic_params_default(vvlic_params* p);
+/* Camera() defaults (camera.cpp:42-47): identity rotation, distance 4, fovy 35. */
+void vvlic_view_default(vvlic_view* v);
+/* Human-readable name of a status code. */
+const char* vvlic_status_string(vvlic_status s);
+int32_t vvlic_abi_version(void);
+
+/* Filter-kernel table of `width` uint8 texels (nextPowerTwo(width) as the reference does).
+ * BOX: LICFilter::createBoxFilter (dataset.cpp:1405-1413).  TRIANGLE/COS2/GAUSSIAN are analytic
+ * tables over texel centres t = (i+0.5)/W standing in for the kernel PNGs of
+ * LICFilter::loadData (dataset.cpp:1416-1467).  Writes *out_width; `out` holds >= 1024 bytes. */
+vvlic_status vvlic_make_filter_table(int32_t filter, int32_t width, uint8_t* out, int32_t* out_width);
+
+/* ---- context --------------------------------------------------------------------------- */
+
+/* Replaces Renderer::Renderer + Renderer::init (renderer.cpp:83-103) for the LIC path. */
+vvlic_status vvlic_create(vvlic_ctx** ctx, int32_t device);
+vvlic_status vvlic_destroy(vvlic_ctx* ctx);
+/* Text of the last error on this context ("" if none).  Valid until the next call. */
+const char* vvlic_last_error(const vvlic_ctx* ctx);
+
+/* ---- inputs -------------------------------------------------------------------------- */
+
+/* Vector field upload: VectorDataSet::loadData geometry (dataset.cpp:97-180) +
+ * createTextureIterp/fillTexDataFloatInterp encoding (dataset.cpp:290-366, 533-635) +
+ * Renderer::setDataTex.  `xyz` is host memory, nx*ny*nz*3 values, x fastest.
+ * slice_dist may be NULL (1,1,1).  Returns a volume id for vvlic_render. */
+vvlic_status vvlic_upload_field(vvlic_ctx* ctx, const void* xyz, int32_t dtype,
+                                int32_t nx, int32_t ny, int32_t nz, const float* slice_dist,
+                                int32_t storage, int32_t* vol_id);
+/* Same from a device pointer (float32 xyz only), asynchronous on `stream`. */
+vvlic_status vvlic_upload_field_device(vvlic_ctx* ctx, const float* d_xyz,
+                                       int32_t nx, int32_t ny, int32_t nz, const float* slice_dist,
+                                       int32_t storage, void* stream, int32_t* vol_id);
+vvlic_status vvlic_free_volume(vvlic_ctx* ctx, int32_t vol_id);
+/* Copy a volume's encoded texels (RGBA per voxel, x fastest, at the volume's storage precision:
+ * 16 bytes per voxel for F32, 8 for F16/BF16) to host memory; `capacity` is the size of `out`
+ * in bytes.  The texture-upload counterpart of glGetTexImage on VectorData_Tex. */
+vvlic_status vvlic_download_field(vvlic_ctx* ctx, int32_t vol_id, void* out, uint64_t capacity);
+/* Copy the prepared noise texels (1 or 4 bytes per voxel, see vvlic_upload_noise) to host. */
+vvlic_status vvlic_download_noise(vvlic_ctx* ctx, void* out, uint64_t capacity);
+/* Device bytes held by a volume (all layouts built for it). */
+vvlic_status vvlic_volume_bytes(const vvlic_ctx* ctx, int32_t vol_id, uint64_t* bytes);
+
+/* Noise upload: NoiseDataSet::createTexture (dataset.cpp:1176-1344) + Renderer::setNoiseTex.
+ * `noise` is host uint8, mx*my*mz, x fastest.  mode = VVLIC_NOISE_*; gradient modes run
+ * computeGradients -> filterGradients -> quantizeGradients (gradient.cpp:190-531) on the device
+ * and pack RGBA = (gradient, noise) like dataset.cpp:1270-1286.  Wrap is REPEAT. */
+vvlic_status vvlic_upload_noise(vvlic_ctx* ctx, const uint8_t* noise,
+                                int32_t mx, int32_t my, int32_t mz, int32_t mode);
+
+/* Optional secondary scalar volume for the freqSampling gate (VolumeDataSet, dataset.cpp:840-1050,
+ * Renderer::setScalarTex).  Host float32, values as the shader sees them (.r). */
+vvlic_status vvlic_upload_scalar(vvlic_ctx* ctx, const float* scalar,
+                                 int32_t nx, int32_t ny, int32_t nz);
+
+/* Transfer function: TransferEdit::updateTextures (transferEdit.cpp:480-543) +
+ * Renderer::setTFrgbTex / setTFalphaOpacTex.  rgba: 256*4 floats (TF_RGBA, channels already
+ * divided by 255 for 8-bit tables); opacity: 256 floats (the .a = opacity channel of
+ * TF_AlphaOpac).  Either may be NULL to keep the current table.  Initial tables are the
+ * reference default (transferEdit.cpp:76-82). */
+vvlic_status vvlic_set_tf(vvlic_ctx* ctx, const float* rgba, const float* opacity);
+
+/* Filter kernel: LICFilter::createTexture (dataset.cpp:1470-1500) + Renderer::setLICFilter.
+ * The tap weights w[-L_b..L_f] and the inverse filter area (calcFilterKernelInvArea,
+ * dataset.cpp:1503-1512) are derived at render time from the table and the current L_f/L_b. */
+vvlic_status vvlic_set_filter_table(vvlic_ctx* ctx, const uint8_t* table, int32_t width,
+                                    int32_t clamp_mode);
+/* Explicit tap weights w[j], j = -L_b..L_f (count L_b+L_f+1), replacing the table lookup, and
+ * the inverse filter area used for the intensity scale.  Pass NULL to go back to the table. */
+vvlic_status vvlic_set_filter_taps(vvlic_ctx* ctx, const float* taps, int32_t steps_backward,
+                                   int32_t steps_forward, float inv_filter_area);
+/* The taps the next render would use (count L_b+L_f+1) and the inverse filter area. */
+vvlic_status vvlic_get_filter_taps(const vvlic_ctx* ctx, float* taps, int32_t capacity,
+                                   float* inv_filter_area);
+
+/* LICParams + shader variant: Renderer::setLICParams + setRenderVolParams (renderer.cpp:925-996)
+ * + the define injection of GLSLShader::loadShader (GLSLShader.cpp:120-136). */
+vvlic_status vvlic_set_params(vvlic_ctx* ctx, const vvlic_params* params);
+vvlic_status vvlic_get_params(const vvlic_ctx* ctx, vvlic_params* params);
+/* Camera: Renderer::setCamera + Camera::setCamera (camera.cpp:56-67). */
+vvlic_status vvlic_set_view(vvlic_ctx* ctx, const vvlic_view* view);
+
+/* Per-pixel rays of the current view for volume `vol_id` at w x h, in object space:
+ * origin(u,v) = c[0..2] + u*c[3..5] + v*c[6..8], direction(u,v) = c[9..11] + u*c[12..14] +
+ * v*c[15..17] with u = px+0.5, v = py+0.5; c[18] = 1 when the entry parameter is clamped to
+ * t >= 0 (perspective).  21 doubles are written (c[19], c[20] reserved). */
+vvlic_status vvlic_view_rays(const vvlic_ctx* ctx, int32_t vol_id, int32_t w, int32_t h,
+                             double* coeffs);
+
+/* ---- rendering --------------------------------------------------------------------------- */
+
+/* Renderer::render -> raycastVolume (renderer.cpp:126-312, 1093-1120): one LIC ray per pixel.
+ * `out_rgba` is HOST memory (w*h*4 floats); the call copies the image back and synchronises. */
+vvlic_status vvlic_render(vvlic_ctx* ctx, int32_t vol_id, float* out_rgba, int32_t w, int32_t h);
+/* Same into DEVICE memory, asynchronous on `stream`.  `d_samples` (optional, w*h uint32) gets
+ * the number of LIC samples of each ray. */
+vvlic_status vvlic_render_device(vvlic_ctx* ctx, int32_t vol_id, float* d_out_rgba,
+                                 int32_t w, int32_t h, uint32_t* d_samples, void* stream);
+/* Statistics of the last render (samples are counted on the device every render). */
+vvlic_status vvlic_get_stats(vvlic_ctx* ctx, vvlic_stats* stats);
+
+/* Composite an RGBA image over an opaque white background in place:
+ * background_fragment.glsl:7-20 (dest = clamp((1-dest.a)*white + dest, 0, 1)).  Host memory. */
+vvlic_status vvlic_composite_background(float* rgba, int32_t w, int32_t h, const float* bg_rgba);
+
+/* ---- preprocessing on caller-owned device buffers ----------------------------------- */
+
+/* computeGradients/filterGradients/quantizeGradients + RGBA pack (gradient.cpp:190-531,
+ * dataset.cpp:1270-1286) on device buffers: d_noise (mx*my*mz uint8) -> d_rgba (4 bytes per
+ * voxel: quantised gradient xyz, noise).  mode is VVLIC_NOISE_GRAD_SOBEL or _CENTRAL.
+ * Allocates a temporary float gradient buffer of 12 bytes per voxel. */
+vvlic_status vvlic_noise_gradients_device(const uint8_t* d_noise, int32_t mx, int32_t my,
+                                          int32_t mz, int32_t mode, const float* slice_dist,
+                                          uint8_t* d_rgba, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VVLIC_H_ */

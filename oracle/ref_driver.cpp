@@ -1,0 +1,49 @@
+/*
+ * ORACLE — test infrastructure, not product code.
+ *
+ * Compiles the reference's own noise-gradient code (VectorVisualization/gradient.cpp:190-531)
+ * unmodified and exposes it through one C function, so the restatement in vvlic_oracle.hpp and
+ * the device kernel can be pinned against what the reference itself computes.  Built by
+ * oracle/build_ref.sh into oracle/_ref/ (never committed).  VVREF_CENTRAL selects the
+ * central-difference branch (SOBEL 0); gradient.h hard-codes SOBEL 1.
+ */
+#include "gradient.h"
+#ifdef VVREF_CENTRAL
+#undef SOBEL
+#define SOBEL 0
+#endif
+#include "gradient.cpp"
+
+/* VolumeData's destructor lives in dataset.cpp, which is not compiled here; the buffers below
+ * are owned by the caller. */
+VolumeData::~VolumeData(void) {}
+
+extern "C" int vvref_noise_gradients(const unsigned char* noise, const int m[3], const float sd[3],
+                                     unsigned char* out_rgba) {
+  VolumeData vd;
+  vd.data = (void*)noise;
+  vd.newData = NULL;
+  vd.dataType = DATRAW_UCHAR;
+  vd.dataDim = 1;
+  for (int i = 0; i < 3; ++i) {
+    vd.size[i] = m[i];
+    vd.texSize[i] = m[i];
+    vd.sliceDist[i] = sd ? sd[i] : 1.0f;
+  }
+  float* g = computeGradients(&vd);
+  if (!g) return -1;
+  filterGradients(&vd, g);
+  unsigned char* q = (unsigned char*)quantizeGradients(&vd, g, DATRAW_UCHAR);
+  if (!q) return -2;
+  /* RGBA pack of NoiseDataSet::createTexture (dataset.cpp:1270-1286) */
+  const long count = (long)m[0] * m[1] * m[2];
+  for (long a = 0; a < count; ++a) {
+    out_rgba[4 * a + 0] = q[3 * a + 0];
+    out_rgba[4 * a + 1] = q[3 * a + 1];
+    out_rgba[4 * a + 2] = q[3 * a + 2];
+    out_rgba[4 * a + 3] = noise[a];
+  }
+  delete[] g;
+  delete[] q;
+  return 0;
+}

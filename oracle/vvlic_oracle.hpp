@@ -1,0 +1,760 @@
+/*
+ * ORACLE — test infrastructure, not product code.
+ *
+ * A CPU restatement of the voLIC LIC ray-casting hot path (liaoyg/VectorVisualization), written
+ * to be checked against and timed beside the CUDA kernels.  Only tests/, the smoke check and
+ * bench.py's CPU-baseline / reference arm may call it.  Nothing in the product links it.
+ *
+ * One template over the arithmetic type Real gives
+ *   - the FP64 correctness oracle (Real = double), and
+ *   - the FP32 OpenMP CPU baseline (Real = float).
+ *
+ * What it follows (file:line within VectorVisualization/):
+ *   GLSL hot path      shader/lic3d_fragment.glsl:5-99, shader/inc_lic.glsl:134-265,
+ *                      shader/inc_illum.glsl:1-41 and 257-271, shader/inc_header.glsl:22-63
+ *   uniforms           renderer.cpp:925-996 (setRenderVolParams)
+ *   volume geometry    dataset.cpp:139-176 (VectorDataSet::loadData)
+ *   view               camera.cpp:56-67 (Camera::setCamera), renderer.cpp:146, 682-736
+ *   field encoding     dataset.cpp:533-635 (fillTexDataFloatInterp, interpolation index 0)
+ *   noise gradients    gradient.cpp:190-531, gradient.h:37-39, dataset.cpp:1270-1286
+ *   filter kernel      dataset.cpp:1405-1413, 1470-1512
+ *   transfer function  transferEdit.cpp:76-82, 480-543
+ * GL sampler behaviour (texel centres, LINEAR, CLAMP_TO_EDGE / REPEAT / GL_CLAMP with a zero
+ * border, uint8 read as x/255) is restated from the OpenGL 2.1 specification, section 3.8.
+ *
+ * Parity of the GLSL part is unpinned by reference tests (the reference has none and its
+ * inputs are not shipped); the preprocessing restatements are pinned against the reference's
+ * own gradient.cpp compiled here (oracle/build_ref.sh).
+ */
+#ifndef VVLIC_ORACLE_HPP_
+#define VVLIC_ORACLE_HPP_
+
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include "../include/vvlic.h"
+
+#if defined(_OPENMP)
+#include <omp.h>
+#endif
+
+namespace vvo {
+
+/* ------------------------------------------------------------------------------------- */
+/* small vector types                                                                     */
+/* ------------------------------------------------------------------------------------- */
+template <class R> struct V3 { R x, y, z; };
+template <class R> struct V4 { R x, y, z, w; };
+
+template <class R> static inline V3<R> v3(R x, R y, R z) { return V3<R>{x, y, z}; }
+template <class R> static inline V3<R> operator+(V3<R> a, V3<R> b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+template <class R> static inline V3<R> operator-(V3<R> a, V3<R> b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+template <class R> static inline V3<R> operator*(V3<R> a, R s) { return {a.x * s, a.y * s, a.z * s}; }
+template <class R> static inline V3<R> mul(V3<R> a, V3<R> b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
+template <class R> static inline R dot(V3<R> a, V3<R> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+/* normalize(0) is defined as 0 (GLSL leaves it undefined). */
+template <class R> static inline V3<R> normalize(V3<R> a) {
+  R d = dot(a, a);
+  if (!(d > R(0))) return {R(0), R(0), R(0)};
+  R s = R(1) / std::sqrt(d);
+  return a * s;
+}
+template <class R> static inline R clamp01(R v) { return v < R(0) ? R(0) : (v > R(1) ? R(1) : v); }
+
+/* ------------------------------------------------------------------------------------- */
+/* volume geometry: VectorDataSet::loadData (dataset.cpp:139-176)                          */
+/* ------------------------------------------------------------------------------------- */
+struct Geometry {
+  double scale[3], scale_inv[3], extent[3], center[3], tex_max[3];
+};
+
+static inline Geometry geometry(const int n[3], const float sd_in[3]) {
+  Geometry g;
+  float sd[3] = {1.f, 1.f, 1.f};
+  if (sd_in) for (int i = 0; i < 3; ++i) sd[i] = sd_in[i];
+  /* the reference computes these in float */
+  float vol_size[3], max_vol = 0.f;
+  int max_tex = 0;
+  for (int i = 0; i < 3; ++i) {
+    vol_size[i] = (float)n[i] * sd[i];
+    if (vol_size[i] > max_vol) max_vol = vol_size[i];
+    if (n[i] > max_tex) max_tex = n[i];
+  }
+  for (int i = 0; i < 3; ++i) {
+    float scale = (float)max_tex / ((float)n[i] * sd[i]);
+    float scale_inv = (float)n[i] * sd[i] / (float)max_tex;
+    float extent = (float)n[i] * sd[i] / max_vol;
+    g.scale[i] = scale;
+    g.scale_inv[i] = scale_inv;
+    g.extent[i] = extent;
+    g.center[i] = extent / 2.0f;
+    g.tex_max[i] = (double)(extent * scale); /* renderer.cpp:934-937 (float product) */
+  }
+  return g;
+}
+
+/* ------------------------------------------------------------------------------------- */
+/* field encoding: fillTexDataFloatInterp (dataset.cpp:533-635) with interpIndex = 0        */
+/* float arithmetic exactly as the reference performs it; compile with -ffp-contract=off.  */
+/* An all-zero field (maxLen = 0) gets magnitude 0 where the reference would divide 0/0.   */
+/* ------------------------------------------------------------------------------------- */
+static inline void encode_field(const void* xyz, int dtype, const int n[3], float* out_rgba) {
+  const size_t count = (size_t)n[0] * n[1] * n[2];
+  float max_len = -1.0f;
+  for (size_t a = 0; a < count; ++a) {
+    float len;
+    float* o = out_rgba + 4 * a;
+    if (dtype == VVLIC_DTYPE_UINT8) {
+      /* dataU -= 128 on unsigned char wraps modulo 256 (dataset.cpp:565-569) */
+      const uint8_t* u = (const uint8_t*)xyz + 3 * a;
+      unsigned char t[3];
+      for (int c = 0; c < 3; ++c) t[c] = (unsigned char)(u[c] - 128);
+      len = std::sqrt((float)((int)t[0] * t[0]) + (float)((int)t[1] * t[1]) + (float)((int)t[2] * t[2]));
+      if (len < 1e-5f) {
+        len = 0.0f;
+        o[0] = o[1] = o[2] = 0.5f;
+      } else {
+        for (int c = 0; c < 3; ++c) o[c] = 0.5f * (float)t[c] / len + 0.5f;
+      }
+    } else {
+      const float* f = (const float*)xyz + 3 * a;
+      len = std::sqrt(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]);
+      if (len < 1e-5f) {
+        len = 0.0f;
+        o[0] = o[1] = o[2] = 0.5f;
+      } else {
+        for (int c = 0; c < 3; ++c) o[c] = 0.5f * f[c] / len + 0.5f;
+      }
+    }
+    if (len > max_len) max_len = len;
+    o[3] = len;
+  }
+  for (size_t a = 0; a < count; ++a) {
+    float* o = out_rgba + 4 * a;
+    float len = max_len > 0.0f ? o[3] / max_len : 0.0f;
+    o[3] = (len > 1.0f) ? 1.0f : ((len < 0.0f) ? 0.0f : len);
+  }
+}
+
+/* Round-to-nearest-even to FP16 / BF16 and back, the storage emulation used to compare with
+ * reduced-precision field storage (the reference itself stores RGBA16F). */
+static inline float round_to_f16(float f) {
+  if (std::isnan(f)) return f;
+  float a = std::fabs(f);
+  if (a >= 65520.0f) return std::copysign(INFINITY, f);
+  if (a < 6.103515625e-05f) { /* subnormal half: quantum 2^-24 */
+    float q = std::nearbyint(a * 16777216.0f) / 16777216.0f;
+    return std::copysign(q, f);
+  }
+  int e;
+  std::frexp(a, &e); /* a = m * 2^e, m in [0.5,1) */
+  float quantum = std::ldexp(1.0f, e - 11);
+  float q = std::nearbyint(a / quantum) * quantum;
+  return std::copysign(q, f);
+}
+static inline float round_to_bf16(float f) {
+  if (std::isnan(f)) return f;
+  uint32_t u;
+  std::memcpy(&u, &f, 4);
+  uint32_t lsb = (u >> 16) & 1u;
+  u += 0x7fffu + lsb;
+  u &= 0xffff0000u;
+  float r;
+  std::memcpy(&r, &u, 4);
+  return r;
+}
+static inline void round_storage(float* v, size_t count, int storage) {
+  if (storage == VVLIC_STORAGE_F16)
+    for (size_t i = 0; i < count; ++i) v[i] = round_to_f16(v[i]);
+  else if (storage == VVLIC_STORAGE_BF16)
+    for (size_t i = 0; i < count; ++i) v[i] = round_to_bf16(v[i]);
+}
+
+/* ------------------------------------------------------------------------------------- */
+/* noise gradients: computeGradients / filterGradients / quantizeGradients                */
+/* (gradient.cpp:190-531; GRAD_FILTER_SIZE 5, SIGMA2 5.0f, gradient.h:38-39), RGBA pack    */
+/* (dataset.cpp:1270-1286).  Float arithmetic in the reference's order.                    */
+/* ------------------------------------------------------------------------------------- */
+static inline void noise_gradient_filter_weights(float w[27]) {
+  /* filter[((fw+k)*5 + fw+j)*5 + fw+i] for i,j,k in [-2, 0] (gradient.cpp:393-409) */
+  float sum = 0.0f;
+  int idx = 0;
+  for (int k = -2; k < 1; ++k)
+    for (int j = -2; j < 1; ++j)
+      for (int i = -2; i < 1; ++i) {
+        float v = std::exp(-(float)(i * i + j * j + k * k) / 5.0f);
+        w[idx++] = v;
+        sum += v;
+      }
+  for (int q = 0; q < 27; ++q) w[q] /= sum;
+}
+
+static inline void noise_gradients(const uint8_t* noise, const int m[3], int mode,
+                                   const float* sd_in, uint8_t* out_rgba) {
+  const int nx = m[0], ny = m[1], nz = m[2];
+  float sd[3] = {1.f, 1.f, 1.f};
+  if (sd_in) for (int i = 0; i < 3; ++i) sd[i] = sd_in[i];
+  const size_t count = (size_t)nx * ny * nz;
+  std::vector<float> g(3 * count), fg(3 * count);
+  auto V = [&](int x, int y, int z) -> float { return (float)noise[((size_t)z * ny + y) * nx + x]; };
+  /* Sobel weights, weights[dir][i+1][j+1][k+1] (gradient.cpp:199-224) */
+  static const int W[3][3][3][3] = {
+      {{{-1, -3, -1}, {-3, -6, -3}, {-1, -3, -1}}, {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, {{1, 3, 1}, {3, 6, 3}, {1, 3, 1}}},
+      {{{-1, -3, -1}, {0, 0, 0}, {1, 3, 1}}, {{-3, -6, -3}, {0, 0, 0}, {3, 6, 3}}, {{-1, -3, -1}, {0, 0, 0}, {1, 3, 1}}},
+      {{{-1, 0, 1}, {-3, 0, 3}, {-1, 0, 1}}, {{-3, 0, 3}, {-6, 0, 6}, {-3, 0, 3}}, {{-1, 0, 1}, {-3, 0, 3}, {-1, 0, 1}}}};
+  for (int z = 0; z < nz; ++z)
+    for (int y = 0; y < ny; ++y)
+      for (int x = 0; x < nx; ++x) {
+        float* gp = &g[3 * (((size_t)z * ny + y) * nx + x)];
+        if (mode == VVLIC_NOISE_GRAD_SOBEL) {
+          if (x > 0 && x < nx - 1 && y > 0 && y < ny - 1 && z > 0 && z < nz - 1) {
+            for (int d = 0; d < 3; ++d) {
+              gp[d] = 0.0f;
+              for (int i = -1; i < 2; i++)
+                for (int j = -1; j < 2; j++)
+                  for (int k = -1; k < 2; k++) gp[d] += (float)W[d][i + 1][j + 1][k + 1] * V(x + i, y + j, z + k);
+              gp[d] /= 2.0f * sd[d];
+            }
+          } else {
+            gp[0] = (x < 1) ? (V(x + 1, y, z) - V(x, y, z)) / sd[0] : (V(x, y, z) - V(x - 1, y, z)) / sd[0];
+            gp[1] = (y < 1) ? (V(x, y + 1, z) - V(x, y, z)) / sd[1] : (V(x, y, z) - V(x, y - 1, z)) / sd[1];
+            gp[2] = (z < 1) ? (V(x, y, z + 1) - V(x, y, z)) / sd[2] : (V(x, y, z) - V(x, y, z - 1)) / sd[2];
+          }
+        } else {
+          /* SOBEL 0 branch (gradient.cpp:294-368).  Its high-border test `idx > size-1` never
+           * holds, so at the last slice it reads one voxel past the row; those gradients are
+           * never read by the asymmetric smoothing window below, so a one-sided difference is
+           * used there instead of the out-of-row read. */
+          auto cd = [&](int c, int lim, float lo, float mid, float hi, float s) -> float {
+            if (c < 1) return (hi - mid) / s;
+            if (c >= lim - 1) return (mid - lo) / s;
+            return (hi - lo) / s * 0.5f;
+          };
+          float c0 = V(x, y, z);
+          gp[0] = cd(x, nx, x > 0 ? V(x - 1, y, z) : c0, c0, x < nx - 1 ? V(x + 1, y, z) : c0, sd[0]);
+          gp[1] = cd(y, ny, y > 0 ? V(x, y - 1, z) : c0, c0, y < ny - 1 ? V(x, y + 1, z) : c0, sd[1]);
+          gp[2] = cd(z, nz, z > 0 ? V(x, y, z - 1) : c0, c0, z < nz - 1 ? V(x, y, z + 1) : c0, sd[2]);
+        }
+      }
+  float w[27];
+  noise_gradient_filter_weights(w);
+  for (int z = 0; z < nz; ++z)
+    for (int y = 0; y < ny; ++y)
+      for (int x = 0; x < nx; ++x) {
+        int bd = std::min(std::min(std::min(x, nx - x - 1), std::min(y, ny - y - 1)), std::min(z, nz - z - 1));
+        int fw = std::min(2, bd);
+        size_t gi = 3 * (((size_t)z * ny + y) * nx + x);
+        for (int c = 0; c < 3; ++c) {
+          float acc = 0.0f;
+          for (int k = -fw; k < fw - 1; ++k)
+            for (int j = -fw; j < fw - 1; ++j)
+              for (int i = -fw; i < fw - 1; ++i) {
+                /* the reference indexes the 5x5x5 table with the shrunken fw */
+                int widx = ((fw + k) * 5 + fw + j) * 5 + fw + i;
+                int wk = widx / 25, wj = (widx / 5) % 5, wi = widx % 5;
+                float wv = w[(wk * 3 + wj) * 3 + wi];
+                acc += wv * g[3 * (((size_t)(z + k) * ny + (y + j)) * nx + (x + i)) + c];
+              }
+          fg[gi + c] = acc;
+        }
+      }
+  for (size_t a = 0; a < count; ++a) {
+    float gr[3] = {fg[3 * a], fg[3 * a + 1], fg[3 * a + 2]};
+    float len = std::sqrt(gr[0] * gr[0] + gr[1] * gr[1] + gr[2] * gr[2]);
+    if (len < 1e-5f) {
+      gr[0] = gr[1] = gr[2] = 0.0f;
+    } else {
+      gr[0] /= len;
+      gr[1] /= len;
+      gr[2] /= len;
+    }
+    for (int c = 0; c < 3; ++c) out_rgba[4 * a + c] = (unsigned char)(((double)gr[c] + 1.0) / 2.0 * UCHAR_MAX);
+    out_rgba[4 * a + 3] = noise[a];
+  }
+}
+
+/* ------------------------------------------------------------------------------------- */
+/* filter table and taps                                                                   */
+/* ------------------------------------------------------------------------------------- */
+static inline int next_pow2(int w) {
+  int p = 1;
+  while (p < w) p <<= 1;
+  return p;
+}
+
+/* calcFilterKernelInvArea (dataset.cpp:1503-1512); the box filter uses 0.5 (dataset.cpp:1412). */
+static inline float filter_inv_area(const uint8_t* t, int W, bool is_box) {
+  if (is_box) return 0.5f;
+  float area = 0.0f;
+  for (int i = 0; i < W; ++i) area += t[i];
+  return 0.5f * W * 255.0f / area;
+}
+
+/* texture1D(licKernelSampler, s).r: LUMINANCE8 table, LINEAR, GL_CLAMP (border 0) or
+ * CLAMP_TO_EDGE (dataset.cpp:1494-1499). */
+template <class R> static inline R kernel_lookup(const uint8_t* t, int W, R s, int clamp_mode) {
+  if (s < R(0)) s = R(0);
+  if (s > R(1)) s = R(1);
+  R u = s * R(W) - R(0.5);
+  R fl = std::floor(u);
+  int i0 = (int)fl;
+  R a = u - fl;
+  auto tex = [&](int i) -> R {
+    if (clamp_mode == VVLIC_KERNEL_CLAMP_EDGE) i = std::min(std::max(i, 0), W - 1);
+    else if (i < 0 || i >= W) return R(0);
+    return R(t[i]) / R(255);
+  };
+  return (R(1) - a) * tex(i0) + a * tex(i0 + 1);
+}
+
+/* taps[j + L_b] = kernel weight of tap j (j = -L_b..L_f), offsets as accumulated by
+ * computeLIC (inc_lic.glsl:219-262): 0.5, then -= 0.5/L_b per backward step, += 0.5/L_f per
+ * forward step. */
+template <class R> static inline void filter_taps(const uint8_t* t, int W, int clamp_mode, int lb, int lf, R* taps) {
+  taps[lb] = kernel_lookup<R>(t, W, R(0.5), clamp_mode);
+  R off = R(0.5);
+  R kb = lb > 0 ? R(0.5) / R(lb) : R(0);
+  for (int i = 1; i <= lb; ++i) {
+    off -= kb;
+    taps[lb - i] = kernel_lookup<R>(t, W, off, clamp_mode);
+  }
+  off = R(0.5);
+  R kf = lf > 0 ? R(0.5) / R(lf) : R(0);
+  for (int i = 1; i <= lf; ++i) {
+    off += kf;
+    taps[lb + i] = kernel_lookup<R>(t, W, off, clamp_mode);
+  }
+}
+
+/* ------------------------------------------------------------------------------------- */
+/* GL samplers                                                                             */
+/* ------------------------------------------------------------------------------------- */
+struct Inputs {
+  const float* field;      /* encoded RGBA, n[0]*n[1]*n[2]*4 (already at storage precision) */
+  int n[3];
+  float slice_dist[3];
+  const uint8_t* noise;    /* noise_channels per voxel: 1 (value) or 4 (gradient xyz, value) */
+  int m[3];
+  int noise_channels;
+  const float* scalar;     /* optional, sn[0]*sn[1]*sn[2] */
+  int sn[3];
+  const float* tf_rgba;    /* 256*4 */
+  const float* tf_opac;    /* 256 */
+  const double* taps;      /* L_b + L_f + 1 kernel weights */
+  double inv_filter_area;
+};
+
+/* LINEAR + CLAMP_TO_EDGE trilinear at texture coordinate s (GL 2.1 eq. 3.23/3.27). */
+template <class R> static inline V4<R> tex3d_field(const Inputs& in, V3<R> s) {
+  const int* n = in.n;
+  R u[3] = {s.x * R(n[0]) - R(0.5), s.y * R(n[1]) - R(0.5), s.z * R(n[2]) - R(0.5)};
+  int i0[3], i1[3];
+  R a[3];
+  for (int d = 0; d < 3; ++d) {
+    R uc = u[d];
+    if (!(uc > R(-1))) uc = R(-1); /* below -1 (or NaN) both texels clamp to 0 */
+    if (uc > R(n[d])) uc = R(n[d]);
+    R fl = std::floor(uc);
+    a[d] = uc - fl;
+    int b = (int)fl;
+    i0[d] = std::min(std::max(b, 0), n[d] - 1);
+    i1[d] = std::min(std::max(b + 1, 0), n[d] - 1);
+  }
+  V4<R> r{R(0), R(0), R(0), R(0)};
+  for (int c = 0; c < 8; ++c) {
+    int xi = (c & 1) ? i1[0] : i0[0], yi = (c & 2) ? i1[1] : i0[1], zi = (c & 4) ? i1[2] : i0[2];
+    R w = ((c & 1) ? a[0] : R(1) - a[0]) * ((c & 2) ? a[1] : R(1) - a[1]) * ((c & 4) ? a[2] : R(1) - a[2]);
+    const float* t = in.field + 4 * (((size_t)zi * n[1] + yi) * n[0] + xi);
+    r.x += w * R(t[0]);
+    r.y += w * R(t[1]);
+    r.z += w * R(t[2]);
+    r.w += w * R(t[3]);
+  }
+  return r;
+}
+
+template <class R> static inline R tex3d_scalar(const Inputs& in, V3<R> s) {
+  const int* n = in.sn;
+  R u[3] = {s.x * R(n[0]) - R(0.5), s.y * R(n[1]) - R(0.5), s.z * R(n[2]) - R(0.5)};
+  int i0[3], i1[3];
+  R a[3];
+  for (int d = 0; d < 3; ++d) {
+    R uc = u[d];
+    if (!(uc > R(-1))) uc = R(-1);
+    if (uc > R(n[d])) uc = R(n[d]);
+    R fl = std::floor(uc);
+    a[d] = uc - fl;
+    int b = (int)fl;
+    i0[d] = std::min(std::max(b, 0), n[d] - 1);
+    i1[d] = std::min(std::max(b + 1, 0), n[d] - 1);
+  }
+  R r = R(0);
+  for (int c = 0; c < 8; ++c) {
+    int xi = (c & 1) ? i1[0] : i0[0], yi = (c & 2) ? i1[1] : i0[1], zi = (c & 4) ? i1[2] : i0[2];
+    R w = ((c & 1) ? a[0] : R(1) - a[0]) * ((c & 2) ? a[1] : R(1) - a[1]) * ((c & 4) ? a[2] : R(1) - a[2]);
+    r += w * R(in.scalar[((size_t)zi * n[1] + yi) * n[0] + xi]);
+  }
+  return r;
+}
+
+/* LINEAR + REPEAT trilinear of the uint8 noise; returns RGBA/255 (value in .w; for a
+ * one-channel noise the gradient part is 0). */
+template <class R> static inline V4<R> tex3d_noise(const Inputs& in, V3<R> s) {
+  const int* m = in.m;
+  R u[3] = {s.x * R(m[0]) - R(0.5), s.y * R(m[1]) - R(0.5), s.z * R(m[2]) - R(0.5)};
+  int i0[3], i1[3];
+  R a[3];
+  for (int d = 0; d < 3; ++d) {
+    R uc = u[d];
+    if (!(uc > R(-16777216))) uc = R(-16777216);
+    if (uc > R(16777216)) uc = R(16777216);
+    R fl = std::floor(uc);
+    a[d] = uc - fl;
+    long long b = (long long)fl;
+    long long md = m[d];
+    i0[d] = (int)(((b % md) + md) % md);
+    i1[d] = (int)((((b + 1) % md) + md) % md);
+  }
+  V4<R> r{R(0), R(0), R(0), R(0)};
+  const int ch = in.noise_channels;
+  for (int c = 0; c < 8; ++c) {
+    int xi = (c & 1) ? i1[0] : i0[0], yi = (c & 2) ? i1[1] : i0[1], zi = (c & 4) ? i1[2] : i0[2];
+    R w = ((c & 1) ? a[0] : R(1) - a[0]) * ((c & 2) ? a[1] : R(1) - a[1]) * ((c & 4) ? a[2] : R(1) - a[2]);
+    const uint8_t* t = in.noise + (size_t)ch * (((size_t)zi * m[1] + yi) * m[0] + xi);
+    if (ch == 4) {
+      r.x += w * R(t[0]);
+      r.y += w * R(t[1]);
+      r.z += w * R(t[2]);
+      r.w += w * R(t[3]);
+    } else {
+      r.w += w * R(t[0]);
+    }
+  }
+  R k = R(1) / R(255);
+  return V4<R>{r.x * k, r.y * k, r.z * k, r.w * k};
+}
+
+/* 1D LINEAR + CLAMP_TO_EDGE lookup in a 256-entry float table with `stride` channels. */
+template <class R> static inline R tex1d(const float* t, int stride, int ch, R s) {
+  const int N = VVLIC_TF_ENTRIES;
+  R u = s * R(N) - R(0.5);
+  if (!(u > R(-1))) u = R(-1);
+  if (u > R(N)) u = R(N);
+  R fl = std::floor(u);
+  R a = u - fl;
+  int b = (int)fl;
+  int i0 = std::min(std::max(b, 0), N - 1), i1 = std::min(std::max(b + 1, 0), N - 1);
+  return (R(1) - a) * R(t[i0 * stride + ch]) + a * R(t[i1 * stride + ch]);
+}
+
+/* ------------------------------------------------------------------------------------- */
+/* uniforms: setRenderVolParams (renderer.cpp:925-996)                                     */
+/* ------------------------------------------------------------------------------------- */
+template <class R> struct Uniforms {
+  R tex_max[3], scale_vol[3], scale_vol_inv[3], extent[3];
+  R step_size, gradient_scale, illum_scale, freq_scale;
+  int num_iterations, lf, lb;
+  R h, h_eff, alpha_correction, intensity_scale;
+};
+
+template <class R> static inline Uniforms<R> uniforms(const Inputs& in, const vvlic_params& p) {
+  Geometry g = geometry(in.n, in.slice_dist);
+  Uniforms<R> u;
+  bool bug = (p.quirks & VVLIC_QUIRK_UNIFORM_SCALE_BUG) && p.illum != VVLIC_ILLUM_NONE;
+  for (int i = 0; i < 3; ++i) {
+    u.tex_max[i] = R(g.tex_max[i]);
+    u.extent[i] = R(g.extent[i]);
+    u.scale_vol[i] = R(bug ? g.scale_inv[i] : g.scale[i]);
+    u.scale_vol_inv[i] = R(bug ? 0.0 : g.scale_inv[i]);
+  }
+  if (p.low_res) {
+    u.step_size = R(2.0f * p.step_size_vol);
+    u.freq_scale = R(0.7f * p.freq_scale);
+    u.lf = 15;
+    u.lb = 15;
+    u.h = R(1.0f / 64.0f);
+    u.alpha_correction = R(2.0f * p.step_size_vol * 128.0f);
+  } else {
+    u.step_size = R(p.step_size_vol);
+    u.freq_scale = R(p.freq_scale);
+    u.lf = p.steps_forward;
+    u.lb = p.steps_backward;
+    u.h = R(p.step_size_lic);
+    u.alpha_correction = R(p.step_size_vol * 128.0f);
+  }
+  u.gradient_scale = R(p.gradient_scale);
+  u.illum_scale = R(p.illum_scale);
+  u.num_iterations = p.num_iterations;
+  u.h_eff = u.h * R(p.eye_dist_factor);
+  u.intensity_scale = R(in.inv_filter_area) / R(u.lf + u.lb) * u.gradient_scale;
+  return u;
+}
+
+/* ------------------------------------------------------------------------------------- */
+/* view: per-pixel ray coefficients (camera.cpp:56-67, renderer.cpp:146)                    */
+/* c[0..2] o0, c[3..5] o1, c[6..8] o2, c[9..11] d0, c[12..14] d1, c[15..17] d2, c[18] clamp */
+/* ------------------------------------------------------------------------------------- */
+static inline void view_rays(const vvlic_view& v, const int n[3], const float sd[3], int W, int H, double* c) {
+  Geometry g = geometry(n, sd);
+  for (int i = 0; i < 21; ++i) c[i] = 0.0;
+  if (v.projection == VVLIC_ORTHOGRAPHIC) {
+    for (int i = 0; i < 3; ++i) {
+      c[0 + i] = (double)v.ortho_center[i] - v.ortho_right[i] - v.ortho_up[i];
+      c[3 + i] = 2.0 * v.ortho_right[i] / W;
+      c[6 + i] = 2.0 * v.ortho_up[i] / H;
+      c[9 + i] = v.ortho_dir[i];
+    }
+    c[18] = 0.0;
+    return;
+  }
+  double qx = v.quat[0], qy = v.quat[1], qz = v.quat[2], qw = v.quat[3];
+  double qn = std::sqrt(qx * qx + qy * qy + qz * qz + qw * qw);
+  if (qn > 0) { qx /= qn; qy /= qn; qz /= qn; qw /= qn; } else { qw = 1; }
+  /* rotation matrix of q (glRotatef(2 acos(w), axis), mmath.cpp:213-232) */
+  double Rm[3][3] = {{1 - 2 * (qy * qy + qz * qz), 2 * (qx * qy - qz * qw), 2 * (qx * qz + qy * qw)},
+                     {2 * (qx * qy + qz * qw), 1 - 2 * (qx * qx + qz * qz), 2 * (qy * qz - qx * qw)},
+                     {2 * (qx * qz - qy * qw), 2 * (qy * qz + qx * qw), 1 - 2 * (qx * qx + qy * qy)}};
+  auto rt = [&](const double e[3], double* out) { /* R^T e */
+    for (int i = 0; i < 3; ++i) out[i] = Rm[0][i] * e[0] + Rm[1][i] * e[1] + Rm[2][i] * e[2];
+  };
+  /* eye = MV^-1 (0,0,0,1) with MV = T(pan) T(0,0,-dist) R T(-center) */
+  double e_eye[3] = {-(double)v.pan[0], -(double)v.pan[1], (double)v.distance - v.pan[2]};
+  double eo[3];
+  rt(e_eye, eo);
+  for (int i = 0; i < 3; ++i) c[i] = eo[i] + g.center[i];
+  double aspect = v.aspect > 0 ? (double)v.aspect : (double)W / (double)H;
+  double t = std::tan((double)v.fovy_deg * M_PI / 360.0);
+  double d0[3] = {-aspect * t, -t, -1.0}, d1[3] = {2.0 * aspect * t / W, 0.0, 0.0}, d2[3] = {0.0, 2.0 * t / H, 0.0};
+  rt(d0, c + 9);
+  rt(d1, c + 12);
+  rt(d2, c + 15);
+  c[18] = 1.0;
+}
+
+/* Slab test against [0, extent]: returns false for a miss; t_entry on hit. */
+template <class R> static inline bool ray_entry(const R o[3], const R d[3], const R ext[3], bool clamp0, R* t_entry) {
+  R tn = -INFINITY, tf = INFINITY;
+  for (int i = 0; i < 3; ++i) {
+    if (d[i] == R(0)) {
+      if (o[i] < R(0) || o[i] > ext[i]) return false;
+      continue;
+    }
+    R inv = R(1) / d[i];
+    R t0 = (R(0) - o[i]) * inv, t1 = (ext[i] - o[i]) * inv;
+    if (t0 > t1) std::swap(t0, t1);
+    tn = std::max(tn, t0);
+    tf = std::min(tf, t1);
+  }
+  if (!(tn < tf)) return false;
+  if (clamp0) {
+    if (!(tf > R(0))) return false;
+    tn = std::max(tn, R(0));
+  }
+  *t_entry = tn;
+  return true;
+}
+
+/* ------------------------------------------------------------------------------------- */
+/* LIC: computeLIC / singleLICstep (inc_lic.glsl:134-265)                                  */
+/* ------------------------------------------------------------------------------------- */
+template <class R> struct LicCtx {
+  const Inputs* in;
+  const vvlic_params* p;
+  const Uniforms<R>* u;
+  bool grad;      /* USE_NOISE_GRADIENTS (ILLUM_GRADIENT) */
+};
+
+/* freqSampling (inc_lic.glsl:134-153) / freqSamplingGrad (:124-131) */
+template <class R> static inline V4<R> noise_tap(const LicCtx<R>& c, V3<R> p) {
+  const Inputs& in = *c.in;
+  if (c.grad) {
+    bool nofreq = (c.p->quirks & VVLIC_QUIRK_GRAD_NOISE_NO_FREQ) != 0;
+    return tex3d_noise<R>(in, nofreq ? p : p * c.u->freq_scale);
+  }
+  if (c.p->scalar_gate && in.scalar) {
+    R s = tex3d_scalar<R>(in, p);
+    if (!(s > R(c.p->gate_lo) && s < R(c.p->gate_hi))) return V4<R>{R(0), R(0), R(0), R(0)};
+  }
+  if (c.p->quirks & VVLIC_QUIRK_LUMINANCE_NOISE) return V4<R>{R(0), R(0), R(0), R(1)};
+  V4<R> n = tex3d_noise<R>(in, p * c.u->freq_scale);
+  return V4<R>{R(0), R(0), R(0), n.w};
+}
+
+template <class R> static inline V3<R> slope(V4<R> f) {
+  return V3<R>{R(2) * f.x - R(1), R(2) * f.y - R(1), R(2) * f.z - R(1)};
+}
+
+/* One streamline step from p with current field value `step` in direction dirs (+-1).
+ * Returns the new position and replaces `step` with the field there. */
+template <class R> static inline V3<R> lic_step(const LicCtx<R>& c, V3<R> p, V4<R>& step, R dirs) {
+  const Inputs& in = *c.in;
+  R h = c.u->h_eff;
+  R sof = c.p->speed_of_flow ? step.w : R(1);
+  V3<R> k1 = slope(step) * dirs * sof * h; /* licdir (inc_lic.glsl:243/257, 172, 177) */
+  int integ = c.p->integrator;
+  if (integ == VVLIC_EULER) {
+    p = p + k1;
+  } else if (integ == VVLIC_HEUN) {
+    V3<R> p2 = p + k1;
+    V3<R> k2 = slope(tex3d_field<R>(in, p2)) * dirs * sof * h;
+    p = p + (k1 + k2) * R(0.5);
+  } else {
+    V3<R> k2 = slope(tex3d_field<R>(in, p + k1 * R(0.5))) * dirs * sof * h;
+    V3<R> k3 = slope(tex3d_field<R>(in, p + k2 * R(0.5))) * dirs * sof * h;
+    V3<R> k4 = slope(tex3d_field<R>(in, p + k3)) * dirs * sof * h;
+    p = p + (k1 + k2 * R(2) + k3 * R(2) + k4) * (R(1) / R(6));
+  }
+  step = tex3d_field<R>(in, p);
+  return p;
+}
+
+/* computeLIC: returns (sum w*grad_enc.xyz, sum w*noise) */
+template <class R> static inline V4<R> compute_lic(const LicCtx<R>& c, V3<R> pos, V4<R> f0) {
+  const double* w = c.in->taps;
+  const int lb = c.u->lb, lf = c.u->lf;
+  V4<R> n0 = noise_tap<R>(c, pos);
+  R w0 = R(w[lb]);
+  V4<R> acc{n0.x * w0, n0.y * w0, n0.z * w0, n0.w * w0};
+  for (int half = 0; half < 2; ++half) {
+    R dirs = half == 0 ? R(-1) : R(1);
+    int L = half == 0 ? lb : lf;
+    V3<R> p = pos;
+    V4<R> step = f0;
+    for (int i = 1; i <= L; ++i) {
+      p = lic_step<R>(c, p, step, dirs);
+      V4<R> n = noise_tap<R>(c, p);
+      R wi = R(w[half == 0 ? lb - i : lb + i]);
+      acc.x += n.x * wi;
+      acc.y += n.y * wi;
+      acc.z += n.z * wi;
+      acc.w += n.w * wi;
+    }
+  }
+  return acc;
+}
+
+/* ------------------------------------------------------------------------------------- */
+/* shading: illumLIC (inc_illum.glsl:257-271), illumGradient (:100-140)                    */
+/* ------------------------------------------------------------------------------------- */
+template <class R> static inline R alpha_correct(R a, R corr) {
+  R base = R(1) - a;
+  if (base < R(0)) base = R(0);
+  return R(1) - std::pow(base, corr);
+}
+
+template <class R> static inline V4<R> shade(const LicCtx<R>& c, V4<R> illum, V4<R> tf, V3<R> pos, V3<R> dir) {
+  const Uniforms<R>& u = *c.u;
+  const vvlic_params& p = *c.p;
+  V4<R> col;
+  R I = illum.w;
+  if (p.illum == VVLIC_ILLUM_GRADIENT) {
+    V3<R> lp{R(p.light_pos[0]), R(p.light_pos[1]), R(p.light_pos[2])};
+    V3<R> sv{u.scale_vol_inv[0], u.scale_vol_inv[1], u.scale_vol_inv[2]};
+    V3<R> L = normalize(lp - mul(pos, sv));
+    V3<R> V = normalize(dir * R(-1));
+    V3<R> N = normalize(V3<R>{-illum.x, -illum.y, -illum.z});
+    V3<R> Rf = normalize(N * (R(2) * dot(L, N)) - L);
+    R s = clamp01(dot(Rf, V));
+    s = std::pow(s, R(p.spec_exp));
+    V3<R> spec = V3<R>{R(p.light_specular[0]), R(p.light_specular[1]), R(p.light_specular[2])} * (s * I);
+    R dfac = clamp01(dot(L, N));
+    V3<R> diff = V3<R>{R(p.light_diffuse[0]), R(p.light_diffuse[1]), R(p.light_diffuse[2])} * (dfac * u.illum_scale);
+    V3<R> amb{R(p.light_ambient[0]), R(p.light_ambient[1]), R(p.light_ambient[2])};
+    V3<R> base{tf.x * I, tf.y * I, tf.z * I};
+    V3<R> lit = mul(base, diff + V3<R>{R(0.3), R(0.3), R(0.3)} + amb) + spec;
+    lit = lit * u.illum_scale;
+    col.x = lit.x;
+    col.y = lit.y;
+    col.z = lit.z;
+  } else {
+    col.x = I * tf.x * u.illum_scale;
+    col.y = I * tf.y * u.illum_scale;
+    col.z = I * tf.z * u.illum_scale;
+  }
+  R a = tex1d<R>(c.in->tf_opac, 1, 0, I * R(1.3)) * tf.w;
+  col.w = alpha_correct<R>(a, u.alpha_correction);
+  return col;
+}
+
+/* ------------------------------------------------------------------------------------- */
+/* the ray: lic3d_fragment.glsl:5-99                                                       */
+/* ------------------------------------------------------------------------------------- */
+template <class R> static inline uint32_t render_pixel(const Inputs& in, const vvlic_params& p, const Uniforms<R>& u,
+                                                       const double* rc, int px, int py, float out[4]) {
+  out[0] = out[1] = out[2] = out[3] = 0.0f;
+  R o[3], d[3], ext[3];
+  R uu = R(px) + R(0.5), vv = R(py) + R(0.5);
+  for (int i = 0; i < 3; ++i) {
+    o[i] = R(rc[0 + i]) + uu * R(rc[3 + i]) + vv * R(rc[6 + i]);
+    d[i] = R(rc[9 + i]) + uu * R(rc[12 + i]) + vv * R(rc[15 + i]);
+    ext[i] = u.extent[i];
+  }
+  R te;
+  if (!ray_entry<R>(o, d, ext, rc[18] != 0.0, &te)) return 0;
+  V3<R> sv{u.scale_vol[0], u.scale_vol[1], u.scale_vol[2]};
+  V3<R> obj{o[0] + te * d[0], o[1] + te * d[1], o[2] + te * d[2]};
+  V3<R> pos = mul(obj, sv);
+  V3<R> dir = mul(normalize(V3<R>{d[0], d[1], d[2]}), sv);
+  LicCtx<R> c{&in, &p, &u, p.illum == VVLIC_ILLUM_GRADIENT};
+  V4<R> dest{R(0), R(0), R(0), R(0)}, src{R(0), R(0), R(0), R(0)};
+  uint32_t samples = 0;
+  bool outside = false;
+  const R thr = R(p.alpha_threshold);
+  for (int j = 0; !outside && j < u.num_iterations; ++j) {
+    for (int i = 0; i < u.num_iterations; ++i) {
+      V4<R> f = tex3d_field<R>(in, pos);
+      R idx = p.tf_index == VVLIC_TF_INDEX_MAGNITUDE ? f.w : f.z;
+      V4<R> tf{tex1d<R>(in.tf_rgba, 4, 0, idx), tex1d<R>(in.tf_rgba, 4, 1, idx), tex1d<R>(in.tf_rgba, 4, 2, idx),
+               tex1d<R>(in.tf_rgba, 4, 3, idx)};
+      V4<R> il = compute_lic<R>(c, pos, f);
+      ++samples;
+      il.w *= u.intensity_scale;
+      src = shade<R>(c, il, tf, pos, dir);
+      src.x *= src.w;
+      src.y *= src.w;
+      src.z *= src.w;
+      R om = R(1) - dest.w;
+      dest.x = clamp01(om * src.x + dest.x);
+      dest.y = clamp01(om * src.y + dest.y);
+      dest.z = clamp01(om * src.z + dest.z);
+      dest.w = clamp01(om * src.w + dest.w);
+      pos = pos + dir * u.step_size;
+      outside = pos.x < R(0) || pos.y < R(0) || pos.z < R(0) || pos.x > u.tex_max[0] || pos.y > u.tex_max[1] ||
+                pos.z > u.tex_max[2] || src.w > thr;
+      if (outside) break;
+    }
+  }
+  out[0] = (float)dest.x;
+  out[1] = (float)dest.y;
+  out[2] = (float)dest.z;
+  out[3] = (float)dest.w;
+  return samples;
+}
+
+/* Render the rows listed in `rows` (all rows when rows == NULL) into out (nrows x W x 4). */
+template <class R> static inline void render(const Inputs& in, const vvlic_params& p, const double* rc, int W, int H,
+                                             const int32_t* rows, int nrows, float* out, uint32_t* samples,
+                                             int threads) {
+  Uniforms<R> u = uniforms<R>(in, p);
+  int nr = rows ? nrows : H;
+#if defined(_OPENMP)
+  if (threads > 0) omp_set_num_threads(threads);
+#pragma omp parallel for schedule(dynamic, 1)
+#endif
+  for (int r = 0; r < nr; ++r) {
+    int py = rows ? rows[r] : r;
+    for (int px = 0; px < W; ++px) {
+      uint32_t s = render_pixel<R>(in, p, u, rc, px, py, out + 4 * ((size_t)r * W + px));
+      if (samples) samples[(size_t)r * W + px] = s;
+    }
+  }
+  (void)threads;
+}
+
+}  // namespace vvo
+
+#endif  // VVLIC_ORACLE_HPP_

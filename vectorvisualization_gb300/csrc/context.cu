@@ -1,0 +1,665 @@
+// C ABI of libvvlic: context, uploads, tables, parameters, view and the render entry points.
+//
+// The host side derives everything the reference computes on the CPU per frame
+// (Renderer::setRenderVolParams renderer.cpp:925-996, the view of Camera::setCamera
+// camera.cpp:56-67, the filter-kernel lookups of computeLIC inc_lic.glsl:219-262) and hands it
+// to the kernels as one by-value argument block.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/vvlic.h"
+#include "vvlic_device.cuh"
+#include "vvlic_host.hpp"
+#include "vvlic_launch.hpp"
+
+using namespace vvlic;
+
+// ------------------------------------------------------------------------------------------
+// helpers
+// ------------------------------------------------------------------------------------------
+namespace vvlic {
+
+vvlic_status fail(vvlic_ctx* c, vvlic_status s, const char* fmt, ...) {
+  if (c) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    c->err = buf;
+  }
+  return s;
+}
+
+vvlic_status cuda_fail(vvlic_ctx* c, cudaError_t e, const char* what) {
+  if (e == cudaErrorMemoryAllocation)
+    return fail(c, VVLIC_ERR_OUT_OF_MEMORY, "%s: %s", what, cudaGetErrorString(e));
+  return fail(c, VVLIC_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+// VectorDataSet::loadData geometry (dataset.cpp:139-176), in float like the reference.
+Geometry make_geometry(const int n[3], const float* sd_in) {
+  Geometry g;
+  float sd[3] = {1.f, 1.f, 1.f};
+  if (sd_in)
+    for (int i = 0; i < 3; ++i) sd[i] = sd_in[i];
+  float max_vol = 0.f;
+  int max_tex = 0;
+  for (int i = 0; i < 3; ++i) {
+    max_vol = std::max(max_vol, (float)n[i] * sd[i]);
+    max_tex = std::max(max_tex, n[i]);
+  }
+  for (int i = 0; i < 3; ++i) {
+    g.slice_dist[i] = sd[i];
+    g.scale[i] = (float)max_tex / ((float)n[i] * sd[i]);
+    g.scale_inv[i] = (float)n[i] * sd[i] / (float)max_tex;
+    g.extent[i] = (float)n[i] * sd[i] / max_vol;
+    g.center[i] = g.extent[i] / 2.0f;
+    g.tex_max[i] = g.extent[i] * g.scale[i];
+  }
+  return g;
+}
+
+static int next_pow2(int w) {
+  int p = 1;
+  while (p < w) p <<= 1;
+  return p;
+}
+
+// texture1D(licKernelSampler, s).r with LINEAR filtering and GL_CLAMP (zero border) or
+// CLAMP_TO_EDGE over a LUMINANCE8 table (dataset.cpp:1470-1500).
+static double kernel_lookup(const uint8_t* t, int W, double s, int clamp_mode) {
+  s = std::min(std::max(s, 0.0), 1.0);
+  double u = s * W - 0.5, fl = std::floor(u), a = u - fl;
+  int i0 = (int)fl;
+  auto tex = [&](int i) -> double {
+    if (clamp_mode == VVLIC_KERNEL_CLAMP_EDGE) i = std::min(std::max(i, 0), W - 1);
+    else if (i < 0 || i >= W) return 0.0;
+    return t[i] / 255.0;
+  };
+  return (1.0 - a) * tex(i0) + a * tex(i0 + 1);
+}
+
+// Effective LIC lengths: the low-resolution preview substitutes 15/15 (renderer.cpp:956-962).
+static void effective_steps(const vvlic_params& p, int* lb, int* lf) {
+  *lb = p.low_res ? 15 : p.steps_backward;
+  *lf = p.low_res ? 15 : p.steps_forward;
+}
+
+// Tap weights w[j], j = -L_b..L_f, at the offsets computeLIC walks (inc_lic.glsl:219-262).
+vvlic_status derive_taps(const vvlic_ctx* c, int lb, int lf, float* taps, float* inv_area) {
+  if (c->taps_override) {
+    if (c->taps_lb != lb || c->taps_lf != lf) return VVLIC_ERR_INVALID_ARGUMENT;
+    for (int i = 0; i < lb + lf + 1; ++i) taps[i] = c->taps[i];
+    *inv_area = c->taps_inv_area;
+    return VVLIC_OK;
+  }
+  const uint8_t* t = c->filter;
+  const int W = c->filter_width;
+  taps[lb] = (float)kernel_lookup(t, W, 0.5, c->filter_clamp);
+  double off = 0.5, kb = lb > 0 ? 0.5 / lb : 0.0, kf = lf > 0 ? 0.5 / lf : 0.0;
+  for (int i = 1; i <= lb; ++i) {
+    off -= kb;
+    taps[lb - i] = (float)kernel_lookup(t, W, off, c->filter_clamp);
+  }
+  off = 0.5;
+  for (int i = 1; i <= lf; ++i) {
+    off += kf;
+    taps[lb + i] = (float)kernel_lookup(t, W, off, c->filter_clamp);
+  }
+  if (c->filter_is_box) {
+    *inv_area = 0.5f;  // LICFilter::createBoxFilter (dataset.cpp:1412)
+  } else {
+    float area = 0.0f;  // calcFilterKernelInvArea (dataset.cpp:1503-1512)
+    for (int i = 0; i < W; ++i) area += t[i];
+    *inv_area = 0.5f * W * 255.0f / area;
+  }
+  return VVLIC_OK;
+}
+
+// Rays of the view for a volume (camera.cpp:56-67 followed by glTranslatef(-center),
+// renderer.cpp:146): origin/direction as affine functions of the pixel centre.
+void derive_rays(const vvlic_view& v, const Geometry& g, int W, int H, double* c) {
+  for (int i = 0; i < 21; ++i) c[i] = 0.0;
+  if (v.projection == VVLIC_ORTHOGRAPHIC) {
+    for (int i = 0; i < 3; ++i) {
+      c[i] = (double)v.ortho_center[i] - v.ortho_right[i] - v.ortho_up[i];
+      c[3 + i] = 2.0 * v.ortho_right[i] / W;
+      c[6 + i] = 2.0 * v.ortho_up[i] / H;
+      c[9 + i] = v.ortho_dir[i];
+    }
+    return;
+  }
+  double x = v.quat[0], y = v.quat[1], z = v.quat[2], w = v.quat[3];
+  double qn = std::sqrt(x * x + y * y + z * z + w * w);
+  if (qn > 0) {
+    x /= qn;
+    y /= qn;
+    z /= qn;
+    w /= qn;
+  } else {
+    w = 1.0;
+  }
+  // R(q); object-space vectors are R^T times eye-space vectors
+  const double R[3][3] = {{1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)},
+                          {2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)},
+                          {2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)}};
+  auto to_obj = [&](double ex, double ey, double ez, double* out) {
+    for (int i = 0; i < 3; ++i) out[i] = R[0][i] * ex + R[1][i] * ey + R[2][i] * ez;
+  };
+  double eye[3];
+  to_obj(-(double)v.pan[0], -(double)v.pan[1], (double)v.distance - v.pan[2], eye);
+  for (int i = 0; i < 3; ++i) c[i] = eye[i] + g.center[i];
+  const double aspect = v.aspect > 0 ? (double)v.aspect : (double)W / H;
+  const double t = std::tan((double)v.fovy_deg * M_PI / 360.0);  // gluPerspective(fovy, ...)
+  to_obj(-aspect * t, -t, -1.0, c + 9);
+  to_obj(2.0 * aspect * t / W, 0.0, 0.0, c + 12);
+  to_obj(0.0, 2.0 * t / H, 0.0, c + 15);
+  c[18] = 1.0;
+}
+
+}  // namespace vvlic
+
+// ------------------------------------------------------------------------------------------
+// defaults
+// ------------------------------------------------------------------------------------------
+extern "C" void vvlic_params_default(vvlic_params* p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof *p);
+  p->step_size_vol = 1.0f / 128.0f;  // LICParams() (types.h:91-99)
+  p->gradient_scale = 30.0f;
+  p->illum_scale = 1.0f;
+  p->freq_scale = 1.0f;
+  p->num_iterations = 255;
+  p->steps_forward = 32;
+  p->steps_backward = 32;
+  p->step_size_lic = 0.01f;
+  p->integrator = VVLIC_HEUN;
+  p->illum = VVLIC_ILLUM_NONE;
+  p->tf_index = VVLIC_TF_INDEX_DIR_Z;
+  p->gate_lo = 0.1f;
+  p->gate_hi = 0.3f;
+  p->eye_dist_factor = 0.3f;
+  p->alpha_threshold = 0.95f;
+  p->quirks = VVLIC_QUIRKS_REFERENCE;
+  p->light_pos[0] = 0.5f;
+  p->light_pos[1] = 0.5f;
+  p->light_pos[2] = 1.5f;
+  p->spec_exp = 40.0f;
+  for (int i = 0; i < 3; ++i) {
+    p->light_diffuse[i] = 1.0f;
+    p->light_specular[i] = 1.0f;
+    p->light_ambient[i] = 0.0f;
+  }
+  p->sampler = VVLIC_SAMPLER_CELL;
+}
+
+extern "C" void vvlic_view_default(vvlic_view* v) {
+  if (!v) return;
+  std::memset(v, 0, sizeof *v);
+  v->projection = VVLIC_PERSPECTIVE;
+  v->quat[3] = 1.0f;
+  v->distance = 4.0f;
+  v->fovy_deg = 35.0f;
+  v->ortho_center[0] = v->ortho_center[1] = 0.5f;
+  v->ortho_right[0] = 0.5f;
+  v->ortho_up[1] = 0.5f;
+  v->ortho_dir[2] = 1.0f;
+}
+
+extern "C" const char* vvlic_status_string(vvlic_status s) {
+  switch (s) {
+    case VVLIC_OK: return "ok";
+    case VVLIC_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case VVLIC_ERR_OUT_OF_MEMORY: return "out of memory";
+    case VVLIC_ERR_CUDA: return "CUDA error";
+    case VVLIC_ERR_NO_DEVICE: return "no CUDA device";
+    case VVLIC_ERR_NOT_READY: return "input not set";
+    case VVLIC_ERR_TIMEOUT: return "device wait timed out";
+    case VVLIC_ERR_UNSUPPORTED: return "unsupported";
+    case VVLIC_ERR_BAD_HANDLE: return "bad handle";
+    case VVLIC_ERR_IO: return "I/O error";
+    case VVLIC_ERR_FORMAT: return "format error";
+    default: return "unknown status";
+  }
+}
+
+extern "C" int32_t vvlic_abi_version(void) { return VVLIC_ABI_VERSION; }
+
+extern "C" vvlic_status vvlic_make_filter_table(int32_t filter, int32_t width, uint8_t* out, int32_t* out_width) {
+  if (!out || !out_width || width < 2 || width > 1024) return VVLIC_ERR_INVALID_ARGUMENT;
+  const int W = next_pow2(width);
+  if (W > 1024) return VVLIC_ERR_INVALID_ARGUMENT;
+  for (int i = 0; i < W; ++i) {
+    const double t = (i + 0.5) / W;  // texel centre in [0,1]; 0.5 is the streamline centre
+    const double d = 2.0 * t - 1.0;  // in [-1, 1]
+    double v;
+    switch (filter) {
+      case VVLIC_FILTER_BOX: v = 1.0; break;
+      case VVLIC_FILTER_TRIANGLE: v = 1.0 - std::fabs(d); break;
+      case VVLIC_FILTER_COS2: v = std::cos(M_PI * d / 2.0) * std::cos(M_PI * d / 2.0); break;
+      case VVLIC_FILTER_GAUSSIAN: v = std::exp(-4.5 * d * d); break;  // sigma = L/3 in tap units
+      default: return VVLIC_ERR_INVALID_ARGUMENT;
+    }
+    out[i] = (uint8_t)std::lround(std::min(std::max(v, 0.0), 1.0) * 255.0);
+  }
+  *out_width = W;
+  return VVLIC_OK;
+}
+
+// ------------------------------------------------------------------------------------------
+// context
+// ------------------------------------------------------------------------------------------
+static void default_tables(vvlic_ctx* c) {
+  // TransferEdit(): rgb identity, alpha and opacity max(0, i-20) (transferEdit.cpp:76-82)
+  for (int i = 0; i < VVLIC_TF_ENTRIES; ++i) {
+    for (int ch = 0; ch < 3; ++ch) c->tf[4 * i + ch] = (float)i / 255.0f;
+    c->tf[4 * i + 3] = (float)(i < 20 ? 0 : i - 20) / 255.0f;
+    c->tf[4 * VVLIC_TF_ENTRIES + i] = (float)(i < 20 ? 0 : i - 20) / 255.0f;
+  }
+  // LICFilter::createBoxFilter(256) (dataset.cpp:1405-1413), GL_CLAMP
+  int w = 0;
+  vvlic_make_filter_table(VVLIC_FILTER_BOX, 256, c->filter, &w);
+  c->filter_width = w;
+  c->filter_clamp = VVLIC_KERNEL_CLAMP_BORDER;
+  c->filter_is_box = true;
+}
+
+extern "C" vvlic_status vvlic_create(vvlic_ctx** out, int32_t device) {
+  if (!out) return VVLIC_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  int count = 0;
+  cudaError_t e = cudaGetDeviceCount(&count);
+  if (e != cudaSuccess || count == 0) return VVLIC_ERR_NO_DEVICE;
+  if (device < 0 || device >= count) return VVLIC_ERR_INVALID_ARGUMENT;
+  vvlic_ctx* c = new vvlic_ctx();
+  c->device = device;
+  vvlic_params_default(&c->params);
+  vvlic_view_default(&c->view);
+  default_tables(c);
+  DeviceGuard g(device);
+  if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaMalloc(&c->d_tf, sizeof(float) * 5 * VVLIC_TF_ENTRIES)) != cudaSuccess ||
+      (e = cudaMalloc(&c->d_counters, sizeof(unsigned long long) * 4)) != cudaSuccess ||
+      (e = cudaMalloc(&c->d_scratch_word, sizeof(unsigned) * 4)) != cudaSuccess ||
+      (e = cudaEventCreate(&c->ev0)) != cudaSuccess || (e = cudaEventCreate(&c->ev1)) != cudaSuccess ||
+      (e = cudaMemcpy(c->d_tf, c->tf, sizeof(float) * 5 * VVLIC_TF_ENTRIES, cudaMemcpyHostToDevice)) != cudaSuccess) {
+    vvlic_destroy(c);
+    return e == cudaErrorMemoryAllocation ? VVLIC_ERR_OUT_OF_MEMORY : VVLIC_ERR_CUDA;
+  }
+  *out = c;
+  return VVLIC_OK;
+}
+
+static void free_volume(Volume& v) {
+  if (v.tex) cudaDestroyTextureObject(v.tex);
+  if (v.array) cudaFreeArray(v.array);
+  if (v.d_texels) cudaFree(v.d_texels);
+  if (v.d_cells) cudaFree(v.d_cells);
+  v = Volume();
+}
+
+static void free_noise(NoiseTex& n) {
+  if (n.d_texels) cudaFree(n.d_texels);
+  if (n.d_cells) cudaFree(n.d_cells);
+  n = NoiseTex();
+}
+
+extern "C" vvlic_status vvlic_destroy(vvlic_ctx* c) {
+  if (!c) return VVLIC_ERR_BAD_HANDLE;
+  DeviceGuard g(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  for (auto& kv : c->vols) free_volume(kv.second);
+  free_noise(c->noise);
+  if (c->d_scalar) cudaFree(c->d_scalar);
+  if (c->d_tf) cudaFree(c->d_tf);
+  if (c->d_counters) cudaFree(c->d_counters);
+  if (c->d_scratch_word) cudaFree(c->d_scratch_word);
+  if (c->d_image) cudaFree(c->d_image);
+  if (c->d_upload) cudaFree(c->d_upload);
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return VVLIC_OK;
+}
+
+extern "C" const char* vvlic_last_error(const vvlic_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+// ------------------------------------------------------------------------------------------
+// uploads
+// ------------------------------------------------------------------------------------------
+static bool valid_dims(const int32_t* n) {
+  for (int i = 0; i < 3; ++i)
+    if (n[i] < 1 || n[i] > 2048) return false;
+  return (size_t)(n[0] + 1) * (n[1] + 1) * (n[2] + 1) < (size_t)1 << 31;
+}
+
+static vvlic_status grow(vvlic_ctx* c, void** buf, size_t* cap, size_t bytes) {
+  if (*cap >= bytes) return VVLIC_OK;
+  if (*buf) cudaFree(*buf);
+  *buf = nullptr;
+  *cap = 0;
+  cudaError_t e = cudaMalloc(buf, bytes);
+  if (e != cudaSuccess) return cuda_fail(c, e, "cudaMalloc");
+  *cap = bytes;
+  return VVLIC_OK;
+}
+
+static vvlic_status encode_into_volume(vvlic_ctx* c, const void* d_xyz, int dtype, const int n[3],
+                                       const float* slice_dist, int storage, cudaStream_t s, int32_t* vol_id) {
+  Volume v;
+  v.n[0] = n[0];
+  v.n[1] = n[1];
+  v.n[2] = n[2];
+  v.storage = storage;
+  v.geom = make_geometry(n, slice_dist);
+  const size_t count = (size_t)n[0] * n[1] * n[2];
+  v.texel_bytes = count * (storage == VVLIC_STORAGE_F32 ? 16 : 8);
+  cudaError_t e = cudaMalloc(&v.d_texels, v.texel_bytes);
+  if (e != cudaSuccess) return cuda_fail(c, e, "field allocation");
+  e = launch_encode_field(d_xyz, dtype, n, storage, v.d_texels, c->d_scratch_word, s);
+  if (e != cudaSuccess) {
+    free_volume(v);
+    return cuda_fail(c, e, "field encoding");
+  }
+  const int id = c->next_vol_id++;
+  c->vols[id] = v;
+  *vol_id = id;
+  return VVLIC_OK;
+}
+
+extern "C" vvlic_status vvlic_upload_field(vvlic_ctx* c, const void* xyz, int32_t dtype, int32_t nx, int32_t ny,
+                                          int32_t nz, const float* slice_dist, int32_t storage, int32_t* vol_id) {
+  if (!c) return VVLIC_ERR_BAD_HANDLE;
+  const int n[3] = {nx, ny, nz};
+  if (!xyz || !vol_id || !valid_dims(n)) return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "upload_field: bad arguments");
+  if (dtype != VVLIC_DTYPE_FLOAT32 && dtype != VVLIC_DTYPE_UINT8)
+    return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "upload_field: dtype %d", dtype);
+  if (storage < VVLIC_STORAGE_F32 || storage > VVLIC_STORAGE_BF16)
+    return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "upload_field: storage %d", storage);
+  if (slice_dist)
+    for (int i = 0; i < 3; ++i)
+      if (!(slice_dist[i] > 0.0f)) return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "upload_field: slice distance");
+  DeviceGuard g(c->device);
+  const size_t bytes = (size_t)nx * ny * nz * 3 * (dtype == VVLIC_DTYPE_FLOAT32 ? 4 : 1);
+  vvlic_status st = grow(c, &c->d_upload, &c->upload_cap, bytes);
+  if (st) return st;
+  cudaError_t e = cudaMemcpyAsync(c->d_upload, xyz, bytes, cudaMemcpyHostToDevice, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "upload_field copy");
+  st = encode_into_volume(c, c->d_upload, dtype, n, slice_dist, storage, c->stream, vol_id);
+  if (st) return st;
+  e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "upload_field");
+  return VVLIC_OK;
+}
+
+extern "C" vvlic_status vvlic_upload_field_device(vvlic_ctx* c, const float* d_xyz, int32_t nx, int32_t ny, int32_t nz,
+                                                 const float* slice_dist, int32_t storage, void* stream,
+                                                 int32_t* vol_id) {
+  if (!c) return VVLIC_ERR_BAD_HANDLE;
+  const int n[3] = {nx, ny, nz};
+  if (!d_xyz || !vol_id || !valid_dims(n)) return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "upload_field_device: bad arguments");
+  if (storage < VVLIC_STORAGE_F32 || storage > VVLIC_STORAGE_BF16)
+    return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "upload_field_device: storage %d", storage);
+  DeviceGuard g(c->device);
+  return encode_into_volume(c, d_xyz, VVLIC_DTYPE_FLOAT32, n, slice_dist, storage, (cudaStream_t)stream, vol_id);
+}
+
+extern "C" vvlic_status vvlic_free_volume(vvlic_ctx* c, int32_t vol_id) {
+  if (!c) return VVLIC_ERR_BAD_HANDLE;
+  auto it = c->vols.find(vol_id);
+  if (it == c->vols.end()) return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "free_volume: unknown volume %d", vol_id);
+  DeviceGuard g(c->device);
+  cudaStreamSynchronize(c->stream);
+  free_volume(it->second);
+  c->vols.erase(it);
+  return VVLIC_OK;
+}
+
+extern "C" vvlic_status vvlic_volume_bytes(const vvlic_ctx* c, int32_t vol_id, uint64_t* bytes) {
+  if (!c) return VVLIC_ERR_BAD_HANDLE;
+  auto it = c->vols.find(vol_id);
+  if (it == c->vols.end() || !bytes) return VVLIC_ERR_INVALID_ARGUMENT;
+  *bytes = it->second.texel_bytes + it->second.cell_bytes + it->second.array_bytes;
+  return VVLIC_OK;
+}
+
+extern "C" vvlic_status vvlic_noise_gradients_device(const uint8_t* d_noise, int32_t mx, int32_t my, int32_t mz,
+                                                    int32_t mode, const float* slice_dist, uint8_t* d_rgba,
+                                                    void* stream) {
+  const int m[3] = {mx, my, mz};
+  if (!d_noise || !d_rgba || !valid_dims(m)) return VVLIC_ERR_INVALID_ARGUMENT;
+  if (mode != VVLIC_NOISE_GRAD_SOBEL && mode != VVLIC_NOISE_GRAD_CENTRAL) return VVLIC_ERR_INVALID_ARGUMENT;
+  float sd[3] = {1.f, 1.f, 1.f};
+  if (slice_dist)
+    for (int i = 0; i < 3; ++i) sd[i] = slice_dist[i];
+  float w27[27];
+  noise_filter_weights(w27);
+  cudaStream_t s = (cudaStream_t)stream;
+  float* d_grad = nullptr;
+  const size_t bytes = (size_t)mx * my * mz * 3 * sizeof(float);
+  cudaError_t e = cudaMallocAsync((void**)&d_grad, bytes, s);
+  if (e != cudaSuccess) return e == cudaErrorMemoryAllocation ? VVLIC_ERR_OUT_OF_MEMORY : VVLIC_ERR_CUDA;
+  e = launch_noise_gradients(d_noise, m, mode, sd, d_grad, d_rgba, w27, s);
+  cudaError_t e2 = cudaFreeAsync(d_grad, s);
+  if (e != cudaSuccess || e2 != cudaSuccess) return VVLIC_ERR_CUDA;
+  return VVLIC_OK;
+}
+
+extern "C" vvlic_status vvlic_upload_noise(vvlic_ctx* c, const uint8_t* noise, int32_t mx, int32_t my, int32_t mz,
+                                          int32_t mode) {
+  if (!c) return VVLIC_ERR_BAD_HANDLE;
+  const int m[3] = {mx, my, mz};
+  if (!noise || !valid_dims(m)) return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "upload_noise: bad arguments");
+  if (mode < VVLIC_NOISE_SCALAR || mode > VVLIC_NOISE_GRAD_CENTRAL)
+    return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "upload_noise: mode %d", mode);
+  DeviceGuard g(c->device);
+  free_noise(c->noise);
+  NoiseTex& n = c->noise;
+  const size_t count = (size_t)mx * my * mz;
+  n.m[0] = mx;
+  n.m[1] = my;
+  n.m[2] = mz;
+  n.ch = mode == VVLIC_NOISE_SCALAR ? 1 : 4;
+  n.mode = mode;
+  cudaError_t e = cudaMalloc(&n.d_texels, count * n.ch);
+  if (e != cudaSuccess) return cuda_fail(c, e, "noise allocation");
+  if (mode == VVLIC_NOISE_SCALAR) {
+    e = cudaMemcpyAsync(n.d_texels, noise, count, cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "noise copy");
+  } else {
+    vvlic_status st = grow(c, &c->d_upload, &c->upload_cap, count);
+    if (st) return st;
+    e = cudaMemcpyAsync(c->d_upload, noise, count, cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "noise copy");
+    st = vvlic_noise_gradients_device((const uint8_t*)c->d_upload, mx, my, mz, mode, nullptr, n.d_texels, c->stream);
+    if (st) return fail(c, st, "noise gradients: %s", cudaGetErrorString(cudaGetLastError()));
+  }
+  e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "upload_noise");
+  return VVLIC_OK;
+}
+
+extern "C" vvlic_status vvlic_upload_scalar(vvlic_ctx* c, const float* scalar, int32_t nx, int32_t ny, int32_t nz) {
+  if (!c) return VVLIC_ERR_BAD_HANDLE;
+  const int n[3] = {nx, ny, nz};
+  if (!scalar || !valid_dims(n)) return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "upload_scalar: bad arguments");
+  DeviceGuard g(c->device);
+  if (c->d_scalar) cudaFree(c->d_scalar);
+  c->d_scalar = nullptr;
+  const size_t bytes = (size_t)nx * ny * nz * sizeof(float);
+  cudaError_t e = cudaMalloc(&c->d_scalar, bytes);
+  if (e != cudaSuccess) return cuda_fail(c, e, "scalar allocation");
+  e = cudaMemcpy(c->d_scalar, scalar, bytes, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_fail(c, e, "scalar copy");
+  for (int i = 0; i < 3; ++i) c->sn[i] = n[i];
+  return VVLIC_OK;
+}
+
+extern "C" vvlic_status vvlic_set_tf(vvlic_ctx* c, const float* rgba, const float* opacity) {
+  if (!c) return VVLIC_ERR_BAD_HANDLE;
+  if (rgba) std::memcpy(c->tf, rgba, sizeof(float) * 4 * VVLIC_TF_ENTRIES);
+  if (opacity) std::memcpy(c->tf + 4 * VVLIC_TF_ENTRIES, opacity, sizeof(float) * VVLIC_TF_ENTRIES);
+  for (int i = 0; i < 5 * VVLIC_TF_ENTRIES; ++i)
+    if (!std::isfinite(c->tf[i])) return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "set_tf: non-finite entry %d", i);
+  DeviceGuard g(c->device);
+  cudaError_t e = cudaMemcpyAsync(c->d_tf, c->tf, sizeof(float) * 5 * VVLIC_TF_ENTRIES, cudaMemcpyHostToDevice,
+                                  c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "set_tf");
+  return VVLIC_OK;
+}
+
+extern "C" vvlic_status vvlic_set_filter_table(vvlic_ctx* c, const uint8_t* table, int32_t width, int32_t clamp_mode) {
+  if (!c) return VVLIC_ERR_BAD_HANDLE;
+  if (!table || width < 1 || width > 1024 || (clamp_mode != VVLIC_KERNEL_CLAMP_BORDER && clamp_mode != VVLIC_KERNEL_CLAMP_EDGE))
+    return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "set_filter_table: bad arguments");
+  // LICFilter::loadData centres the table in the next power of two (dataset.cpp:1446-1458)
+  const int W = next_pow2(width), shift = (W - width) / 2;
+  std::memset(c->filter, 0, sizeof c->filter);
+  std::memcpy(c->filter + shift, table, width);
+  bool box = true;
+  for (int i = 0; i < W; ++i) box = box && c->filter[i] == 255;
+  unsigned sum = 0;
+  for (int i = 0; i < W; ++i) sum += c->filter[i];
+  if (sum == 0) return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "set_filter_table: all-zero filter");
+  c->filter_width = W;
+  c->filter_clamp = clamp_mode;
+  c->filter_is_box = box;
+  c->taps_override = false;
+  return VVLIC_OK;
+}
+
+extern "C" vvlic_status vvlic_set_filter_taps(vvlic_ctx* c, const float* taps, int32_t lb, int32_t lf,
+                                             float inv_filter_area) {
+  if (!c) return VVLIC_ERR_BAD_HANDLE;
+  if (!taps) {
+    c->taps_override = false;
+    return VVLIC_OK;
+  }
+  if (lb < 0 || lf < 0 || lb > VVLIC_MAX_STEPS || lf > VVLIC_MAX_STEPS || lb + lf == 0 || !std::isfinite(inv_filter_area))
+    return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "set_filter_taps: bad arguments");
+  for (int i = 0; i < lb + lf + 1; ++i) {
+    if (!std::isfinite(taps[i])) return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "set_filter_taps: non-finite tap");
+    c->taps[i] = taps[i];
+  }
+  c->taps_lb = lb;
+  c->taps_lf = lf;
+  c->taps_inv_area = inv_filter_area;
+  c->taps_override = true;
+  return VVLIC_OK;
+}
+
+extern "C" vvlic_status vvlic_get_filter_taps(const vvlic_ctx* c, float* taps, int32_t capacity, float* inv_area) {
+  if (!c) return VVLIC_ERR_BAD_HANDLE;
+  int lb, lf;
+  effective_steps(c->params, &lb, &lf);
+  if (!taps || !inv_area || capacity < lb + lf + 1) return VVLIC_ERR_INVALID_ARGUMENT;
+  return derive_taps(c, lb, lf, taps, inv_area);
+}
+
+static vvlic_status check_params(vvlic_ctx* c, const vvlic_params& p) {
+  if (!(p.step_size_vol > 0.0f) || !std::isfinite(p.step_size_vol))
+    return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "params: step_size_vol must be > 0");
+  if (!std::isfinite(p.step_size_lic) || !std::isfinite(p.gradient_scale) || !std::isfinite(p.illum_scale) ||
+      !std::isfinite(p.freq_scale) || !std::isfinite(p.eye_dist_factor) || !std::isfinite(p.alpha_threshold))
+    return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "params: non-finite value");
+  if (p.steps_forward < 0 || p.steps_backward < 0 || p.steps_forward > VVLIC_MAX_STEPS ||
+      p.steps_backward > VVLIC_MAX_STEPS || p.steps_forward + p.steps_backward == 0)
+    return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "params: steps must be in [0, %d] and not both 0", VVLIC_MAX_STEPS);
+  if (p.num_iterations < 0) return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "params: num_iterations < 0");
+  if (p.integrator < VVLIC_EULER || p.integrator > VVLIC_RK4)
+    return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "params: integrator %d", p.integrator);
+  if (p.illum < VVLIC_ILLUM_NONE || p.illum > VVLIC_ILLUM_MALLO)
+    return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "params: illum %d", p.illum);
+  if (p.illum == VVLIC_ILLUM_ZOECKLER || p.illum == VVLIC_ILLUM_MALLO)
+    return fail(c, VVLIC_ERR_UNSUPPORTED, "params: illumination model %d not built", p.illum);
+  if (p.tf_index != VVLIC_TF_INDEX_DIR_Z && p.tf_index != VVLIC_TF_INDEX_MAGNITUDE)
+    return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "params: tf_index %d", p.tf_index);
+  if (p.sampler < VVLIC_SAMPLER_GATHER || p.sampler > VVLIC_SAMPLER_TEXTURE)
+    return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "params: sampler %d", p.sampler);
+  return VVLIC_OK;
+}
+
+extern "C" vvlic_status vvlic_set_params(vvlic_ctx* c, const vvlic_params* p) {
+  if (!c) return VVLIC_ERR_BAD_HANDLE;
+  if (!p) return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "set_params: null");
+  vvlic_status st = check_params(c, *p);
+  if (st) return st;
+  c->params = *p;
+  return VVLIC_OK;
+}
+
+extern "C" vvlic_status vvlic_get_params(const vvlic_ctx* c, vvlic_params* p) {
+  if (!c) return VVLIC_ERR_BAD_HANDLE;
+  if (!p) return VVLIC_ERR_INVALID_ARGUMENT;
+  *p = c->params;
+  return VVLIC_OK;
+}
+
+extern "C" vvlic_status vvlic_set_view(vvlic_ctx* c, const vvlic_view* v) {
+  if (!c) return VVLIC_ERR_BAD_HANDLE;
+  if (!v) return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "set_view: null");
+  if (v->projection != VVLIC_PERSPECTIVE && v->projection != VVLIC_ORTHOGRAPHIC)
+    return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "set_view: projection %d", v->projection);
+  if (v->projection == VVLIC_PERSPECTIVE && !(v->fovy_deg > 0.0f && v->fovy_deg < 180.0f))
+    return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "set_view: fovy");
+  if (v->projection == VVLIC_ORTHOGRAPHIC &&
+      !(std::fabs(v->ortho_dir[0]) + std::fabs(v->ortho_dir[1]) + std::fabs(v->ortho_dir[2]) > 0.0f))
+    return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "set_view: zero ortho direction");
+  c->view = *v;
+  return VVLIC_OK;
+}
+
+extern "C" vvlic_status vvlic_view_rays(const vvlic_ctx* c, int32_t vol_id, int32_t w, int32_t h, double* coeffs) {
+  if (!c) return VVLIC_ERR_BAD_HANDLE;
+  auto it = c->vols.find(vol_id);
+  if (it == c->vols.end() || !coeffs || w < 1 || h < 1) return VVLIC_ERR_INVALID_ARGUMENT;
+  derive_rays(c->view, it->second.geom, w, h, coeffs);
+  return VVLIC_OK;
+}
+
+extern "C" vvlic_status vvlic_composite_background(float* rgba, int32_t w, int32_t h, const float* bg) {
+  if (!rgba || w < 1 || h < 1) return VVLIC_ERR_INVALID_ARGUMENT;
+  const float white[4] = {1.f, 1.f, 1.f, 1.f};
+  const float* b = bg ? bg : white;
+  for (size_t i = 0; i < (size_t)w * h; ++i) {
+    float* d = rgba + 4 * i;
+    const float om = 1.0f - d[3];
+    for (int ch = 0; ch < 4; ++ch) d[ch] = std::min(std::max(om * b[ch] + d[ch], 0.0f), 1.0f);
+  }
+  return VVLIC_OK;
+}
+
+extern "C" vvlic_status vvlic_download_field(vvlic_ctx* c, int32_t vol_id, void* out, uint64_t capacity) {
+  if (!c) return VVLIC_ERR_BAD_HANDLE;
+  auto it = c->vols.find(vol_id);
+  if (it == c->vols.end()) return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "download_field: unknown volume %d", vol_id);
+  if (!out || capacity < it->second.texel_bytes)
+    return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "download_field: need %zu bytes", it->second.texel_bytes);
+  DeviceGuard g(c->device);
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e == cudaSuccess) e = cudaMemcpy(out, it->second.d_texels, it->second.texel_bytes, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(c, e, "download_field");
+  return VVLIC_OK;
+}
+
+extern "C" vvlic_status vvlic_download_noise(vvlic_ctx* c, void* out, uint64_t capacity) {
+  if (!c) return VVLIC_ERR_BAD_HANDLE;
+  if (!c->noise.d_texels) return fail(c, VVLIC_ERR_NOT_READY, "download_noise: no noise uploaded");
+  const size_t bytes = (size_t)c->noise.m[0] * c->noise.m[1] * c->noise.m[2] * c->noise.ch;
+  if (!out || capacity < bytes) return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "download_noise: need %zu bytes", bytes);
+  DeviceGuard g(c->device);
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e == cudaSuccess) e = cudaMemcpy(out, c->noise.d_texels, bytes, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(c, e, "download_noise");
+  return VVLIC_OK;
+}

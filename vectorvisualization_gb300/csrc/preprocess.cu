@@ -1,0 +1,287 @@
+// Device preprocessing: field encoding (dataset.cpp:533-635), noise gradients
+// (gradient.cpp:190-531 + dataset.cpp:1270-1286) and the corner-packed cell arrays.
+//
+// This file is compiled with -fmad=false: every float expression rounds like the reference's
+// CPU code (no fused multiply-add), so the encoded field and the quantised gradients are
+// bit-identical to the reference's own arithmetic.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <stdint.h>
+
+#include <type_traits>
+
+#include "../../include/vvlic.h"
+#include "vvlic_launch.hpp"
+
+namespace vvlic {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ float vlen_f32(const float* f) { return sqrtf(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]); }
+
+// Magnitude of voxel a as fillTexDataFloatInterp computes it (0 below EPS = 1e-5f).
+__device__ __forceinline__ float voxel_len(const void* xyz, int dtype, size_t a, unsigned char t[3]) {
+  float len;
+  if (dtype == VVLIC_DTYPE_UINT8) {
+    const uint8_t* u = reinterpret_cast<const uint8_t*>(xyz) + 3 * a;
+    // `dataU -= 128` on unsigned char wraps modulo 256 (dataset.cpp:565-569)
+    for (int c = 0; c < 3; ++c) t[c] = (unsigned char)(u[c] - 128);
+    len = sqrtf((float)((int)t[0] * t[0]) + (float)((int)t[1] * t[1]) + (float)((int)t[2] * t[2]));
+  } else {
+    len = vlen_f32(reinterpret_cast<const float*>(xyz) + 3 * a);
+  }
+  return len < 1e-5f ? 0.0f : len;
+}
+
+__global__ void field_maxlen_kernel(const void* xyz, int dtype, size_t count, unsigned* maxbits) {
+  float m = 0.0f;
+  for (size_t a = blockIdx.x * (size_t)blockDim.x + threadIdx.x; a < count; a += (size_t)gridDim.x * blockDim.x) {
+    unsigned char t[3];
+    m = fmaxf(m, voxel_len(xyz, dtype, a, t));
+  }
+  // non-negative floats order like their bit patterns
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(maxbits, __float_as_uint(m));
+}
+
+template <int ST>
+__device__ __forceinline__ void store_texel(void* out, size_t a, float r, float g, float b, float al) {
+  if (ST == VVLIC_STORAGE_F32) {
+    reinterpret_cast<float4*>(out)[a] = make_float4(r, g, b, al);
+  } else if (ST == VVLIC_STORAGE_F16) {
+    __half2 lo = __halves2half2(__float2half_rn(r), __float2half_rn(g));
+    __half2 hi = __halves2half2(__float2half_rn(b), __float2half_rn(al));
+    uint2 v;
+    v.x = *reinterpret_cast<unsigned*>(&lo);
+    v.y = *reinterpret_cast<unsigned*>(&hi);
+    reinterpret_cast<uint2*>(out)[a] = v;
+  } else {
+    __nv_bfloat16 br = __float2bfloat16_rn(r), bg = __float2bfloat16_rn(g), bb = __float2bfloat16_rn(b),
+                  ba = __float2bfloat16_rn(al);
+    uint2 v;
+    v.x = (unsigned)*reinterpret_cast<unsigned short*>(&br) | ((unsigned)*reinterpret_cast<unsigned short*>(&bg) << 16);
+    v.y = (unsigned)*reinterpret_cast<unsigned short*>(&bb) | ((unsigned)*reinterpret_cast<unsigned short*>(&ba) << 16);
+    reinterpret_cast<uint2*>(out)[a] = v;
+  }
+}
+
+template <int ST>
+__global__ void field_encode_kernel(const void* xyz, int dtype, size_t count, const unsigned* maxbits, void* out) {
+  const float max_len = __uint_as_float(*maxbits);
+  for (size_t a = blockIdx.x * (size_t)blockDim.x + threadIdx.x; a < count; a += (size_t)gridDim.x * blockDim.x) {
+    unsigned char t[3];
+    float len = voxel_len(xyz, dtype, a, t);
+    float r, g, b;
+    if (len == 0.0f) {
+      r = g = b = 0.5f;
+    } else if (dtype == VVLIC_DTYPE_UINT8) {
+      r = 0.5f * (float)t[0] / len + 0.5f;
+      g = 0.5f * (float)t[1] / len + 0.5f;
+      b = 0.5f * (float)t[2] / len + 0.5f;
+    } else {
+      const float* f = reinterpret_cast<const float*>(xyz) + 3 * a;
+      r = 0.5f * f[0] / len + 0.5f;
+      g = 0.5f * f[1] / len + 0.5f;
+      b = 0.5f * f[2] / len + 0.5f;
+    }
+    float al = max_len > 0.0f ? len / max_len : 0.0f;
+    al = (al > 1.0f) ? 1.0f : ((al < 0.0f) ? 0.0f : al);
+    store_texel<ST>(out, a, r, g, b, al);
+  }
+}
+
+__device__ __forceinline__ float nv(const uint8_t* v, int nx, int ny, int x, int y, int z) {
+  return (float)v[((size_t)z * ny + y) * nx + x];
+}
+
+// computeGradients (gradient.cpp:190-374) for one voxel.
+__global__ void noise_grad_raw_kernel(const uint8_t* v, int nx, int ny, int nz, int mode, float sd0, float sd1,
+                                      float sd2, float* g) {
+  const size_t count = (size_t)nx * ny * nz;
+  for (size_t a = blockIdx.x * (size_t)blockDim.x + threadIdx.x; a < count; a += (size_t)gridDim.x * blockDim.x) {
+    const int x = (int)(a % nx), y = (int)((a / nx) % ny), z = (int)(a / ((size_t)nx * ny));
+    const float sd[3] = {sd0, sd1, sd2};
+    float gp[3];
+    if (mode == VVLIC_NOISE_GRAD_SOBEL && x > 0 && x < nx - 1 && y > 0 && y < ny - 1 && z > 0 && z < nz - 1) {
+      // weights[dir][i+1][j+1][k+1]: the 3x3x3 Sobel masks (gradient.cpp:199-224), summed in
+      // the reference's i, j, k order
+      const int s1[3] = {1, 3, 1}, s2[3] = {3, 6, 3};
+      for (int d = 0; d < 3; ++d) {
+        float acc = 0.0f;
+        for (int i = -1; i < 2; i++)
+          for (int j = -1; j < 2; j++)
+            for (int k = -1; k < 2; k++) {
+              const int o[3] = {i, j, k};
+              const int e = o[d];  // derivative axis offset
+              const int p = o[(d + 1) % 3], q = o[(d + 2) % 3];
+              // mask = sign(e) * w(p) * w(q) with w = (1,3,1) cross (1,3,1) pattern (1,3,1;3,6,3;1,3,1)
+              int w = e == 0 ? 0 : e * ((p == 0 ? s2 : s1)[q + 1]);
+              acc += (float)w * nv(v, nx, ny, x + i, y + j, z + k);
+            }
+        gp[d] = acc / (2.0f * sd[d]);
+      }
+    } else if (mode == VVLIC_NOISE_GRAD_SOBEL) {
+      const float c = nv(v, nx, ny, x, y, z);
+      gp[0] = (x < 1) ? (nv(v, nx, ny, x + 1, y, z) - c) / sd[0] : (c - nv(v, nx, ny, x - 1, y, z)) / sd[0];
+      gp[1] = (y < 1) ? (nv(v, nx, ny, x, y + 1, z) - c) / sd[1] : (c - nv(v, nx, ny, x, y - 1, z)) / sd[1];
+      gp[2] = (z < 1) ? (nv(v, nx, ny, x, y, z + 1) - c) / sd[2] : (c - nv(v, nx, ny, x, y, z - 1)) / sd[2];
+    } else {
+      // central differences (SOBEL 0 branch); the last slice per axis uses a one-sided
+      // difference — those values are never read by the smoothing window below
+      const float c = nv(v, nx, ny, x, y, z);
+      const int P[3] = {x, y, z}, N[3] = {nx, ny, nz};
+      for (int d = 0; d < 3; ++d) {
+        int lo[3] = {x, y, z}, hi[3] = {x, y, z};
+        lo[d] = P[d] - 1;
+        hi[d] = P[d] + 1;
+        if (P[d] < 1) gp[d] = (nv(v, nx, ny, hi[0], hi[1], hi[2]) - c) / sd[d];
+        else if (P[d] >= N[d] - 1) gp[d] = (c - nv(v, nx, ny, lo[0], lo[1], lo[2])) / sd[d];
+        else gp[d] = (nv(v, nx, ny, hi[0], hi[1], hi[2]) - nv(v, nx, ny, lo[0], lo[1], lo[2])) / sd[d] * 0.5f;
+      }
+    }
+    g[3 * a + 0] = gp[0];
+    g[3 * a + 1] = gp[1];
+    g[3 * a + 2] = gp[2];
+  }
+}
+
+struct W27 {
+  float w[27];
+};
+
+// filterGradients + quantize8 + RGBA pack (gradient.cpp:377-478, dataset.cpp:1270-1286).
+__global__ void noise_grad_filter_kernel(const uint8_t* v, const float* g, int nx, int ny, int nz, W27 fw27,
+                                         uint8_t* out) {
+  const size_t count = (size_t)nx * ny * nz;
+  for (size_t a = blockIdx.x * (size_t)blockDim.x + threadIdx.x; a < count; a += (size_t)gridDim.x * blockDim.x) {
+    const int x = (int)(a % nx), y = (int)((a / nx) % ny), z = (int)(a / ((size_t)nx * ny));
+    int bd = min(min(min(x, nx - x - 1), min(y, ny - y - 1)), min(z, nz - z - 1));
+    const int fw = min(2, bd);
+    float acc[3];
+    for (int c = 0; c < 3; ++c) {
+      float s = 0.0f;
+      for (int k = -fw; k < fw - 1; ++k)
+        for (int j = -fw; j < fw - 1; ++j)
+          for (int i = -fw; i < fw - 1; ++i) {
+            // the reference indexes its 5x5x5 table with the shrunken fw; only entries with
+            // all three indices in [0, 2] are ever used
+            const int wk = fw + k, wj = fw + j, wi = fw + i;
+            s += fw27.w[(wk * 3 + wj) * 3 + wi] * g[3 * (((size_t)(z + k) * ny + (y + j)) * nx + (x + i)) + c];
+          }
+      acc[c] = s;
+    }
+    float len = sqrtf(acc[0] * acc[0] + acc[1] * acc[1] + acc[2] * acc[2]);
+    if (len < 1e-5f) {
+      acc[0] = acc[1] = acc[2] = 0.0f;
+    } else {
+      acc[0] /= len;
+      acc[1] /= len;
+      acc[2] /= len;
+    }
+    uchar4 o;
+    o.x = (unsigned char)(((double)acc[0] + 1.0) / 2.0 * 255.0);
+    o.y = (unsigned char)(((double)acc[1] + 1.0) / 2.0 * 255.0);
+    o.z = (unsigned char)(((double)acc[2] + 1.0) / 2.0 * 255.0);
+    o.w = v[a];
+    reinterpret_cast<uchar4*>(out)[a] = o;
+  }
+}
+
+template <int ST> struct TexelBytes { static constexpr int value = ST == VVLIC_STORAGE_F32 ? 16 : 8; };
+
+// cell c per axis covers texels clamp(c-1), clamp(c): (n+1)^3 cells of 8 texels
+template <int ST>
+__global__ void field_cells_kernel(const void* texels, int nx, int ny, int nz, void* cells) {
+  using T = typename std::conditional<ST == VVLIC_STORAGE_F32, float4, uint2>::type;
+  const T* t = reinterpret_cast<const T*>(texels);
+  T* c = reinterpret_cast<T*>(cells);
+  const int cx = nx + 1, cy = ny + 1, cz = nz + 1;
+  const size_t count = (size_t)cx * cy * cz;
+  for (size_t a = blockIdx.x * (size_t)blockDim.x + threadIdx.x; a < count; a += (size_t)gridDim.x * blockDim.x) {
+    const int x = (int)(a % cx), y = (int)((a / cx) % cy), z = (int)(a / ((size_t)cx * cy));
+    const int x0 = max(x - 1, 0), x1 = min(x, nx - 1), y0 = max(y - 1, 0), y1 = min(y, ny - 1), z0 = max(z - 1, 0),
+              z1 = min(z, nz - 1);
+    const int xs[2] = {x0, x1}, ys[2] = {y0, y1}, zs[2] = {z0, z1};
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      c[8 * a + k] = t[((size_t)zs[(k >> 2) & 1] * ny + ys[(k >> 1) & 1]) * nx + xs[k & 1]];
+    }
+  }
+}
+
+// noise cell i per axis covers texels i and (i+1) mod m (REPEAT): m^3 cells
+__global__ void noise_cells_kernel(const uint8_t* texels, int mx, int my, int mz, int ch, uint8_t* cells) {
+  const size_t count = (size_t)mx * my * mz;
+  for (size_t a = blockIdx.x * (size_t)blockDim.x + threadIdx.x; a < count; a += (size_t)gridDim.x * blockDim.x) {
+    const int x = (int)(a % mx), y = (int)((a / mx) % my), z = (int)(a / ((size_t)mx * my));
+    const int xs[2] = {x, x + 1 == mx ? 0 : x + 1}, ys[2] = {y, y + 1 == my ? 0 : y + 1},
+              zs[2] = {z, z + 1 == mz ? 0 : z + 1};
+    if (ch == 4) {
+      const uint32_t* t = reinterpret_cast<const uint32_t*>(texels);
+      uint32_t* c = reinterpret_cast<uint32_t*>(cells);
+#pragma unroll
+      for (int k = 0; k < 8; ++k)
+        c[8 * a + k] = t[((size_t)zs[(k >> 2) & 1] * my + ys[(k >> 1) & 1]) * mx + xs[k & 1]];
+    } else {
+#pragma unroll
+      for (int k = 0; k < 8; ++k)
+        cells[8 * a + k] = texels[((size_t)zs[(k >> 2) & 1] * my + ys[(k >> 1) & 1]) * mx + xs[k & 1]];
+    }
+  }
+}
+
+inline int grid_for(size_t count) {
+  size_t b = (count + kThreads - 1) / kThreads;
+  return (int)(b < 152 * 64 ? (b == 0 ? 1 : b) : 152 * 64);
+}
+
+}  // namespace
+
+cudaError_t launch_encode_field(const void* d_xyz, int dtype, const int n[3], int storage, void* d_texels,
+                                unsigned* d_maxbits, cudaStream_t s) {
+  const size_t count = (size_t)n[0] * n[1] * n[2];
+  cudaError_t e = cudaMemsetAsync(d_maxbits, 0, sizeof(unsigned), s);
+  if (e != cudaSuccess) return e;
+  field_maxlen_kernel<<<grid_for(count), kThreads, 0, s>>>(d_xyz, dtype, count, d_maxbits);
+  if (storage == VVLIC_STORAGE_F32)
+    field_encode_kernel<VVLIC_STORAGE_F32><<<grid_for(count), kThreads, 0, s>>>(d_xyz, dtype, count, d_maxbits, d_texels);
+  else if (storage == VVLIC_STORAGE_F16)
+    field_encode_kernel<VVLIC_STORAGE_F16><<<grid_for(count), kThreads, 0, s>>>(d_xyz, dtype, count, d_maxbits, d_texels);
+  else
+    field_encode_kernel<VVLIC_STORAGE_BF16><<<grid_for(count), kThreads, 0, s>>>(d_xyz, dtype, count, d_maxbits, d_texels);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_noise_gradients(const uint8_t* d_noise, const int m[3], int mode, const float sd[3], float* d_grad,
+                                   uint8_t* d_rgba, const float w27[27], cudaStream_t s) {
+  const size_t count = (size_t)m[0] * m[1] * m[2];
+  noise_grad_raw_kernel<<<grid_for(count), kThreads, 0, s>>>(d_noise, m[0], m[1], m[2], mode, sd[0], sd[1], sd[2],
+                                                              d_grad);
+  W27 w;
+  for (int i = 0; i < 27; ++i) w.w[i] = w27[i];
+  noise_grad_filter_kernel<<<grid_for(count), kThreads, 0, s>>>(d_noise, d_grad, m[0], m[1], m[2], w, d_rgba);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_build_field_cells(const void* d_texels, const int n[3], int storage, void* d_cells,
+                                     cudaStream_t s) {
+  const size_t count = (size_t)(n[0] + 1) * (n[1] + 1) * (n[2] + 1);
+  if (storage == VVLIC_STORAGE_F32)
+    field_cells_kernel<VVLIC_STORAGE_F32><<<grid_for(count), kThreads, 0, s>>>(d_texels, n[0], n[1], n[2], d_cells);
+  else if (storage == VVLIC_STORAGE_F16)
+    field_cells_kernel<VVLIC_STORAGE_F16><<<grid_for(count), kThreads, 0, s>>>(d_texels, n[0], n[1], n[2], d_cells);
+  else
+    field_cells_kernel<VVLIC_STORAGE_BF16><<<grid_for(count), kThreads, 0, s>>>(d_texels, n[0], n[1], n[2], d_cells);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_build_noise_cells(const uint8_t* d_texels, const int m[3], int ch, uint8_t* d_cells,
+                                     cudaStream_t s) {
+  const size_t count = (size_t)m[0] * m[1] * m[2];
+  noise_cells_kernel<<<grid_for(count), kThreads, 0, s>>>(d_texels, m[0], m[1], m[2], ch, d_cells);
+  return cudaGetLastError();
+}
+
+}  // namespace vvlic

@@ -1,0 +1,466 @@
+// Device-side building blocks of the LIC ray-caster: GL-semantics samplers over the field,
+// noise and transfer-function tables, the streamline integrators, computeLIC, the shading models
+// and the front-to-back blend.  Each function names the reference GLSL it computes
+// (paths within VectorVisualization/shader/).
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/vvlic.h"
+
+namespace vvlic {
+
+constexpr int kMaxTaps = 2 * VVLIC_MAX_STEPS + 1;
+
+// Field layouts (see VVLIC_SAMPLER_*).
+enum Layout : int { kGather = 0, kCell = 1, kTexture = 2 };
+
+// Kernel arguments, passed by value as a __grid_constant__ parameter (≈2.4 KB, in the
+// constant bank; the taps are read warp-uniformly so they broadcast).
+struct RenderArgs {
+  const void* field;          // GATHER: n0*n1*n2 RGBA texels; CELL: (n+1)^3 cells of 8 texels
+  cudaTextureObject_t tex;    // TEXTURE layout
+  int n[3];
+  const uint8_t* noise;       // GATHER: m0*m1*m2 texels of noise_ch bytes; CELL: m^3 cells
+  int noise_cells;            // 1 when `noise` is the corner-packed cell array
+  int m[3];
+  int noise_ch;               // 1 (value) or 4 (gradient xyz, value)
+  const float* scalar;        // optional gate volume
+  int sn[3];
+  const float* tf;            // 256 RGBA entries followed by 256 opacity entries
+  float* out;                 // W*H RGBA
+  uint32_t* samples;          // optional per-pixel sample counts
+  unsigned long long* counters;  // [0] samples, [1] rays
+  int W, H;
+  int pixel_offset;           // first linear pixel index of this launch (batching)
+  float o0[3], o1[3], o2[3], d0[3], d1[3], d2[3];
+  int clamp0;
+  float ext[3], tex_max[3], scale_vol[3], scale_vol_inv[3];
+  float step_size, h_eff, intensity_scale, alpha_corr, illum_scale, freq_scale, alpha_thr;
+  float gate_lo, gate_hi;
+  int num_iter, lb, lf, illum, tf_index, sof, gate, quirks;
+  float light_pos[3], spec_exp, light_diff[3], light_spec[3], light_amb[3];
+  float taps[kMaxTaps];
+};
+
+// ------------------------------------------------------------------------------------------
+// small vector helpers
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
+__device__ __forceinline__ float3 add3(float3 a, float3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ float3 sub3(float3 a, float3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ float3 scl3(float3 a, float s) { return f3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ float3 mul3(float3 a, float3 b) { return f3(a.x * b.x, a.y * b.y, a.z * b.z); }
+__device__ __forceinline__ float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float3 norm3(float3 a) {
+  float d = dot3(a, a);
+  if (!(d > 0.0f)) return f3(0.f, 0.f, 0.f);  // normalize(0) := 0
+  return scl3(a, 1.0f / sqrtf(d));
+}
+__device__ __forceinline__ float lerpf(float a, float b, float t) { return fmaf(t, b - a, a); }
+__device__ __forceinline__ float4 lerp4(float4 a, float4 b, float t) {
+  return make_float4(lerpf(a.x, b.x, t), lerpf(a.y, b.y, t), lerpf(a.z, b.z, t), lerpf(a.w, b.w, t));
+}
+
+// ------------------------------------------------------------------------------------------
+// texel decoding per storage precision
+// ------------------------------------------------------------------------------------------
+template <int ST> struct Texel;
+template <> struct Texel<VVLIC_STORAGE_F32> {
+  using raw = float4;
+  static __device__ __forceinline__ float4 load(const void* base, int idx) {
+    return __ldg(reinterpret_cast<const float4*>(base) + idx);
+  }
+};
+template <> struct Texel<VVLIC_STORAGE_F16> {
+  using raw = uint2;
+  static __device__ __forceinline__ float4 decode(uint2 r) {
+    __half2 a = *reinterpret_cast<__half2*>(&r.x), b = *reinterpret_cast<__half2*>(&r.y);
+    float2 fa = __half22float2(a), fb = __half22float2(b);
+    return make_float4(fa.x, fa.y, fb.x, fb.y);
+  }
+  static __device__ __forceinline__ float4 load(const void* base, int idx) {
+    return decode(__ldg(reinterpret_cast<const uint2*>(base) + idx));
+  }
+};
+template <> struct Texel<VVLIC_STORAGE_BF16> {
+  using raw = uint2;
+  static __device__ __forceinline__ float4 decode(uint2 r) {
+    // bf16 -> f32 is a 16-bit shift
+    return make_float4(__uint_as_float(r.x << 16), __uint_as_float(r.x & 0xffff0000u), __uint_as_float(r.y << 16),
+                       __uint_as_float(r.y & 0xffff0000u));
+  }
+  static __device__ __forceinline__ float4 load(const void* base, int idx) {
+    return decode(__ldg(reinterpret_cast<const uint2*>(base) + idx));
+  }
+};
+
+// Texel-space coordinate of a CLAMP_TO_EDGE axis: returns the lower texel index (clamped) and
+// the weight of the upper one.  GL: u = s*N - 1/2, i0 = floor(u), alpha = frac(u).
+__device__ __forceinline__ void clamp_axis(float s, int n, int& i0, int& i1, float& a) {
+  float u = fmaf(s, (float)n, -0.5f);
+  u = fminf(fmaxf(u, -1.0f), (float)n);  // also maps NaN to -1; clamped texels are equal there
+  float fl = floorf(u);
+  a = u - fl;
+  int b = (int)fl;
+  i0 = min(max(b, 0), n - 1);
+  i1 = min(max(b + 1, 0), n - 1);
+}
+
+// ------------------------------------------------------------------------------------------
+// field sampling: texture3D(volumeSampler, s), LINEAR + CLAMP_TO_EDGE (dataset.cpp:351-357)
+// ------------------------------------------------------------------------------------------
+template <int ST, int LAYOUT> struct Field;
+
+template <int ST> struct Field<ST, kGather> {
+  static __device__ __forceinline__ float4 sample(const RenderArgs& a, float3 s) {
+    int x0, x1, y0, y1, z0, z1;
+    float ax, ay, az;
+    clamp_axis(s.x, a.n[0], x0, x1, ax);
+    clamp_axis(s.y, a.n[1], y0, y1, ay);
+    clamp_axis(s.z, a.n[2], z0, z1, az);
+    const int nx = a.n[0], nxy = a.n[0] * a.n[1];
+    const int r00 = z0 * nxy + y0 * nx, r10 = z0 * nxy + y1 * nx, r01 = z1 * nxy + y0 * nx, r11 = z1 * nxy + y1 * nx;
+    const void* f = a.field;
+    float4 t000 = Texel<ST>::load(f, r00 + x0), t100 = Texel<ST>::load(f, r00 + x1);
+    float4 t010 = Texel<ST>::load(f, r10 + x0), t110 = Texel<ST>::load(f, r10 + x1);
+    float4 t001 = Texel<ST>::load(f, r01 + x0), t101 = Texel<ST>::load(f, r01 + x1);
+    float4 t011 = Texel<ST>::load(f, r11 + x0), t111 = Texel<ST>::load(f, r11 + x1);
+    float4 c0 = lerp4(lerp4(t000, t100, ax), lerp4(t010, t110, ax), ay);
+    float4 c1 = lerp4(lerp4(t001, t101, ax), lerp4(t011, t111, ax), ay);
+    return lerp4(c0, c1, az);
+  }
+};
+
+// Corner-packed cells: cell c (per axis 0..n) holds texels clamp(c-1) and clamp(c), so the
+// cell of coordinate u = s*n + 1/2 is floor(u) clamped to [0, n] for every s.
+__device__ __forceinline__ void cell_axis(float s, int n, int& c, float& a) {
+  float u = fmaf(s, (float)n, 0.5f);
+  u = fminf(fmaxf(u, 0.0f), (float)n + 0.5f);
+  float fl = floorf(u);
+  a = u - fl;
+  c = min((int)fl, n);
+}
+
+template <> struct Field<VVLIC_STORAGE_F32, kCell> {
+  static __device__ __forceinline__ float4 sample(const RenderArgs& a, float3 s) {
+    int cx, cy, cz;
+    float ax, ay, az;
+    cell_axis(s.x, a.n[0], cx, ax);
+    cell_axis(s.y, a.n[1], cy, ay);
+    cell_axis(s.z, a.n[2], cz, az);
+    const int cnx = a.n[0] + 1, cny = a.n[1] + 1;
+    const float4* cell = reinterpret_cast<const float4*>(a.field) + 8 * ((cz * cny + cy) * cnx + cx);
+    float4 t000 = __ldg(cell + 0), t100 = __ldg(cell + 1), t010 = __ldg(cell + 2), t110 = __ldg(cell + 3);
+    float4 t001 = __ldg(cell + 4), t101 = __ldg(cell + 5), t011 = __ldg(cell + 6), t111 = __ldg(cell + 7);
+    float4 c0 = lerp4(lerp4(t000, t100, ax), lerp4(t010, t110, ax), ay);
+    float4 c1 = lerp4(lerp4(t001, t101, ax), lerp4(t011, t111, ax), ay);
+    return lerp4(c0, c1, az);
+  }
+};
+
+template <int ST> struct Field<ST, kCell> {  // F16 / BF16: 64-byte cells, four 16-byte loads
+  static __device__ __forceinline__ float4 sample(const RenderArgs& a, float3 s) {
+    int cx, cy, cz;
+    float ax, ay, az;
+    cell_axis(s.x, a.n[0], cx, ax);
+    cell_axis(s.y, a.n[1], cy, ay);
+    cell_axis(s.z, a.n[2], cz, az);
+    const int cnx = a.n[0] + 1, cny = a.n[1] + 1;
+    const uint4* cell = reinterpret_cast<const uint4*>(a.field) + 4 * ((cz * cny + cy) * cnx + cx);
+    uint4 q0 = __ldg(cell + 0), q1 = __ldg(cell + 1), q2 = __ldg(cell + 2), q3 = __ldg(cell + 3);
+    float4 t000 = Texel<ST>::decode(make_uint2(q0.x, q0.y)), t100 = Texel<ST>::decode(make_uint2(q0.z, q0.w));
+    float4 t010 = Texel<ST>::decode(make_uint2(q1.x, q1.y)), t110 = Texel<ST>::decode(make_uint2(q1.z, q1.w));
+    float4 t001 = Texel<ST>::decode(make_uint2(q2.x, q2.y)), t101 = Texel<ST>::decode(make_uint2(q2.z, q2.w));
+    float4 t011 = Texel<ST>::decode(make_uint2(q3.x, q3.y)), t111 = Texel<ST>::decode(make_uint2(q3.z, q3.w));
+    float4 c0 = lerp4(lerp4(t000, t100, ax), lerp4(t010, t110, ax), ay);
+    float4 c1 = lerp4(lerp4(t001, t101, ax), lerp4(t011, t111, ax), ay);
+    return lerp4(c0, c1, az);
+  }
+};
+
+template <int ST> struct Field<ST, kTexture> {  // hardware trilinear, unnormalised coordinates
+  static __device__ __forceinline__ float4 sample(const RenderArgs& a, float3 s) {
+    return tex3D<float4>(a.tex, s.x * (float)a.n[0], s.y * (float)a.n[1], s.z * (float)a.n[2]);
+  }
+};
+
+// ------------------------------------------------------------------------------------------
+// noise sampling: texture3D(noiseSampler, s), LINEAR + REPEAT (dataset.cpp:1333-1335), uint8/255
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ void repeat_axis(float s, int m, int& i0, int& i1, float& a) {
+  float u = fmaf(s, (float)m, -0.5f);
+  u = fminf(fmaxf(u, -16777216.0f), 16777216.0f);
+  float fl = floorf(u);
+  a = u - fl;
+  int b = (int)fl % m;
+  if (b < 0) b += m;
+  i0 = b;
+  i1 = (b + 1 == m) ? 0 : b + 1;
+}
+
+__device__ __forceinline__ float bytef(uint32_t w, int k) { return (float)((w >> (8 * k)) & 0xffu); }
+
+// Returns (gradient rgb, value) / 255; for one-channel noise rgb = 0.
+template <bool RGBA> __device__ __forceinline__ float4 sample_noise(const RenderArgs& a, float3 s) {
+  int x0, x1, y0, y1, z0, z1;
+  float ax, ay, az;
+  repeat_axis(s.x, a.m[0], x0, x1, ax);
+  repeat_axis(s.y, a.m[1], y0, y1, ay);
+  repeat_axis(s.z, a.m[2], z0, z1, az);
+  const float k = 1.0f / 255.0f;
+  if (a.noise_cells) {
+    // cell (x0,y0,z0) holds the 8 corners; RGBA: 32 bytes, value-only: 8 bytes
+    const int cidx = (z0 * a.m[1] + y0) * a.m[0] + x0;
+    if (RGBA) {
+      const uint4* c = reinterpret_cast<const uint4*>(a.noise) + 2 * cidx;
+      uint4 q0 = __ldg(c), q1 = __ldg(c + 1);
+      float4 r;
+      float* rp = &r.x;
+#pragma unroll
+      for (int ch = 0; ch < 4; ++ch) {
+        float c00 = lerpf(bytef(q0.x, ch), bytef(q0.y, ch), ax), c10 = lerpf(bytef(q0.z, ch), bytef(q0.w, ch), ax);
+        float c01 = lerpf(bytef(q1.x, ch), bytef(q1.y, ch), ax), c11 = lerpf(bytef(q1.z, ch), bytef(q1.w, ch), ax);
+        rp[ch] = lerpf(lerpf(c00, c10, ay), lerpf(c01, c11, ay), az) * k;
+      }
+      return r;
+    } else {
+      uint2 q = __ldg(reinterpret_cast<const uint2*>(a.noise) + cidx);
+      float c00 = lerpf(bytef(q.x, 0), bytef(q.x, 1), ax), c10 = lerpf(bytef(q.x, 2), bytef(q.x, 3), ax);
+      float c01 = lerpf(bytef(q.y, 0), bytef(q.y, 1), ax), c11 = lerpf(bytef(q.y, 2), bytef(q.y, 3), ax);
+      return make_float4(0.f, 0.f, 0.f, lerpf(lerpf(c00, c10, ay), lerpf(c01, c11, ay), az) * k);
+    }
+  }
+  const int mx = a.m[0], mxy = a.m[0] * a.m[1];
+  const int r00 = z0 * mxy + y0 * mx, r10 = z0 * mxy + y1 * mx, r01 = z1 * mxy + y0 * mx, r11 = z1 * mxy + y1 * mx;
+  if (RGBA) {
+    const uint32_t* t = reinterpret_cast<const uint32_t*>(a.noise);
+    uint32_t t000 = __ldg(t + r00 + x0), t100 = __ldg(t + r00 + x1), t010 = __ldg(t + r10 + x0),
+             t110 = __ldg(t + r10 + x1), t001 = __ldg(t + r01 + x0), t101 = __ldg(t + r01 + x1),
+             t011 = __ldg(t + r11 + x0), t111 = __ldg(t + r11 + x1);
+    float4 r;
+    float* rp = &r.x;
+#pragma unroll
+    for (int ch = 0; ch < 4; ++ch) {
+      float c00 = lerpf(bytef(t000, ch), bytef(t100, ch), ax), c10 = lerpf(bytef(t010, ch), bytef(t110, ch), ax);
+      float c01 = lerpf(bytef(t001, ch), bytef(t101, ch), ax), c11 = lerpf(bytef(t011, ch), bytef(t111, ch), ax);
+      rp[ch] = lerpf(lerpf(c00, c10, ay), lerpf(c01, c11, ay), az) * k;
+    }
+    return r;
+  } else {
+    const uint8_t* t = a.noise;
+    float c00 = lerpf((float)__ldg(t + r00 + x0), (float)__ldg(t + r00 + x1), ax);
+    float c10 = lerpf((float)__ldg(t + r10 + x0), (float)__ldg(t + r10 + x1), ax);
+    float c01 = lerpf((float)__ldg(t + r01 + x0), (float)__ldg(t + r01 + x1), ax);
+    float c11 = lerpf((float)__ldg(t + r11 + x0), (float)__ldg(t + r11 + x1), ax);
+    return make_float4(0.f, 0.f, 0.f, lerpf(lerpf(c00, c10, ay), lerpf(c01, c11, ay), az) * k);
+  }
+}
+
+// Value-only read of an RGBA noise (its .a channel), for the non-gradient LIC over -g noise.
+__device__ __forceinline__ float noise_value(const RenderArgs& a, float3 s) {
+  return a.noise_ch == 4 ? sample_noise<true>(a, s).w : sample_noise<false>(a, s).w;
+}
+
+__device__ __forceinline__ float sample_scalar(const RenderArgs& a, float3 s) {
+  int x0, x1, y0, y1, z0, z1;
+  float ax, ay, az;
+  clamp_axis(s.x, a.sn[0], x0, x1, ax);
+  clamp_axis(s.y, a.sn[1], y0, y1, ay);
+  clamp_axis(s.z, a.sn[2], z0, z1, az);
+  const int nx = a.sn[0], nxy = a.sn[0] * a.sn[1];
+  const float* t = a.scalar;
+  float c00 = lerpf(__ldg(t + z0 * nxy + y0 * nx + x0), __ldg(t + z0 * nxy + y0 * nx + x1), ax);
+  float c10 = lerpf(__ldg(t + z0 * nxy + y1 * nx + x0), __ldg(t + z0 * nxy + y1 * nx + x1), ax);
+  float c01 = lerpf(__ldg(t + z1 * nxy + y0 * nx + x0), __ldg(t + z1 * nxy + y0 * nx + x1), ax);
+  float c11 = lerpf(__ldg(t + z1 * nxy + y1 * nx + x0), __ldg(t + z1 * nxy + y1 * nx + x1), ax);
+  return lerpf(lerpf(c00, c10, ay), lerpf(c01, c11, ay), az);
+}
+
+// 1D LINEAR + CLAMP_TO_EDGE lookup in a 256-entry table (transferEdit.cpp:519-540), `tab`
+// laid out with `stride` floats per entry.
+__device__ __forceinline__ float tf1d(const float* tab, int stride, int ch, float s) {
+  float u = fmaf(s, (float)VVLIC_TF_ENTRIES, -0.5f);
+  u = fminf(fmaxf(u, -1.0f), (float)VVLIC_TF_ENTRIES);
+  float fl = floorf(u);
+  float t = u - fl;
+  int b = (int)fl;
+  int i0 = min(max(b, 0), VVLIC_TF_ENTRIES - 1), i1 = min(max(b + 1, 0), VVLIC_TF_ENTRIES - 1);
+  return lerpf(tab[i0 * stride + ch], tab[i1 * stride + ch], t);
+}
+__device__ __forceinline__ float4 tf_rgba(const float* tab, float s) {
+  float u = fmaf(s, (float)VVLIC_TF_ENTRIES, -0.5f);
+  u = fminf(fmaxf(u, -1.0f), (float)VVLIC_TF_ENTRIES);
+  float fl = floorf(u);
+  float t = u - fl;
+  int b = (int)fl;
+  int i0 = min(max(b, 0), VVLIC_TF_ENTRIES - 1), i1 = min(max(b + 1, 0), VVLIC_TF_ENTRIES - 1);
+  float4 a0 = reinterpret_cast<const float4*>(tab)[i0], a1 = reinterpret_cast<const float4*>(tab)[i1];
+  return lerp4(a0, a1, t);
+}
+
+// ------------------------------------------------------------------------------------------
+// LIC: computeLIC / singleLICstep (inc_lic.glsl:157-265)
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ float3 slope(float4 f) { return f3(2.0f * f.x - 1.0f, 2.0f * f.y - 1.0f, 2.0f * f.z - 1.0f); }
+
+// One streamline step; replaces `step` with the field value at the new position (the
+// first-same-as-last reuse of the reference's `step` in/out argument).
+template <int ST, int LAYOUT, int INTEG>
+__device__ __forceinline__ float3 lic_step(const RenderArgs& a, float3 p, float4& step, float dirs) {
+  using F = Field<ST, LAYOUT>;
+  const float hs = a.h_eff * dirs * (a.sof ? step.w : 1.0f);
+  float3 k1 = scl3(slope(step), hs);
+  if (INTEG == VVLIC_EULER) {
+    p = add3(p, k1);
+  } else if (INTEG == VVLIC_HEUN) {
+    float3 k2 = scl3(slope(F::sample(a, add3(p, k1))), hs);
+    p = add3(p, scl3(add3(k1, k2), 0.5f));
+  } else {
+    float3 k2 = scl3(slope(F::sample(a, add3(p, scl3(k1, 0.5f)))), hs);
+    float3 k3 = scl3(slope(F::sample(a, add3(p, scl3(k2, 0.5f)))), hs);
+    float3 k4 = scl3(slope(F::sample(a, add3(p, k3))), hs);
+    p = add3(p, scl3(add3(add3(k1, scl3(k2, 2.0f)), add3(scl3(k3, 2.0f), k4)), 1.0f / 6.0f));
+  }
+  step = F::sample(a, p);
+  return p;
+}
+
+// freqSampling / freqSamplingGrad (inc_lic.glsl:124-153)
+template <bool GRAD> __device__ __forceinline__ float4 noise_tap(const RenderArgs& a, float3 p) {
+  if (GRAD) {
+    const bool nofreq = (a.quirks & VVLIC_QUIRK_GRAD_NOISE_NO_FREQ) != 0;
+    return sample_noise<true>(a, nofreq ? p : scl3(p, a.freq_scale));
+  }
+  if (a.gate) {
+    float s = sample_scalar(a, p);
+    if (!(s > a.gate_lo && s < a.gate_hi)) return make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  if (a.quirks & VVLIC_QUIRK_LUMINANCE_NOISE) return make_float4(0.f, 0.f, 0.f, 1.0f);
+  return make_float4(0.f, 0.f, 0.f, noise_value(a, scl3(p, a.freq_scale)));
+}
+
+// computeLIC: (sum w*gradient_enc.xyz, sum w*noise); only .w without gradients.
+template <int ST, int LAYOUT, int INTEG, bool GRAD>
+__device__ __forceinline__ float4 compute_lic(const RenderArgs& a, float3 pos, float4 f0) {
+  const int lb = a.lb, lf = a.lf;
+  float4 n0 = noise_tap<GRAD>(a, pos);
+  float w0 = a.taps[lb];
+  float4 acc = make_float4(n0.x * w0, n0.y * w0, n0.z * w0, n0.w * w0);
+  {
+    float3 p = pos;
+    float4 step = f0;
+    for (int i = 1; i <= lb; ++i) {
+      p = lic_step<ST, LAYOUT, INTEG>(a, p, step, -1.0f);
+      float4 n = noise_tap<GRAD>(a, p);
+      float w = a.taps[lb - i];
+      if (GRAD) {
+        acc.x = fmaf(n.x, w, acc.x);
+        acc.y = fmaf(n.y, w, acc.y);
+        acc.z = fmaf(n.z, w, acc.z);
+      }
+      acc.w = fmaf(n.w, w, acc.w);
+    }
+  }
+  {
+    float3 p = pos;
+    float4 step = f0;
+    for (int i = 1; i <= lf; ++i) {
+      p = lic_step<ST, LAYOUT, INTEG>(a, p, step, 1.0f);
+      float4 n = noise_tap<GRAD>(a, p);
+      float w = a.taps[lb + i];
+      if (GRAD) {
+        acc.x = fmaf(n.x, w, acc.x);
+        acc.y = fmaf(n.y, w, acc.y);
+        acc.z = fmaf(n.z, w, acc.z);
+      }
+      acc.w = fmaf(n.w, w, acc.w);
+    }
+  }
+  return acc;
+}
+
+// ------------------------------------------------------------------------------------------
+// shading: illumLIC (inc_illum.glsl:257-271) and illumGradient (inc_illum.glsl:100-140)
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ float alpha_correct(float al, float corr) {
+  float base = fmaxf(1.0f - al, 0.0f);
+  return 1.0f - powf(base, corr);
+}
+
+__device__ __forceinline__ float4 shade(const RenderArgs& a, const float* s_tf, float4 il, float4 tf, float3 pos,
+                                        float3 dir) {
+  const float I = il.w;
+  float4 col;
+  if (a.illum == VVLIC_ILLUM_GRADIENT) {
+    float3 L = norm3(sub3(f3(a.light_pos[0], a.light_pos[1], a.light_pos[2]),
+                          mul3(pos, f3(a.scale_vol_inv[0], a.scale_vol_inv[1], a.scale_vol_inv[2]))));
+    float3 V = norm3(scl3(dir, -1.0f));
+    float3 N = norm3(f3(-il.x, -il.y, -il.z));
+    float3 R = norm3(sub3(scl3(N, 2.0f * dot3(L, N)), L));
+    float sp = powf(__saturatef(dot3(R, V)), a.spec_exp) * I;
+    float df = __saturatef(dot3(L, N)) * a.illum_scale;
+    col.x = (tf.x * I * (a.light_diff[0] * df + 0.3f + a.light_amb[0]) + a.light_spec[0] * sp) * a.illum_scale;
+    col.y = (tf.y * I * (a.light_diff[1] * df + 0.3f + a.light_amb[1]) + a.light_spec[1] * sp) * a.illum_scale;
+    col.z = (tf.z * I * (a.light_diff[2] * df + 0.3f + a.light_amb[2]) + a.light_spec[2] * sp) * a.illum_scale;
+  } else {
+    col.x = I * tf.x * a.illum_scale;
+    col.y = I * tf.y * a.illum_scale;
+    col.z = I * tf.z * a.illum_scale;
+  }
+  float al = tf1d(s_tf + 4 * VVLIC_TF_ENTRIES, 1, 0, I * 1.3f) * tf.w;
+  col.w = alpha_correct(al, a.alpha_corr);
+  return col;
+}
+
+// Front-to-back blend with per-step clamp (lic3d_fragment.glsl:83-84).
+__device__ __forceinline__ float4 blend(float4 dest, float4 src) {
+  src.x *= src.w;
+  src.y *= src.w;
+  src.z *= src.w;
+  const float om = 1.0f - dest.w;
+  return make_float4(__saturatef(fmaf(om, src.x, dest.x)), __saturatef(fmaf(om, src.y, dest.y)),
+                     __saturatef(fmaf(om, src.z, dest.z)), __saturatef(fmaf(om, src.w, dest.w)));
+}
+
+// Per-pixel ray: slab test against [0, extent] and the reference's start position
+// pos = objPos * scaleVol, dir = normalize(objPos - eye) * scaleVol (lic3d_fragment.glsl:12-21).
+__device__ __forceinline__ bool ray_setup(const RenderArgs& a, int px, int py, float3& pos, float3& dir) {
+  const float u = (float)px + 0.5f, v = (float)py + 0.5f;
+  float o[3], d[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    o[i] = a.o0[i] + u * a.o1[i] + v * a.o2[i];
+    d[i] = a.d0[i] + u * a.d1[i] + v * a.d2[i];
+  }
+  float tn = -INFINITY, tf = INFINITY;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    if (d[i] == 0.0f) {
+      if (o[i] < 0.0f || o[i] > a.ext[i]) return false;
+      continue;
+    }
+    float inv = 1.0f / d[i];
+    float t0 = (0.0f - o[i]) * inv, t1 = (a.ext[i] - o[i]) * inv;
+    tn = fmaxf(tn, fminf(t0, t1));
+    tf = fminf(tf, fmaxf(t0, t1));
+  }
+  if (!(tn < tf)) return false;
+  if (a.clamp0) {
+    if (!(tf > 0.0f)) return false;
+    tn = fmaxf(tn, 0.0f);
+  }
+  const float3 sv = f3(a.scale_vol[0], a.scale_vol[1], a.scale_vol[2]);
+  pos = mul3(f3(o[0] + tn * d[0], o[1] + tn * d[1], o[2] + tn * d[2]), sv);
+  dir = mul3(norm3(f3(d[0], d[1], d[2])), sv);
+  return true;
+}
+
+__device__ __forceinline__ bool outside_box(const RenderArgs& a, float3 p) {
+  return p.x < 0.0f || p.y < 0.0f || p.z < 0.0f || p.x > a.tex_max[0] || p.y > a.tex_max[1] || p.z > a.tex_max[2];
+}
+
+}  // namespace vvlic

@@ -1,0 +1,114 @@
+// Host-side state of a vvlic context (opaque to callers of the C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <map>
+#include <string>
+
+#include "../../include/vvlic.h"
+#include "vvlic_device.cuh"
+
+namespace vvlic {
+
+// VolumeData geometry (dataset.h:21-51 fields scale / scaleInv / extent / center).
+struct Geometry {
+  float slice_dist[3];
+  float scale[3], scale_inv[3], extent[3], center[3], tex_max[3];
+};
+
+struct Volume {
+  int n[3] = {0, 0, 0};
+  int storage = VVLIC_STORAGE_F32;
+  Geometry geom{};
+  void* d_texels = nullptr;       // x-fastest RGBA texels at `storage` precision
+  size_t texel_bytes = 0;
+  void* d_cells = nullptr;        // corner-packed cells, built on first CELL render
+  size_t cell_bytes = 0;
+  cudaArray_t array = nullptr;    // texture copy, built on first TEXTURE render
+  cudaTextureObject_t tex = 0;
+  size_t array_bytes = 0;
+};
+
+struct NoiseTex {
+  int m[3] = {0, 0, 0};
+  int ch = 0;                     // 1: value, 4: quantised gradient + value
+  int mode = VVLIC_NOISE_SCALAR;
+  uint8_t* d_texels = nullptr;
+  uint8_t* d_cells = nullptr;     // m^3 cells of 8 corners, built on first CELL render
+};
+
+class DeviceGuard {
+ public:
+  explicit DeviceGuard(int dev) {
+    cudaGetDevice(&prev_);
+    if (prev_ != dev) cudaSetDevice(dev);
+    dev_ = dev;
+  }
+  ~DeviceGuard() {
+    if (prev_ != dev_) cudaSetDevice(prev_);
+  }
+
+ private:
+  int prev_ = 0, dev_ = 0;
+};
+
+// The 27 smoothing weights of filterGradients (gradient.cpp:393-409: exp(-(i^2+j^2+k^2)/SIGMA2)
+// for i, j, k in [-2, 0], normalised by their float sum), computed in float like the reference.
+inline void noise_filter_weights(float w[27]) {
+  float sum = 0.0f;
+  int idx = 0;
+  for (int k = -2; k < 1; ++k)
+    for (int j = -2; j < 1; ++j)
+      for (int i = -2; i < 1; ++i) {
+        float v = std::exp(-(float)(i * i + j * j + k * k) / 5.0f);
+        w[idx++] = v;
+        sum += v;
+      }
+  for (int q = 0; q < 27; ++q) w[q] /= sum;
+}
+
+}  // namespace vvlic
+
+struct vvlic_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::map<int, vvlic::Volume> vols;
+  int next_vol_id = 1;
+  vvlic::NoiseTex noise;
+  float* d_scalar = nullptr;
+  int sn[3] = {0, 0, 0};
+  float tf[5 * VVLIC_TF_ENTRIES];  // RGBA entries then opacity entries
+  float* d_tf = nullptr;
+  uint8_t filter[1024];
+  int filter_width = 0;
+  int filter_clamp = VVLIC_KERNEL_CLAMP_BORDER;
+  bool filter_is_box = true;
+  bool taps_override = false;
+  float taps[vvlic::kMaxTaps];
+  int taps_lb = 0, taps_lf = 0;
+  float taps_inv_area = 0.5f;
+  vvlic_params params;
+  vvlic_view view;
+  unsigned long long* d_counters = nullptr;
+  unsigned* d_scratch_word = nullptr;
+  void* d_image = nullptr;
+  size_t image_cap = 0;
+  void* d_upload = nullptr;
+  size_t upload_cap = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  bool stats_pending = false;
+  uint64_t stats_steps_per_sample = 0;
+  vvlic_stats stats{};
+  std::string err;
+};
+
+namespace vvlic {
+vvlic_status fail(vvlic_ctx* c, vvlic_status s, const char* fmt, ...);
+vvlic_status cuda_fail(vvlic_ctx* c, cudaError_t e, const char* what);
+Geometry make_geometry(const int n[3], const float* slice_dist);
+vvlic_status derive_taps(const vvlic_ctx* c, int lb, int lf, float* taps, float* inv_area);
+void derive_rays(const vvlic_view& v, const Geometry& g, int W, int H, double* coeffs);
+}  // namespace vvlic

@@ -1,0 +1,31 @@
+// Host-visible launch entry points shared between the translation units of libvvlic.so.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace vvlic {
+
+struct RenderArgs;
+
+// Forward ray-cast, one launcher per field storage (render_f32.cu / render_f16.cu / render_bf16.cu).
+cudaError_t launch_raycast_f32(const RenderArgs& a, int layout, int integ, bool grad, cudaStream_t s);
+cudaError_t launch_raycast_f16(const RenderArgs& a, int layout, int integ, bool grad, cudaStream_t s);
+cudaError_t launch_raycast_bf16(const RenderArgs& a, int layout, int integ, bool grad, cudaStream_t s);
+
+// Preprocessing (preprocess.cu, compiled without FMA contraction so results match the
+// reference's CPU arithmetic bit for bit).
+// Field encoding of fillTexDataFloatInterp into `storage` texels; d_maxbits is a 4-byte
+// device scratch word.
+cudaError_t launch_encode_field(const void* d_xyz, int dtype, const int n[3], int storage, void* d_texels,
+                                unsigned* d_maxbits, cudaStream_t s);
+// Raw noise gradients (float xyz per voxel) into d_grad, then smoothing + quantisation + pack.
+cudaError_t launch_noise_gradients(const uint8_t* d_noise, const int m[3], int mode, const float sd[3],
+                                   float* d_grad, uint8_t* d_rgba, const float w27[27], cudaStream_t s);
+// Corner-packed cell arrays (see VVLIC_SAMPLER_CELL).
+cudaError_t launch_build_field_cells(const void* d_texels, const int n[3], int storage, void* d_cells,
+                                     cudaStream_t s);
+cudaError_t launch_build_noise_cells(const uint8_t* d_texels, const int m[3], int ch, uint8_t* d_cells,
+                                     cudaStream_t s);
+
+}  // namespace vvlic
