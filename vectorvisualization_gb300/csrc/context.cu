@@ -438,6 +438,8 @@ extern "C" vvlic_status vvlic_noise_gradients_device(const uint8_t* d_noise, int
   const int m[3] = {mx, my, mz};
   if (!d_noise || !d_rgba || !valid_dims(m)) return VVLIC_ERR_INVALID_ARGUMENT;
   if (mode != VVLIC_NOISE_GRAD_SOBEL && mode != VVLIC_NOISE_GRAD_CENTRAL) return VVLIC_ERR_INVALID_ARGUMENT;
+  // the one-sided border differences read the neighbour at +1: every axis needs two voxels
+  if (mx < 2 || my < 2 || mz < 2) return VVLIC_ERR_INVALID_ARGUMENT;
   float sd[3] = {1.f, 1.f, 1.f};
   if (slice_dist)
     for (int i = 0; i < 3; ++i) sd[i] = slice_dist[i];
@@ -461,6 +463,8 @@ extern "C" vvlic_status vvlic_upload_noise(vvlic_ctx* c, const uint8_t* noise, i
   if (!noise || !valid_dims(m)) return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "upload_noise: bad arguments");
   if (mode < VVLIC_NOISE_SCALAR || mode > VVLIC_NOISE_GRAD_CENTRAL)
     return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "upload_noise: mode %d", mode);
+  if (mode != VVLIC_NOISE_SCALAR && (mx < 2 || my < 2 || mz < 2))
+    return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "upload_noise: gradients need at least 2 voxels per axis");
   DeviceGuard g(c->device);
   free_noise(c->noise);
   NoiseTex& n = c->noise;
@@ -567,15 +571,17 @@ extern "C" vvlic_status vvlic_get_filter_taps(const vvlic_ctx* c, float* taps, i
 }
 
 static vvlic_status check_params(vvlic_ctx* c, const vvlic_params& p) {
-  if (!(p.step_size_vol > 0.0f) || !std::isfinite(p.step_size_vol))
-    return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "params: step_size_vol must be > 0");
+  if (!(p.step_size_vol >= 1e-5f) || !std::isfinite(p.step_size_vol))
+    return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "params: step_size_vol must be >= 1e-5");
   if (!std::isfinite(p.step_size_lic) || !std::isfinite(p.gradient_scale) || !std::isfinite(p.illum_scale) ||
       !std::isfinite(p.freq_scale) || !std::isfinite(p.eye_dist_factor) || !std::isfinite(p.alpha_threshold))
     return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "params: non-finite value");
   if (p.steps_forward < 0 || p.steps_backward < 0 || p.steps_forward > VVLIC_MAX_STEPS ||
       p.steps_backward > VVLIC_MAX_STEPS || p.steps_forward + p.steps_backward == 0)
     return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "params: steps must be in [0, %d] and not both 0", VVLIC_MAX_STEPS);
-  if (p.num_iterations < 0) return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "params: num_iterations < 0");
+  // two nested loops of num_iterations bound every ray (lic3d_fragment.glsl:38-40)
+  if (p.num_iterations < 0 || p.num_iterations > 1024)
+    return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "params: num_iterations must be in [0, 1024]");
   if (p.integrator < VVLIC_EULER || p.integrator > VVLIC_RK4)
     return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "params: integrator %d", p.integrator);
   if (p.illum < VVLIC_ILLUM_NONE || p.illum > VVLIC_ILLUM_MALLO)
