@@ -103,8 +103,10 @@ def test_noise_gradients_device_entry(vvlic_lib, oracle):
     sd = (1.0, 0.5, 2.0)
     d_in = torch.from_numpy(noise).cuda()
     d_out = torch.empty(noise.shape + (4,), dtype=torch.uint8, device="cuda")
+    dims = noise.shape[::-1]  # (mx, my, mz)
+    assert dims == (40, 33, 29)
     for mode in (capi.NOISE_GRAD_SOBEL, capi.NOISE_GRAD_CENTRAL):
-        capi.noise_gradients_device(d_in.data_ptr(), (29, 33, 40), mode, d_out.data_ptr(), slice_dist=sd)
+        capi.noise_gradients_device(d_in.data_ptr(), dims, mode, d_out.data_ptr(), slice_dist=sd)
         torch.cuda.synchronize()
         np.testing.assert_array_equal(d_out.cpu().numpy(), oracle.noise_gradients(noise, mode, sd))
 
