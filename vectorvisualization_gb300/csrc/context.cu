@@ -307,6 +307,8 @@ static void free_volume(Volume& v) {
 }
 
 static void free_noise(NoiseTex& n) {
+  if (n.tex) cudaDestroyTextureObject(n.tex);
+  if (n.array) cudaFreeArray(n.array);
   if (n.d_texels) cudaFree(n.d_texels);
   if (n.d_cells) cudaFree(n.d_cells);
   n = NoiseTex();

@@ -63,9 +63,40 @@ vvlic_status ensure_texture(vvlic_ctx* c, Volume& v, cudaStream_t s) {
   td.addressMode[0] = td.addressMode[1] = td.addressMode[2] = cudaAddressModeClamp;  // CLAMP_TO_EDGE
   td.filterMode = cudaFilterModeLinear;
   td.readMode = cudaReadModeElementType;
-  td.normalizedCoords = 0;
+  td.normalizedCoords = 1;  // GL texture coordinates
   e = cudaCreateTextureObject(&v.tex, &rd, &td, nullptr);
   if (e != cudaSuccess) return cuda_fail(c, e, "texture object");
+  return VVLIC_OK;
+}
+
+// Noise as an R8 / RGBA8 texture read as normalised float with WRAP addressing (GL REPEAT).
+vvlic_status ensure_noise_texture(vvlic_ctx* c, NoiseTex& n, cudaStream_t s) {
+  if (n.tex) return VVLIC_OK;
+  cudaChannelFormatDesc desc =
+      n.ch == 4 ? cudaCreateChannelDesc<uchar4>() : cudaCreateChannelDesc<unsigned char>();
+  cudaExtent ext = make_cudaExtent(n.m[0], n.m[1], n.m[2]);
+  cudaError_t e = cudaMalloc3DArray(&n.array, &desc, ext);
+  if (e != cudaSuccess) return cuda_fail(c, e, "noise texture allocation");
+  cudaMemcpy3DParms cp;
+  std::memset(&cp, 0, sizeof cp);
+  cp.srcPtr = make_cudaPitchedPtr(n.d_texels, (size_t)n.m[0] * n.ch, n.m[0], n.m[1]);
+  cp.dstArray = n.array;
+  cp.extent = ext;
+  cp.kind = cudaMemcpyDeviceToDevice;
+  e = cudaMemcpy3DAsync(&cp, s);
+  if (e != cudaSuccess) return cuda_fail(c, e, "noise texture copy");
+  cudaResourceDesc rd;
+  std::memset(&rd, 0, sizeof rd);
+  rd.resType = cudaResourceTypeArray;
+  rd.res.array.array = n.array;
+  cudaTextureDesc td;
+  std::memset(&td, 0, sizeof td);
+  td.addressMode[0] = td.addressMode[1] = td.addressMode[2] = cudaAddressModeWrap;
+  td.filterMode = cudaFilterModeLinear;
+  td.readMode = cudaReadModeNormalizedFloat;
+  td.normalizedCoords = 1;
+  e = cudaCreateTextureObject(&n.tex, &rd, &td, nullptr);
+  if (e != cudaSuccess) return cuda_fail(c, e, "noise texture object");
   return VVLIC_OK;
 }
 
@@ -98,13 +129,15 @@ vvlic_status build_render_args(vvlic_ctx* c, Volume& v, int W, int H, cudaStream
     if (p.sampler == VVLIC_SAMPLER_CELL) {
       if ((st = ensure_cells(c, v, s))) return st;
       a.field = v.d_cells;
+      if ((st = ensure_noise_cells(c, c->noise, s))) return st;
+      a.noise = c->noise.d_cells;
+      a.noise_cells = 1;
     } else {
       if ((st = ensure_texture(c, v, s))) return st;
+      if ((st = ensure_noise_texture(c, c->noise, s))) return st;
       a.tex = v.tex;
+      a.noise_tex = c->noise.tex;
     }
-    if ((st = ensure_noise_cells(c, c->noise, s))) return st;
-    a.noise = c->noise.d_cells;
-    a.noise_cells = 1;
   }
   for (int i = 0; i < 3; ++i) {
     a.m[i] = c->noise.m[i];

@@ -25,6 +25,7 @@ struct RenderArgs {
   cudaTextureObject_t tex;    // TEXTURE layout
   int n[3];
   const uint8_t* noise;       // GATHER: m0*m1*m2 texels of noise_ch bytes; CELL: m^3 cells
+  cudaTextureObject_t noise_tex;  // TEXTURE layout
   int noise_cells;            // 1 when `noise` is the corner-packed cell array
   int m[3];
   int noise_ch;               // 1 (value) or 4 (gradient xyz, value)
@@ -182,9 +183,9 @@ template <int ST> struct Field<ST, kCell> {  // F16 / BF16: 64-byte cells, four 
   }
 };
 
-template <int ST> struct Field<ST, kTexture> {  // hardware trilinear, unnormalised coordinates
+template <int ST> struct Field<ST, kTexture> {  // hardware trilinear, normalised coordinates, CLAMP
   static __device__ __forceinline__ float4 sample(const RenderArgs& a, float3 s) {
-    return tex3D<float4>(a.tex, s.x * (float)a.n[0], s.y * (float)a.n[1], s.z * (float)a.n[2]);
+    return tex3D<float4>(a.tex, s.x, s.y, s.z);
   }
 };
 
@@ -329,58 +330,77 @@ __device__ __forceinline__ float3 lic_step(const RenderArgs& a, float3 p, float4
   return p;
 }
 
+// Noise through the texture unit: RGBA8 / R8 read as normalised float (x/255), LINEAR filter,
+// WRAP addressing on normalised coordinates — GL's REPEAT (dataset.cpp:1333-1335).
+template <bool RGBA> __device__ __forceinline__ float4 sample_noise_tex(const RenderArgs& a, float3 s) {
+  if (RGBA) return tex3D<float4>(a.noise_tex, s.x, s.y, s.z);
+  return make_float4(0.f, 0.f, 0.f, tex3D<float>(a.noise_tex, s.x, s.y, s.z));
+}
+
+template <int LAYOUT> __device__ __forceinline__ float4 noise_rgba(const RenderArgs& a, float3 s) {
+  if (LAYOUT == kTexture) return sample_noise_tex<true>(a, s);
+  return sample_noise<true>(a, s);
+}
+template <int LAYOUT> __device__ __forceinline__ float noise_val(const RenderArgs& a, float3 s) {
+  if (LAYOUT == kTexture) return a.noise_ch == 4 ? sample_noise_tex<true>(a, s).w : sample_noise_tex<false>(a, s).w;
+  return noise_value(a, s);
+}
+
 // freqSampling / freqSamplingGrad (inc_lic.glsl:124-153)
-template <bool GRAD> __device__ __forceinline__ float4 noise_tap(const RenderArgs& a, float3 p) {
+template <int LAYOUT, bool GRAD> __device__ __forceinline__ float4 noise_tap(const RenderArgs& a, float3 p) {
   if (GRAD) {
     const bool nofreq = (a.quirks & VVLIC_QUIRK_GRAD_NOISE_NO_FREQ) != 0;
-    return sample_noise<true>(a, nofreq ? p : scl3(p, a.freq_scale));
+    return noise_rgba<LAYOUT>(a, nofreq ? p : scl3(p, a.freq_scale));
   }
   if (a.gate) {
     float s = sample_scalar(a, p);
     if (!(s > a.gate_lo && s < a.gate_hi)) return make_float4(0.f, 0.f, 0.f, 0.f);
   }
   if (a.quirks & VVLIC_QUIRK_LUMINANCE_NOISE) return make_float4(0.f, 0.f, 0.f, 1.0f);
-  return make_float4(0.f, 0.f, 0.f, noise_value(a, scl3(p, a.freq_scale)));
+  return make_float4(0.f, 0.f, 0.f, noise_val<LAYOUT>(a, scl3(p, a.freq_scale)));
+}
+
+template <bool GRAD> __device__ __forceinline__ void accumulate(float4& acc, float4 n, float w) {
+  if (GRAD) {
+    acc.x = fmaf(n.x, w, acc.x);
+    acc.y = fmaf(n.y, w, acc.y);
+    acc.z = fmaf(n.z, w, acc.z);
+  }
+  acc.w = fmaf(n.w, w, acc.w);
 }
 
 // computeLIC: (sum w*gradient_enc.xyz, sum w*noise); only .w without gradients.
+// The backward and forward streamlines are independent, so they advance in the same loop
+// iteration: two dependent gather chains per thread instead of one (the sum is reassociated
+// relative to the reference's backward-then-forward order).
 template <int ST, int LAYOUT, int INTEG, bool GRAD>
 __device__ __forceinline__ float4 compute_lic(const RenderArgs& a, float3 pos, float4 f0) {
   const int lb = a.lb, lf = a.lf;
-  float4 n0 = noise_tap<GRAD>(a, pos);
+  const int both = min(lb, lf);
+  float4 n0 = noise_tap<LAYOUT, GRAD>(a, pos);
   float w0 = a.taps[lb];
-  float4 acc = make_float4(n0.x * w0, n0.y * w0, n0.z * w0, n0.w * w0);
-  {
-    float3 p = pos;
-    float4 step = f0;
-    for (int i = 1; i <= lb; ++i) {
-      p = lic_step<ST, LAYOUT, INTEG>(a, p, step, -1.0f);
-      float4 n = noise_tap<GRAD>(a, p);
-      float w = a.taps[lb - i];
-      if (GRAD) {
-        acc.x = fmaf(n.x, w, acc.x);
-        acc.y = fmaf(n.y, w, acc.y);
-        acc.z = fmaf(n.z, w, acc.z);
-      }
-      acc.w = fmaf(n.w, w, acc.w);
-    }
+  float4 accb = make_float4(n0.x * w0, n0.y * w0, n0.z * w0, n0.w * w0);
+  float4 accf = make_float4(0.f, 0.f, 0.f, 0.f);
+  float3 pb = pos, pf = pos;
+  float4 sb = f0, sf = f0;
+  int i = 1;
+  for (; i <= both; ++i) {
+    pb = lic_step<ST, LAYOUT, INTEG>(a, pb, sb, -1.0f);
+    pf = lic_step<ST, LAYOUT, INTEG>(a, pf, sf, 1.0f);
+    float4 nb = noise_tap<LAYOUT, GRAD>(a, pb);
+    float4 nf = noise_tap<LAYOUT, GRAD>(a, pf);
+    accumulate<GRAD>(accb, nb, a.taps[lb - i]);
+    accumulate<GRAD>(accf, nf, a.taps[lb + i]);
   }
-  {
-    float3 p = pos;
-    float4 step = f0;
-    for (int i = 1; i <= lf; ++i) {
-      p = lic_step<ST, LAYOUT, INTEG>(a, p, step, 1.0f);
-      float4 n = noise_tap<GRAD>(a, p);
-      float w = a.taps[lb + i];
-      if (GRAD) {
-        acc.x = fmaf(n.x, w, acc.x);
-        acc.y = fmaf(n.y, w, acc.y);
-        acc.z = fmaf(n.z, w, acc.z);
-      }
-      acc.w = fmaf(n.w, w, acc.w);
-    }
+  for (int j = i; j <= lb; ++j) {
+    pb = lic_step<ST, LAYOUT, INTEG>(a, pb, sb, -1.0f);
+    accumulate<GRAD>(accb, noise_tap<LAYOUT, GRAD>(a, pb), a.taps[lb - j]);
   }
-  return acc;
+  for (int j = i; j <= lf; ++j) {
+    pf = lic_step<ST, LAYOUT, INTEG>(a, pf, sf, 1.0f);
+    accumulate<GRAD>(accf, noise_tap<LAYOUT, GRAD>(a, pf), a.taps[lb + j]);
+  }
+  return make_float4(accb.x + accf.x, accb.y + accf.y, accb.z + accf.z, accb.w + accf.w);
 }
 
 // ------------------------------------------------------------------------------------------

@@ -38,6 +38,8 @@ struct NoiseTex {
   int mode = VVLIC_NOISE_SCALAR;
   uint8_t* d_texels = nullptr;
   uint8_t* d_cells = nullptr;     // m^3 cells of 8 corners, built on first CELL render
+  cudaArray_t array = nullptr;    // texture copy, built on first TEXTURE render
+  cudaTextureObject_t tex = 0;
 };
 
 class DeviceGuard {
