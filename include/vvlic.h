@@ -53,15 +53,19 @@ enum {
 enum { VVLIC_DTYPE_FLOAT32 = 0, VVLIC_DTYPE_UINT8 = 1 };
 
 /* Device storage precision of the encoded field (RGBA per voxel).  The reference stores RGBA16F
- * (VectorDataSet::createTextureIterp(..., true), 3DLIC.cpp:707 -> dataset.cpp:326-331). */
-enum { VVLIC_STORAGE_F32 = 0, VVLIC_STORAGE_F16 = 1, VVLIC_STORAGE_BF16 = 2 };
+ * (VectorDataSet::createTextureIterp(..., true), 3DLIC.cpp:707 -> dataset.cpp:326-331).
+ * UNORM8 rounds the same float encoding to the nearest multiple of 1/255 (4 bytes per voxel). */
+enum { VVLIC_STORAGE_F32 = 0, VVLIC_STORAGE_F16 = 1, VVLIC_STORAGE_BF16 = 2, VVLIC_STORAGE_UNORM8 = 3 };
 
 /* How the kernels read the field:
  *   GATHER  - 8 texel loads per trilinear from the x-fastest RGBA array;
  *   CELL    - corner-packed cells: the 8 corners of every trilinear cell stored contiguously
  *             (8x the memory, one or two vector loads per trilinear);
- *   TEXTURE - hardware-filtered cudaTextureObject (8-bit fixed-point weights). */
-enum { VVLIC_SAMPLER_GATHER = 0, VVLIC_SAMPLER_CELL = 1, VVLIC_SAMPLER_TEXTURE = 2 };
+ *   TEXTURE - hardware-filtered cudaTextureObjects for field and noise (8-bit fixed-point
+ *             filter weights);
+ *   HYBRID  - field through the texture unit, noise from corner-packed cells through the
+ *             load/store path, splitting the gathers over both L1 data pipes. */
+enum { VVLIC_SAMPLER_GATHER = 0, VVLIC_SAMPLER_CELL = 1, VVLIC_SAMPLER_TEXTURE = 2, VVLIC_SAMPLER_HYBRID = 3 };
 
 /* Noise texture preparation (NoiseDataSet::createTexture, dataset.cpp:1176-1344).
  *   SCALAR  - noise value only (the reference without -g, read as the noise value, see quirks);
@@ -139,9 +143,16 @@ typedef struct vvlic_params {
   float light_specular[3];/* (1,1,1) */
   float light_ambient[3]; /* (0,0,0) */
   /* kernel selection (no reference counterpart) */
-  int32_t sampler;        /* VVLIC_SAMPLER_* (CELL) */
-  int32_t reserved[7];
+  int32_t sampler;        /* VVLIC_SAMPLER_* (TEXTURE) */
+  int32_t schedule;       /* VVLIC_SCHEDULE_* (QUEUE) */
+  int32_t reserved[6];
 } vvlic_params;
+
+/* Work distribution of a render launch:
+ *   QUEUE  - persistent CTAs pull 8x4-pixel ray tiles from a device work queue, tiles ordered
+ *            longest-first by their ray-box chord (no spin-waits: one atomic per tile);
+ *   STATIC - one CTA per 16x8 pixel tile in raster order. */
+enum { VVLIC_SCHEDULE_QUEUE = 0, VVLIC_SCHEDULE_STATIC = 1 };
 
 /* View.  PERSPECTIVE follows Camera::setCamera (camera.cpp:56-67) followed by
  * glTranslatef(-center) (renderer.cpp:146): gluPerspective(fovy, aspect, near, far),

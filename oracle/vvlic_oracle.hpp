@@ -167,11 +167,19 @@ static inline float round_to_bf16(float f) {
   std::memcpy(&r, &u, 4);
   return r;
 }
+/* nearest multiple of 1/255: x*255 rounded in float, then to the nearest integer (ties even) */
+static inline float round_to_unorm8(float f) {
+  float q = std::nearbyint(f * 255.0f);
+  q = q < 0.0f ? 0.0f : (q > 255.0f ? 255.0f : q);
+  return q / 255.0f;
+}
 static inline void round_storage(float* v, size_t count, int storage) {
   if (storage == VVLIC_STORAGE_F16)
     for (size_t i = 0; i < count; ++i) v[i] = round_to_f16(v[i]);
   else if (storage == VVLIC_STORAGE_BF16)
     for (size_t i = 0; i < count; ++i) v[i] = round_to_bf16(v[i]);
+  else if (storage == VVLIC_STORAGE_UNORM8)
+    for (size_t i = 0; i < count; ++i) v[i] = round_to_unorm8(v[i]);
 }
 
 /* ------------------------------------------------------------------------------------- */

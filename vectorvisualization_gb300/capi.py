@@ -20,8 +20,9 @@ TF_ENTRIES = 256
 OK, ERR_INVALID_ARGUMENT, ERR_OUT_OF_MEMORY, ERR_CUDA, ERR_NO_DEVICE, ERR_NOT_READY = 0, 1, 2, 3, 4, 5
 ERR_TIMEOUT, ERR_UNSUPPORTED, ERR_BAD_HANDLE, ERR_IO, ERR_FORMAT = 6, 7, 8, 9, 10
 DTYPE_FLOAT32, DTYPE_UINT8 = 0, 1
-STORAGE = {"f32": 0, "f16": 1, "bf16": 2}
-SAMPLER = {"gather": 0, "cell": 1, "texture": 2}
+STORAGE = {"f32": 0, "f16": 1, "bf16": 2, "u8": 3}
+SAMPLER = {"gather": 0, "cell": 1, "texture": 2, "hybrid": 3}
+SCHEDULE = {"queue": 0, "static": 1}
 NOISE_SCALAR, NOISE_GRAD_SOBEL, NOISE_GRAD_CENTRAL = 0, 1, 2
 EULER, HEUN, RK4 = 0, 1, 2
 ILLUM_NONE, ILLUM_GRADIENT, ILLUM_ZOECKLER, ILLUM_MALLO = 0, 1, 2, 3
@@ -64,7 +65,8 @@ class Params(C.Structure):
         ("light_specular", _f3),
         ("light_ambient", _f3),
         ("sampler", C.c_int32),
-        ("reserved", C.c_int32 * 7),
+        ("schedule", C.c_int32),
+        ("reserved", C.c_int32 * 6),
     ]
 
 
@@ -260,9 +262,13 @@ class Context:
         nx, ny, nz = dims
         if storage == "f32":
             out = np.empty((nz, ny, nx, 4), np.float32)
+        elif storage == "u8":
+            out = np.empty((nz, ny, nx, 4), np.uint8)
         else:
             out = np.empty((nz, ny, nx, 4), np.uint16)
         self._check(self._lib.vvlic_download_field(self.h, vid, out.ctypes.data, out.nbytes), "download_field")
+        if storage == "u8":
+            return out.astype(np.float32) / np.float32(255.0)
         if storage == "f16":
             return out.view(np.float16).astype(np.float32)
         if storage == "bf16":

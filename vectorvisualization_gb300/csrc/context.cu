@@ -198,7 +198,8 @@ extern "C" void vvlic_params_default(vvlic_params* p) {
     p->light_specular[i] = 1.0f;
     p->light_ambient[i] = 0.0f;
   }
-  p->sampler = VVLIC_SAMPLER_CELL;
+  p->sampler = VVLIC_SAMPLER_TEXTURE;
+  p->schedule = VVLIC_SCHEDULE_QUEUE;
 }
 
 extern "C" void vvlic_view_default(vvlic_view* v) {
@@ -285,7 +286,8 @@ extern "C" vvlic_status vvlic_create(vvlic_ctx** out, int32_t device) {
   vvlic_view_default(&c->view);
   default_tables(c);
   DeviceGuard g(device);
-  if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+  if ((e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess ||
+      (e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess ||
       (e = cudaMalloc(&c->d_tf, sizeof(float) * 5 * VVLIC_TF_ENTRIES)) != cudaSuccess ||
       (e = cudaMalloc(&c->d_counters, sizeof(unsigned long long) * 4)) != cudaSuccess ||
       (e = cudaMalloc(&c->d_scratch_word, sizeof(unsigned) * 4)) != cudaSuccess ||
@@ -326,6 +328,7 @@ extern "C" vvlic_status vvlic_destroy(vvlic_ctx* c) {
   if (c->d_scratch_word) cudaFree(c->d_scratch_word);
   if (c->d_image) cudaFree(c->d_image);
   if (c->d_upload) cudaFree(c->d_upload);
+  if (c->d_sched) cudaFree(c->d_sched);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -364,7 +367,7 @@ static vvlic_status encode_into_volume(vvlic_ctx* c, const void* d_xyz, int dtyp
   v.storage = storage;
   v.geom = make_geometry(n, slice_dist);
   const size_t count = (size_t)n[0] * n[1] * n[2];
-  v.texel_bytes = count * (storage == VVLIC_STORAGE_F32 ? 16 : 8);
+  v.texel_bytes = count * texel_bytes(storage);
   cudaError_t e = cudaMalloc(&v.d_texels, v.texel_bytes);
   if (e != cudaSuccess) return cuda_fail(c, e, "field allocation");
   e = launch_encode_field(d_xyz, dtype, n, storage, v.d_texels, c->d_scratch_word, s);
@@ -385,7 +388,7 @@ extern "C" vvlic_status vvlic_upload_field(vvlic_ctx* c, const void* xyz, int32_
   if (!xyz || !vol_id || !valid_dims(n)) return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "upload_field: bad arguments");
   if (dtype != VVLIC_DTYPE_FLOAT32 && dtype != VVLIC_DTYPE_UINT8)
     return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "upload_field: dtype %d", dtype);
-  if (storage < VVLIC_STORAGE_F32 || storage > VVLIC_STORAGE_BF16)
+  if (storage < VVLIC_STORAGE_F32 || storage > VVLIC_STORAGE_UNORM8)
     return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "upload_field: storage %d", storage);
   if (slice_dist)
     for (int i = 0; i < 3; ++i)
@@ -409,7 +412,7 @@ extern "C" vvlic_status vvlic_upload_field_device(vvlic_ctx* c, const float* d_x
   if (!c) return VVLIC_ERR_BAD_HANDLE;
   const int n[3] = {nx, ny, nz};
   if (!d_xyz || !vol_id || !valid_dims(n)) return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "upload_field_device: bad arguments");
-  if (storage < VVLIC_STORAGE_F32 || storage > VVLIC_STORAGE_BF16)
+  if (storage < VVLIC_STORAGE_F32 || storage > VVLIC_STORAGE_UNORM8)
     return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "upload_field_device: storage %d", storage);
   DeviceGuard g(c->device);
   return encode_into_volume(c, d_xyz, VVLIC_DTYPE_FLOAT32, n, slice_dist, storage, (cudaStream_t)stream, vol_id);
@@ -592,8 +595,10 @@ static vvlic_status check_params(vvlic_ctx* c, const vvlic_params& p) {
     return fail(c, VVLIC_ERR_UNSUPPORTED, "params: illumination model %d not built", p.illum);
   if (p.tf_index != VVLIC_TF_INDEX_DIR_Z && p.tf_index != VVLIC_TF_INDEX_MAGNITUDE)
     return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "params: tf_index %d", p.tf_index);
-  if (p.sampler < VVLIC_SAMPLER_GATHER || p.sampler > VVLIC_SAMPLER_TEXTURE)
+  if (p.sampler < VVLIC_SAMPLER_GATHER || p.sampler > VVLIC_SAMPLER_HYBRID)
     return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "params: sampler %d", p.sampler);
+  if (p.schedule != VVLIC_SCHEDULE_QUEUE && p.schedule != VVLIC_SCHEDULE_STATIC)
+    return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "params: schedule %d", p.schedule);
   return VVLIC_OK;
 }
 

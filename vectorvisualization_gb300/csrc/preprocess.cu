@@ -57,6 +57,12 @@ __device__ __forceinline__ void store_texel(void* out, size_t a, float r, float 
     v.x = *reinterpret_cast<unsigned*>(&lo);
     v.y = *reinterpret_cast<unsigned*>(&hi);
     reinterpret_cast<uint2*>(out)[a] = v;
+  } else if (ST == VVLIC_STORAGE_UNORM8) {
+    // nearest multiple of 1/255 (x*255 rounded in float, then to nearest integer)
+    const unsigned q0 = __float2uint_rn(r * 255.0f), q1 = __float2uint_rn(g * 255.0f),
+                   q2 = __float2uint_rn(b * 255.0f), q3 = __float2uint_rn(al * 255.0f);
+    reinterpret_cast<uint32_t*>(out)[a] = min(q0, 255u) | (min(q1, 255u) << 8) | (min(q2, 255u) << 16) |
+                                          (min(q3, 255u) << 24);
   } else {
     __nv_bfloat16 br = __float2bfloat16_rn(r), bg = __float2bfloat16_rn(g), bb = __float2bfloat16_rn(b),
                   ba = __float2bfloat16_rn(al);
@@ -189,12 +195,12 @@ __global__ void noise_grad_filter_kernel(const uint8_t* v, const float* g, int n
   }
 }
 
-template <int ST> struct TexelBytes { static constexpr int value = ST == VVLIC_STORAGE_F32 ? 16 : 8; };
 
 // cell c per axis covers texels clamp(c-1), clamp(c): (n+1)^3 cells of 8 texels
 template <int ST>
 __global__ void field_cells_kernel(const void* texels, int nx, int ny, int nz, void* cells) {
-  using T = typename std::conditional<ST == VVLIC_STORAGE_F32, float4, uint2>::type;
+  using T = typename std::conditional<ST == VVLIC_STORAGE_F32, float4,
+                                      typename std::conditional<ST == VVLIC_STORAGE_UNORM8, uint32_t, uint2>::type>::type;
   const T* t = reinterpret_cast<const T*>(texels);
   T* c = reinterpret_cast<T*>(cells);
   const int cx = nx + 1, cy = ny + 1, cz = nz + 1;
@@ -249,6 +255,9 @@ cudaError_t launch_encode_field(const void* d_xyz, int dtype, const int n[3], in
     field_encode_kernel<VVLIC_STORAGE_F32><<<grid_for(count), kThreads, 0, s>>>(d_xyz, dtype, count, d_maxbits, d_texels);
   else if (storage == VVLIC_STORAGE_F16)
     field_encode_kernel<VVLIC_STORAGE_F16><<<grid_for(count), kThreads, 0, s>>>(d_xyz, dtype, count, d_maxbits, d_texels);
+  else if (storage == VVLIC_STORAGE_UNORM8)
+    field_encode_kernel<VVLIC_STORAGE_UNORM8><<<grid_for(count), kThreads, 0, s>>>(d_xyz, dtype, count, d_maxbits,
+                                                                                    d_texels);
   else
     field_encode_kernel<VVLIC_STORAGE_BF16><<<grid_for(count), kThreads, 0, s>>>(d_xyz, dtype, count, d_maxbits, d_texels);
   return cudaGetLastError();
@@ -272,6 +281,8 @@ cudaError_t launch_build_field_cells(const void* d_texels, const int n[3], int s
     field_cells_kernel<VVLIC_STORAGE_F32><<<grid_for(count), kThreads, 0, s>>>(d_texels, n[0], n[1], n[2], d_cells);
   else if (storage == VVLIC_STORAGE_F16)
     field_cells_kernel<VVLIC_STORAGE_F16><<<grid_for(count), kThreads, 0, s>>>(d_texels, n[0], n[1], n[2], d_cells);
+  else if (storage == VVLIC_STORAGE_UNORM8)
+    field_cells_kernel<VVLIC_STORAGE_UNORM8><<<grid_for(count), kThreads, 0, s>>>(d_texels, n[0], n[1], n[2], d_cells);
   else
     field_cells_kernel<VVLIC_STORAGE_BF16><<<grid_for(count), kThreads, 0, s>>>(d_texels, n[0], n[1], n[2], d_cells);
   return cudaGetLastError();

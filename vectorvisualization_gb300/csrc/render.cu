@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 
 #include "../../include/vvlic.h"
@@ -17,7 +18,7 @@ namespace {
 vvlic_status ensure_cells(vvlic_ctx* c, Volume& v, cudaStream_t s) {
   if (v.d_cells) return VVLIC_OK;
   const size_t cells = (size_t)(v.n[0] + 1) * (v.n[1] + 1) * (v.n[2] + 1);
-  const size_t bytes = cells * 8 * (v.storage == VVLIC_STORAGE_F32 ? 16 : 8);
+  const size_t bytes = cells * 8 * texel_bytes(v.storage);
   cudaError_t e = cudaMalloc(&v.d_cells, bytes);
   if (e != cudaSuccess) return cuda_fail(c, e, "cell layout allocation");
   v.cell_bytes = bytes;
@@ -39,12 +40,13 @@ vvlic_status ensure_noise_cells(vvlic_ctx* c, NoiseTex& n, cudaStream_t s) {
 vvlic_status ensure_texture(vvlic_ctx* c, Volume& v, cudaStream_t s) {
   if (v.tex) return VVLIC_OK;
   if (v.storage == VVLIC_STORAGE_BF16) return fail(c, VVLIC_ERR_UNSUPPORTED, "TEXTURE sampler has no BF16 format");
-  cudaChannelFormatDesc desc =
-      v.storage == VVLIC_STORAGE_F32 ? cudaCreateChannelDesc<float4>() : cudaCreateChannelDescHalf4();
+  cudaChannelFormatDesc desc = v.storage == VVLIC_STORAGE_F32   ? cudaCreateChannelDesc<float4>()
+                               : v.storage == VVLIC_STORAGE_F16 ? cudaCreateChannelDescHalf4()
+                                                                : cudaCreateChannelDesc<uchar4>();
   cudaExtent ext = make_cudaExtent(v.n[0], v.n[1], v.n[2]);
   cudaError_t e = cudaMalloc3DArray(&v.array, &desc, ext);
   if (e != cudaSuccess) return cuda_fail(c, e, "texture array allocation");
-  const size_t tb = v.storage == VVLIC_STORAGE_F32 ? 16 : 8;
+  const size_t tb = texel_bytes(v.storage);
   v.array_bytes = (size_t)v.n[0] * v.n[1] * v.n[2] * tb;
   cudaMemcpy3DParms cp;
   std::memset(&cp, 0, sizeof cp);
@@ -62,7 +64,7 @@ vvlic_status ensure_texture(vvlic_ctx* c, Volume& v, cudaStream_t s) {
   std::memset(&td, 0, sizeof td);
   td.addressMode[0] = td.addressMode[1] = td.addressMode[2] = cudaAddressModeClamp;  // CLAMP_TO_EDGE
   td.filterMode = cudaFilterModeLinear;
-  td.readMode = cudaReadModeElementType;
+  td.readMode = v.storage == VVLIC_STORAGE_UNORM8 ? cudaReadModeNormalizedFloat : cudaReadModeElementType;
   td.normalizedCoords = 1;  // GL texture coordinates
   e = cudaCreateTextureObject(&v.tex, &rd, &td, nullptr);
   if (e != cudaSuccess) return cuda_fail(c, e, "texture object");
@@ -121,23 +123,29 @@ vvlic_status build_render_args(vvlic_ctx* c, Volume& v, int W, int H, cudaStream
   a.n[0] = v.n[0];
   a.n[1] = v.n[1];
   a.n[2] = v.n[2];
-  if (p.sampler == VVLIC_SAMPLER_GATHER) {
-    a.field = v.d_texels;
-    a.noise = c->noise.d_texels;
-    a.noise_cells = 0;
-  } else {
-    if (p.sampler == VVLIC_SAMPLER_CELL) {
+  switch (p.sampler) {
+    case VVLIC_SAMPLER_GATHER:
+      a.field = v.d_texels;
+      a.noise = c->noise.d_texels;
+      break;
+    case VVLIC_SAMPLER_CELL:
       if ((st = ensure_cells(c, v, s))) return st;
-      a.field = v.d_cells;
       if ((st = ensure_noise_cells(c, c->noise, s))) return st;
+      a.field = v.d_cells;
       a.noise = c->noise.d_cells;
-      a.noise_cells = 1;
-    } else {
+      break;
+    case VVLIC_SAMPLER_TEXTURE:
       if ((st = ensure_texture(c, v, s))) return st;
       if ((st = ensure_noise_texture(c, c->noise, s))) return st;
       a.tex = v.tex;
       a.noise_tex = c->noise.tex;
-    }
+      break;
+    default:  // HYBRID
+      if ((st = ensure_texture(c, v, s))) return st;
+      if ((st = ensure_noise_cells(c, c->noise, s))) return st;
+      a.tex = v.tex;
+      a.noise = c->noise.d_cells;
+      break;
   }
   for (int i = 0; i < 3; ++i) {
     a.m[i] = c->noise.m[i];
@@ -196,12 +204,82 @@ vvlic_status build_render_args(vvlic_ctx* c, Volume& v, int W, int H, cudaStream
   return VVLIC_OK;
 }
 
-cudaError_t launch_raycast(const RenderArgs& a, int storage, int sampler, int integ, bool grad, cudaStream_t s) {
+cudaError_t launch_raycast(const RenderArgs& a, int storage, int sampler, int integ, bool grad, const Schedule& sch,
+                           cudaStream_t s) {
   switch (storage) {
-    case VVLIC_STORAGE_F32: return launch_raycast_f32(a, sampler, integ, grad, s);
-    case VVLIC_STORAGE_F16: return launch_raycast_f16(a, sampler, integ, grad, s);
-    default: return launch_raycast_bf16(a, sampler, integ, grad, s);
+    case VVLIC_STORAGE_F32: return launch_raycast_f32(a, sampler, integ, grad, sch, s);
+    case VVLIC_STORAGE_F16: return launch_raycast_f16(a, sampler, integ, grad, sch, s);
+    case VVLIC_STORAGE_UNORM8: return launch_raycast_u8(a, sampler, integ, grad, sch, s);
+    default: return launch_raycast_bf16(a, sampler, integ, grad, sch, s);
   }
+}
+
+// ------------------------------------------------------------------------------------------
+// longest-first tile order for the queue schedule
+// ------------------------------------------------------------------------------------------
+namespace {
+
+constexpr int kBuckets = 1024;
+
+// One warp per 8x4 tile: the tile's cost is its longest ray's sample count (the warp runs until
+// that ray finishes), estimated from the ray-box chord: samples ~ chord / spacing + 1.
+__global__ void tile_cost_kernel(const __grid_constant__ RenderArgs a, int ntiles, int tiles_x, int shift,
+                                 unsigned* bucket, unsigned* hist) {
+  const int lane = threadIdx.x & 31;
+  const int warps = gridDim.x * (blockDim.x >> 5);
+  for (int t = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); t < ntiles; t += warps) {
+    const int px = (t % tiles_x) * 8 + (lane & 7), py = (t / tiles_x) * 4 + (lane >> 3);
+    unsigned cost = 0;
+    float o[3], d[3], tn, tf;
+    if (px < a.W && py < a.H && ray_interval(a, px, py, o, d, tn, tf)) {
+      const float len = (tf - tn) * sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+      cost = (unsigned)fminf(len / a.step_size + 1.0f, 4.0e9f);
+    }
+    cost = __reduce_max_sync(0xffffffffu, cost);
+    if (lane == 0) {
+      const unsigned b = kBuckets - 1 - min(cost >> shift, (unsigned)(kBuckets - 1));  // descending
+      bucket[t] = b;
+      atomicAdd(hist + b, 1u);
+    }
+  }
+}
+
+// Exclusive scan of the bucket histogram into start offsets (one CTA of kBuckets threads).
+__global__ void bucket_scan_kernel(const unsigned* hist, unsigned* offsets) {
+  __shared__ unsigned s[kBuckets];
+  const int i = threadIdx.x;
+  s[i] = hist[i];
+  __syncthreads();
+  for (int d = 1; d < kBuckets; d <<= 1) {
+    unsigned v = i >= d ? s[i - d] : 0u;
+    __syncthreads();
+    s[i] += v;
+    __syncthreads();
+  }
+  offsets[i] = s[i] - hist[i];
+}
+
+__global__ void tile_scatter_kernel(int ntiles, const unsigned* bucket, unsigned* offsets, unsigned* order) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ntiles; t += gridDim.x * blockDim.x)
+    order[atomicAdd(offsets + bucket[t], 1u)] = (unsigned)t;
+}
+
+}  // namespace
+
+cudaError_t launch_tile_order(const RenderArgs& a, int ntiles, int tiles_x, int shift, unsigned* scratch,
+                              cudaStream_t s) {
+  unsigned* bucket = scratch;
+  unsigned* order = scratch + ntiles;
+  unsigned* hist = scratch + 2 * (size_t)ntiles;
+  unsigned* offsets = hist + kBuckets;
+  cudaError_t e = cudaMemsetAsync(hist, 0, kBuckets * sizeof(unsigned), s);
+  if (e != cudaSuccess) return e;
+  const int warps_per_block = 8;
+  const int blocks = std::min((ntiles + warps_per_block - 1) / warps_per_block, 152 * 16);
+  tile_cost_kernel<<<blocks, 32 * warps_per_block, 0, s>>>(a, ntiles, tiles_x, shift, bucket, hist);
+  bucket_scan_kernel<<<1, kBuckets, 0, s>>>(hist, offsets);
+  tile_scatter_kernel<<<std::min((ntiles + 255) / 256, 152 * 8), 256, 0, s>>>(ntiles, bucket, offsets, order);
+  return cudaGetLastError();
 }
 
 }  // namespace vvlic
@@ -220,11 +298,38 @@ extern "C" vvlic_status vvlic_render_device(vvlic_ctx* c, int32_t vol_id, float*
   if (st) return st;
   a.out = d_out;
   a.samples = d_samples;
+  Schedule sch;
+  sch.num_sms = c->num_sms;
   cudaError_t e = cudaMemsetAsync(c->d_counters, 0, 4 * sizeof(unsigned long long), s);
+  if (e == cudaSuccess && c->params.schedule == VVLIC_SCHEDULE_QUEUE) {
+    const int tiles_x = (w + 7) / 8, ntiles = tiles_x * ((h + 3) / 4);
+    const size_t words = 2 * (size_t)ntiles + 2 * 1024 + 1;
+    if (c->sched_cap < words) {
+      if (c->d_sched) cudaFree(c->d_sched);
+      c->d_sched = nullptr;
+      c->sched_cap = 0;
+      e = cudaMalloc(&c->d_sched, words * sizeof(unsigned));
+      if (e != cudaSuccess) return cuda_fail(c, e, "schedule allocation");
+      c->sched_cap = words;
+    }
+    // cost buckets of 2^shift samples so the longest possible chord fits 1024 buckets
+    const Geometry& gm = it->second.geom;
+    const double diag = std::sqrt((double)gm.extent[0] * gm.extent[0] + (double)gm.extent[1] * gm.extent[1] +
+                                  (double)gm.extent[2] * gm.extent[2]);
+    const double maxcost = diag / a.step_size + 2.0;
+    int shift = 0;
+    while ((maxcost / (double)(1u << shift)) >= 1024.0 && shift < 31) ++shift;
+    unsigned* scratch = c->d_sched;
+    e = launch_tile_order(a, ntiles, tiles_x, shift, scratch, s);
+    sch.order = scratch + ntiles;
+    sch.ntiles = ntiles;
+    sch.next = scratch + 2 * (size_t)ntiles + 2 * 1024;
+    if (e == cudaSuccess) e = cudaMemsetAsync(sch.next, 0, sizeof(unsigned), s);
+  }
   if (e == cudaSuccess) e = cudaEventRecord(c->ev0, s);
   if (e == cudaSuccess)
     e = launch_raycast(a, it->second.storage, c->params.sampler, c->params.integrator,
-                       c->params.illum == VVLIC_ILLUM_GRADIENT, s);
+                       c->params.illum == VVLIC_ILLUM_GRADIENT, sch, s);
   if (e == cudaSuccess) e = cudaEventRecord(c->ev1, s);
   if (e != cudaSuccess) return cuda_fail(c, e, "render launch");
   c->stats_pending = true;

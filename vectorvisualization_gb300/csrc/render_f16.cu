@@ -3,13 +3,9 @@
 
 namespace vvlic {
 
-cudaError_t launch_raycast_f16(const RenderArgs& a, int layout, int integ, bool grad, cudaStream_t s) {
-  switch (layout) {
-    case kGather: return launch_layout<VVLIC_STORAGE_F16, kGather>(a, integ, grad, s);
-    case kCell: return launch_layout<VVLIC_STORAGE_F16, kCell>(a, integ, grad, s);
-    case kTexture: return launch_layout<VVLIC_STORAGE_F16, kTexture>(a, integ, grad, s);
-    default: return cudaErrorInvalidValue;
-  }
+cudaError_t launch_raycast_f16(const RenderArgs& a, int sampler, int integ, bool grad, const Schedule& sch,
+                               cudaStream_t s) {
+  return launch_storage<VVLIC_STORAGE_F16>(a, sampler, integ, grad, sch, s);
 }
 
 }  // namespace vvlic

@@ -1,6 +1,10 @@
-// Forward LIC ray-cast kernel: one thread per pixel, the whole lic3d_fragment.glsl main()
-// (lic3d_fragment.glsl:5-99) per thread.  Instantiated per field storage in render_f32.cu,
-// render_f16.cu and render_bf16.cu so the three compile in parallel.
+// Forward LIC ray-cast kernels: one thread per pixel runs the whole lic3d_fragment.glsl main()
+// (lic3d_fragment.glsl:5-99).  Two work distributions:
+//   * static: one CTA per 16x8 pixel tile in raster order;
+//   * queue:  persistent CTAs whose warps pull 8x4 pixel tiles from a device work queue, the
+//             tiles pre-ordered longest ray chord first (one atomicAdd per tile, no waiting).
+// Instantiated per field storage in render_f32.cu / render_f16.cu / render_bf16.cu /
+// render_u8.cu so the translation units compile in parallel.
 #pragma once
 
 #include "vvlic_device.cuh"
@@ -8,70 +12,115 @@
 
 namespace vvlic {
 
-constexpr int kTileW = 16, kTileH = 8;  // 128 threads; a warp covers a 16x2 pixel patch
+constexpr int kTileW = 16, kTileH = 8;  // static schedule: 128 threads, a warp covers 16x2 pixels
+constexpr int kWarpTileW = 8, kWarpTileH = 4;  // queue schedule: one warp per 8x4 pixel tile
+constexpr int kThreads = 128;
 
-template <int ST, int LAYOUT, int INTEG, bool GRAD>
-__global__ void __launch_bounds__(kTileW* kTileH) raycast_kernel(const __grid_constant__ RenderArgs a) {
-  __shared__ __align__(16) float s_tf[5 * VVLIC_TF_ENTRIES];
+__device__ __forceinline__ void load_tf(const RenderArgs& a, float* s_tf) {
   for (int i = threadIdx.x; i < 5 * VVLIC_TF_ENTRIES; i += blockDim.x) s_tf[i] = __ldg(a.tf + i);
   __syncthreads();
+}
 
-  const int px = blockIdx.x * kTileW + (threadIdx.x % kTileW);
-  const int py = blockIdx.y * kTileH + (threadIdx.x / kTileW);
-  const bool active = px < a.W && py < a.H;
-  uint32_t samples = 0, hit = 0;
-  float4 dest = make_float4(0.f, 0.f, 0.f, 0.f);
-  float3 pos, dir;
-  if (active && ray_setup(a, px, py, pos, dir)) {
-    hit = 1;
-    float4 src = make_float4(0.f, 0.f, 0.f, 0.f);
-    bool outside = false;
-    for (int j = 0; !outside && j < a.num_iter; ++j) {
-      for (int i = 0; i < a.num_iter; ++i) {
-        const float4 f = Field<ST, LAYOUT>::sample(a, pos);
-        const float4 tf = tf_rgba(s_tf, a.tf_index == VVLIC_TF_INDEX_MAGNITUDE ? f.w : f.z);
-        float4 il = compute_lic<ST, LAYOUT, INTEG, GRAD>(a, pos, f);
-        ++samples;
-        il.w *= a.intensity_scale;
-        src = shade(a, s_tf, il, tf, pos, dir);
-        dest = blend(dest, src);
-        pos = add3(pos, scl3(dir, a.step_size));
-        outside = outside_box(a, pos) || src.w > a.alpha_thr;
-        if (outside) break;
-      }
-    }
-  }
-  if (active) {
-    const size_t pix = (size_t)py * a.W + px;
-    reinterpret_cast<float4*>(a.out)[pix] = dest;
-    if (a.samples) a.samples[pix] = samples;
-  }
-  // per-warp reduction of the counters
+__device__ __forceinline__ void store_pixel(const RenderArgs& a, int px, int py, float4 dest, uint32_t samples) {
+  const size_t pix = (size_t)py * a.W + px;
+  reinterpret_cast<float4*>(a.out)[pix] = dest;
+  if (a.samples) a.samples[pix] = samples;
+}
+
+__device__ __forceinline__ void flush_counters(const RenderArgs& a, uint32_t samples, uint32_t hits) {
   unsigned s = __reduce_add_sync(0xffffffffu, samples);
-  unsigned h = __reduce_add_sync(0xffffffffu, hit);
+  unsigned h = __reduce_add_sync(0xffffffffu, hits);
   if ((threadIdx.x & 31) == 0) {
     if (s) atomicAdd(a.counters + 0, (unsigned long long)s);
     if (h) atomicAdd(a.counters + 1, (unsigned long long)h);
   }
 }
 
-template <int ST, int LAYOUT, int INTEG, bool GRAD>
-static cudaError_t launch_one(const RenderArgs& a, cudaStream_t stream) {
-  dim3 grid((a.W + kTileW - 1) / kTileW, (a.H + kTileH - 1) / kTileH);
-  raycast_kernel<ST, LAYOUT, INTEG, GRAD><<<grid, kTileW * kTileH, 0, stream>>>(a);
+template <int ST, int FL, int NL, int INTEG, bool GRAD>
+__global__ void __launch_bounds__(kThreads) raycast_kernel(const __grid_constant__ RenderArgs a) {
+  __shared__ __align__(16) float s_tf[5 * VVLIC_TF_ENTRIES];
+  load_tf(a, s_tf);
+  const int px = blockIdx.x * kTileW + (threadIdx.x % kTileW);
+  const int py = blockIdx.y * kTileH + (threadIdx.x / kTileW);
+  uint32_t samples = 0, hit = 0;
+  if (px < a.W && py < a.H) {
+    float4 dest = trace_pixel<ST, FL, NL, INTEG, GRAD>(a, s_tf, px, py, samples, hit);
+    store_pixel(a, px, py, dest, samples);
+  }
+  flush_counters(a, samples, hit);
+}
+
+template <int ST, int FL, int NL, int INTEG, bool GRAD>
+__global__ void __launch_bounds__(kThreads) raycast_queue_kernel(const __grid_constant__ RenderArgs a,
+                                                                 const uint32_t* __restrict__ order, int ntiles,
+                                                                 unsigned* __restrict__ next) {
+  __shared__ __align__(16) float s_tf[5 * VVLIC_TF_ENTRIES];
+  load_tf(a, s_tf);
+  const int lane = threadIdx.x & 31;
+  const int tiles_x = (a.W + kWarpTileW - 1) / kWarpTileW;
+  uint32_t samples_acc = 0, hits_acc = 0;
+  for (;;) {
+    unsigned t = 0;
+    if (lane == 0) t = atomicAdd(next, 1u);
+    t = __shfl_sync(0xffffffffu, t, 0);
+    if (t >= (unsigned)ntiles) break;
+    const unsigned tile = __ldg(order + t);
+    const int px = (int)(tile % tiles_x) * kWarpTileW + (lane & (kWarpTileW - 1));
+    const int py = (int)(tile / tiles_x) * kWarpTileH + (lane / kWarpTileW);
+    if (px < a.W && py < a.H) {
+      uint32_t samples, hit;
+      float4 dest = trace_pixel<ST, FL, NL, INTEG, GRAD>(a, s_tf, px, py, samples, hit);
+      store_pixel(a, px, py, dest, samples);
+      samples_acc += samples;
+      hits_acc += hit;
+    }
+  }
+  flush_counters(a, samples_acc, hits_acc);
+}
+
+template <int ST, int FL, int NL, int INTEG, bool GRAD>
+static cudaError_t launch_one(const RenderArgs& a, const Schedule& sch, cudaStream_t stream) {
+  if (!sch.order) {
+    dim3 grid((a.W + kTileW - 1) / kTileW, (a.H + kTileH - 1) / kTileH);
+    raycast_kernel<ST, FL, NL, INTEG, GRAD><<<grid, kThreads, 0, stream>>>(a);
+    return cudaGetLastError();
+  }
+  auto kern = raycast_queue_kernel<ST, FL, NL, INTEG, GRAD>;
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, 0);
+  if (e != cudaSuccess) return e;
+  const int grid = std::max(1, per_sm) * sch.num_sms;
+  kern<<<grid, kThreads, 0, stream>>>(a, sch.order, sch.ntiles, sch.next);
   return cudaGetLastError();
 }
 
-template <int ST, int LAYOUT>
-static cudaError_t launch_layout(const RenderArgs& a, int integ, bool grad, cudaStream_t s) {
+template <int ST, int FL, int NL>
+static cudaError_t launch_layout(const RenderArgs& a, int integ, bool grad, const Schedule& sch, cudaStream_t s) {
   if (grad) {
-    if (integ == VVLIC_EULER) return launch_one<ST, LAYOUT, VVLIC_EULER, true>(a, s);
-    if (integ == VVLIC_HEUN) return launch_one<ST, LAYOUT, VVLIC_HEUN, true>(a, s);
-    return launch_one<ST, LAYOUT, VVLIC_RK4, true>(a, s);
+    if (integ == VVLIC_EULER) return launch_one<ST, FL, NL, VVLIC_EULER, true>(a, sch, s);
+    if (integ == VVLIC_HEUN) return launch_one<ST, FL, NL, VVLIC_HEUN, true>(a, sch, s);
+    return launch_one<ST, FL, NL, VVLIC_RK4, true>(a, sch, s);
   }
-  if (integ == VVLIC_EULER) return launch_one<ST, LAYOUT, VVLIC_EULER, false>(a, s);
-  if (integ == VVLIC_HEUN) return launch_one<ST, LAYOUT, VVLIC_HEUN, false>(a, s);
-  return launch_one<ST, LAYOUT, VVLIC_RK4, false>(a, s);
+  if (integ == VVLIC_EULER) return launch_one<ST, FL, NL, VVLIC_EULER, false>(a, sch, s);
+  if (integ == VVLIC_HEUN) return launch_one<ST, FL, NL, VVLIC_HEUN, false>(a, sch, s);
+  return launch_one<ST, FL, NL, VVLIC_RK4, false>(a, sch, s);
+}
+
+// Sampler (VVLIC_SAMPLER_*) -> (field layout, noise layout).
+template <int ST>
+static cudaError_t launch_storage(const RenderArgs& a, int sampler, int integ, bool grad, const Schedule& sch,
+                                  cudaStream_t s) {
+  switch (sampler) {
+    case VVLIC_SAMPLER_GATHER: return launch_layout<ST, kGather, kGather>(a, integ, grad, sch, s);
+    case VVLIC_SAMPLER_CELL: return launch_layout<ST, kCell, kCell>(a, integ, grad, sch, s);
+    case VVLIC_SAMPLER_TEXTURE:
+      if constexpr (ST == VVLIC_STORAGE_BF16) return cudaErrorNotSupported;  // no bf16 texture format
+      else return launch_layout<ST, kTexture, kTexture>(a, integ, grad, sch, s);
+    case VVLIC_SAMPLER_HYBRID:
+      if constexpr (ST == VVLIC_STORAGE_BF16) return cudaErrorNotSupported;
+      else return launch_layout<ST, kTexture, kCell>(a, integ, grad, sch, s);
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 }  // namespace vvlic

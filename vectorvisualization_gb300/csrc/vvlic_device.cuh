@@ -15,18 +15,17 @@ namespace vvlic {
 
 constexpr int kMaxTaps = 2 * VVLIC_MAX_STEPS + 1;
 
-// Field layouts (see VVLIC_SAMPLER_*).
+// Memory layouts a sampler reads (field and noise separately).
 enum Layout : int { kGather = 0, kCell = 1, kTexture = 2 };
 
-// Kernel arguments, passed by value as a __grid_constant__ parameter (≈2.4 KB, in the
-// constant bank; the taps are read warp-uniformly so they broadcast).
+// Kernel arguments of one render job, passed by value as a __grid_constant__ parameter (in
+// the constant bank; the taps are read warp-uniformly so they broadcast).
 struct RenderArgs {
   const void* field;          // GATHER: n0*n1*n2 RGBA texels; CELL: (n+1)^3 cells of 8 texels
   cudaTextureObject_t tex;    // TEXTURE layout
   int n[3];
   const uint8_t* noise;       // GATHER: m0*m1*m2 texels of noise_ch bytes; CELL: m^3 cells
   cudaTextureObject_t noise_tex;  // TEXTURE layout
-  int noise_cells;            // 1 when `noise` is the corner-packed cell array
   int m[3];
   int noise_ch;               // 1 (value) or 4 (gradient xyz, value)
   const float* scalar;        // optional gate volume
@@ -36,7 +35,6 @@ struct RenderArgs {
   uint32_t* samples;          // optional per-pixel sample counts
   unsigned long long* counters;  // [0] samples, [1] rays
   int W, H;
-  int pixel_offset;           // first linear pixel index of this launch (batching)
   float o0[3], o1[3], o2[3], d0[3], d1[3], d2[3];
   int clamp0;
   float ext[3], tex_max[3], scale_vol[3], scale_vol_inv[3];
@@ -65,19 +63,29 @@ __device__ __forceinline__ float lerpf(float a, float b, float t) { return fmaf(
 __device__ __forceinline__ float4 lerp4(float4 a, float4 b, float t) {
   return make_float4(lerpf(a.x, b.x, t), lerpf(a.y, b.y, t), lerpf(a.z, b.z, t), lerpf(a.w, b.w, t));
 }
+__device__ __forceinline__ float4 trilerp(float4 t000, float4 t100, float4 t010, float4 t110, float4 t001,
+                                          float4 t101, float4 t011, float4 t111, float ax, float ay, float az) {
+  float4 c0 = lerp4(lerp4(t000, t100, ax), lerp4(t010, t110, ax), ay);
+  float4 c1 = lerp4(lerp4(t001, t101, ax), lerp4(t011, t111, ax), ay);
+  return lerp4(c0, c1, az);
+}
 
 // ------------------------------------------------------------------------------------------
 // texel decoding per storage precision
 // ------------------------------------------------------------------------------------------
+__device__ __forceinline__ float4 unorm8x4(uint32_t r) {
+  const float k = 1.0f / 255.0f;
+  return make_float4((float)(r & 0xffu) * k, (float)((r >> 8) & 0xffu) * k, (float)((r >> 16) & 0xffu) * k,
+                     (float)(r >> 24) * k);
+}
+
 template <int ST> struct Texel;
 template <> struct Texel<VVLIC_STORAGE_F32> {
-  using raw = float4;
   static __device__ __forceinline__ float4 load(const void* base, int idx) {
     return __ldg(reinterpret_cast<const float4*>(base) + idx);
   }
 };
 template <> struct Texel<VVLIC_STORAGE_F16> {
-  using raw = uint2;
   static __device__ __forceinline__ float4 decode(uint2 r) {
     __half2 a = *reinterpret_cast<__half2*>(&r.x), b = *reinterpret_cast<__half2*>(&r.y);
     float2 fa = __half22float2(a), fb = __half22float2(b);
@@ -88,7 +96,6 @@ template <> struct Texel<VVLIC_STORAGE_F16> {
   }
 };
 template <> struct Texel<VVLIC_STORAGE_BF16> {
-  using raw = uint2;
   static __device__ __forceinline__ float4 decode(uint2 r) {
     // bf16 -> f32 is a 16-bit shift
     return make_float4(__uint_as_float(r.x << 16), __uint_as_float(r.x & 0xffff0000u), __uint_as_float(r.y << 16),
@@ -96,6 +103,11 @@ template <> struct Texel<VVLIC_STORAGE_BF16> {
   }
   static __device__ __forceinline__ float4 load(const void* base, int idx) {
     return decode(__ldg(reinterpret_cast<const uint2*>(base) + idx));
+  }
+};
+template <> struct Texel<VVLIC_STORAGE_UNORM8> {
+  static __device__ __forceinline__ float4 load(const void* base, int idx) {
+    return unorm8x4(__ldg(reinterpret_cast<const uint32_t*>(base) + idx));
   }
 };
 
@@ -126,13 +138,9 @@ template <int ST> struct Field<ST, kGather> {
     const int nx = a.n[0], nxy = a.n[0] * a.n[1];
     const int r00 = z0 * nxy + y0 * nx, r10 = z0 * nxy + y1 * nx, r01 = z1 * nxy + y0 * nx, r11 = z1 * nxy + y1 * nx;
     const void* f = a.field;
-    float4 t000 = Texel<ST>::load(f, r00 + x0), t100 = Texel<ST>::load(f, r00 + x1);
-    float4 t010 = Texel<ST>::load(f, r10 + x0), t110 = Texel<ST>::load(f, r10 + x1);
-    float4 t001 = Texel<ST>::load(f, r01 + x0), t101 = Texel<ST>::load(f, r01 + x1);
-    float4 t011 = Texel<ST>::load(f, r11 + x0), t111 = Texel<ST>::load(f, r11 + x1);
-    float4 c0 = lerp4(lerp4(t000, t100, ax), lerp4(t010, t110, ax), ay);
-    float4 c1 = lerp4(lerp4(t001, t101, ax), lerp4(t011, t111, ax), ay);
-    return lerp4(c0, c1, az);
+    return trilerp(Texel<ST>::load(f, r00 + x0), Texel<ST>::load(f, r00 + x1), Texel<ST>::load(f, r10 + x0),
+                   Texel<ST>::load(f, r10 + x1), Texel<ST>::load(f, r01 + x0), Texel<ST>::load(f, r01 + x1),
+                   Texel<ST>::load(f, r11 + x0), Texel<ST>::load(f, r11 + x1), ax, ay, az);
   }
 };
 
@@ -145,41 +153,40 @@ __device__ __forceinline__ void cell_axis(float s, int n, int& c, float& a) {
   a = u - fl;
   c = min((int)fl, n);
 }
+__device__ __forceinline__ int cell_index(const RenderArgs& a, float3 s, float& ax, float& ay, float& az) {
+  int cx, cy, cz;
+  cell_axis(s.x, a.n[0], cx, ax);
+  cell_axis(s.y, a.n[1], cy, ay);
+  cell_axis(s.z, a.n[2], cz, az);
+  return (cz * (a.n[1] + 1) + cy) * (a.n[0] + 1) + cx;
+}
 
-template <> struct Field<VVLIC_STORAGE_F32, kCell> {
+template <> struct Field<VVLIC_STORAGE_F32, kCell> {  // 128-byte cells, eight 16-byte loads
   static __device__ __forceinline__ float4 sample(const RenderArgs& a, float3 s) {
-    int cx, cy, cz;
     float ax, ay, az;
-    cell_axis(s.x, a.n[0], cx, ax);
-    cell_axis(s.y, a.n[1], cy, ay);
-    cell_axis(s.z, a.n[2], cz, az);
-    const int cnx = a.n[0] + 1, cny = a.n[1] + 1;
-    const float4* cell = reinterpret_cast<const float4*>(a.field) + 8 * ((cz * cny + cy) * cnx + cx);
-    float4 t000 = __ldg(cell + 0), t100 = __ldg(cell + 1), t010 = __ldg(cell + 2), t110 = __ldg(cell + 3);
-    float4 t001 = __ldg(cell + 4), t101 = __ldg(cell + 5), t011 = __ldg(cell + 6), t111 = __ldg(cell + 7);
-    float4 c0 = lerp4(lerp4(t000, t100, ax), lerp4(t010, t110, ax), ay);
-    float4 c1 = lerp4(lerp4(t001, t101, ax), lerp4(t011, t111, ax), ay);
-    return lerp4(c0, c1, az);
+    const float4* c = reinterpret_cast<const float4*>(a.field) + 8 * cell_index(a, s, ax, ay, az);
+    return trilerp(__ldg(c + 0), __ldg(c + 1), __ldg(c + 2), __ldg(c + 3), __ldg(c + 4), __ldg(c + 5), __ldg(c + 6),
+                   __ldg(c + 7), ax, ay, az);
   }
 };
-
 template <int ST> struct Field<ST, kCell> {  // F16 / BF16: 64-byte cells, four 16-byte loads
   static __device__ __forceinline__ float4 sample(const RenderArgs& a, float3 s) {
-    int cx, cy, cz;
     float ax, ay, az;
-    cell_axis(s.x, a.n[0], cx, ax);
-    cell_axis(s.y, a.n[1], cy, ay);
-    cell_axis(s.z, a.n[2], cz, az);
-    const int cnx = a.n[0] + 1, cny = a.n[1] + 1;
-    const uint4* cell = reinterpret_cast<const uint4*>(a.field) + 4 * ((cz * cny + cy) * cnx + cx);
-    uint4 q0 = __ldg(cell + 0), q1 = __ldg(cell + 1), q2 = __ldg(cell + 2), q3 = __ldg(cell + 3);
-    float4 t000 = Texel<ST>::decode(make_uint2(q0.x, q0.y)), t100 = Texel<ST>::decode(make_uint2(q0.z, q0.w));
-    float4 t010 = Texel<ST>::decode(make_uint2(q1.x, q1.y)), t110 = Texel<ST>::decode(make_uint2(q1.z, q1.w));
-    float4 t001 = Texel<ST>::decode(make_uint2(q2.x, q2.y)), t101 = Texel<ST>::decode(make_uint2(q2.z, q2.w));
-    float4 t011 = Texel<ST>::decode(make_uint2(q3.x, q3.y)), t111 = Texel<ST>::decode(make_uint2(q3.z, q3.w));
-    float4 c0 = lerp4(lerp4(t000, t100, ax), lerp4(t010, t110, ax), ay);
-    float4 c1 = lerp4(lerp4(t001, t101, ax), lerp4(t011, t111, ax), ay);
-    return lerp4(c0, c1, az);
+    const uint4* c = reinterpret_cast<const uint4*>(a.field) + 4 * cell_index(a, s, ax, ay, az);
+    uint4 q0 = __ldg(c + 0), q1 = __ldg(c + 1), q2 = __ldg(c + 2), q3 = __ldg(c + 3);
+    return trilerp(Texel<ST>::decode(make_uint2(q0.x, q0.y)), Texel<ST>::decode(make_uint2(q0.z, q0.w)),
+                   Texel<ST>::decode(make_uint2(q1.x, q1.y)), Texel<ST>::decode(make_uint2(q1.z, q1.w)),
+                   Texel<ST>::decode(make_uint2(q2.x, q2.y)), Texel<ST>::decode(make_uint2(q2.z, q2.w)),
+                   Texel<ST>::decode(make_uint2(q3.x, q3.y)), Texel<ST>::decode(make_uint2(q3.z, q3.w)), ax, ay, az);
+  }
+};
+template <> struct Field<VVLIC_STORAGE_UNORM8, kCell> {  // 32-byte cells, two 16-byte loads
+  static __device__ __forceinline__ float4 sample(const RenderArgs& a, float3 s) {
+    float ax, ay, az;
+    const uint4* c = reinterpret_cast<const uint4*>(a.field) + 2 * cell_index(a, s, ax, ay, az);
+    uint4 q0 = __ldg(c + 0), q1 = __ldg(c + 1);
+    return trilerp(unorm8x4(q0.x), unorm8x4(q0.y), unorm8x4(q0.z), unorm8x4(q0.w), unorm8x4(q1.x), unorm8x4(q1.y),
+                   unorm8x4(q1.z), unorm8x4(q1.w), ax, ay, az);
   }
 };
 
@@ -190,7 +197,8 @@ template <int ST> struct Field<ST, kTexture> {  // hardware trilinear, normalise
 };
 
 // ------------------------------------------------------------------------------------------
-// noise sampling: texture3D(noiseSampler, s), LINEAR + REPEAT (dataset.cpp:1333-1335), uint8/255
+// noise sampling: texture3D(noiseSampler, s), LINEAR + REPEAT (dataset.cpp:1333-1335), uint8/255.
+// Returns (gradient rgb, value); for a one-channel noise the gradient part is 0.
 // ------------------------------------------------------------------------------------------
 __device__ __forceinline__ void repeat_axis(float s, int m, int& i0, int& i1, float& a) {
   float u = fmaf(s, (float)m, -0.5f);
@@ -205,16 +213,51 @@ __device__ __forceinline__ void repeat_axis(float s, int m, int& i0, int& i1, fl
 
 __device__ __forceinline__ float bytef(uint32_t w, int k) { return (float)((w >> (8 * k)) & 0xffu); }
 
-// Returns (gradient rgb, value) / 255; for one-channel noise rgb = 0.
-template <bool RGBA> __device__ __forceinline__ float4 sample_noise(const RenderArgs& a, float3 s) {
-  int x0, x1, y0, y1, z0, z1;
-  float ax, ay, az;
-  repeat_axis(s.x, a.m[0], x0, x1, ax);
-  repeat_axis(s.y, a.m[1], y0, y1, ay);
-  repeat_axis(s.z, a.m[2], z0, z1, az);
-  const float k = 1.0f / 255.0f;
-  if (a.noise_cells) {
-    // cell (x0,y0,z0) holds the 8 corners; RGBA: 32 bytes, value-only: 8 bytes
+template <int NL> struct Noise;
+
+template <> struct Noise<kGather> {
+  template <bool RGBA> static __device__ __forceinline__ float4 sample(const RenderArgs& a, float3 s) {
+    int x0, x1, y0, y1, z0, z1;
+    float ax, ay, az;
+    repeat_axis(s.x, a.m[0], x0, x1, ax);
+    repeat_axis(s.y, a.m[1], y0, y1, ay);
+    repeat_axis(s.z, a.m[2], z0, z1, az);
+    const float k = 1.0f / 255.0f;
+    const int mx = a.m[0], mxy = a.m[0] * a.m[1];
+    const int r00 = z0 * mxy + y0 * mx, r10 = z0 * mxy + y1 * mx, r01 = z1 * mxy + y0 * mx, r11 = z1 * mxy + y1 * mx;
+    if (RGBA) {
+      const uint32_t* t = reinterpret_cast<const uint32_t*>(a.noise);
+      uint32_t t000 = __ldg(t + r00 + x0), t100 = __ldg(t + r00 + x1), t010 = __ldg(t + r10 + x0),
+               t110 = __ldg(t + r10 + x1), t001 = __ldg(t + r01 + x0), t101 = __ldg(t + r01 + x1),
+               t011 = __ldg(t + r11 + x0), t111 = __ldg(t + r11 + x1);
+      float4 r;
+      float* rp = &r.x;
+#pragma unroll
+      for (int ch = 0; ch < 4; ++ch) {
+        float c00 = lerpf(bytef(t000, ch), bytef(t100, ch), ax), c10 = lerpf(bytef(t010, ch), bytef(t110, ch), ax);
+        float c01 = lerpf(bytef(t001, ch), bytef(t101, ch), ax), c11 = lerpf(bytef(t011, ch), bytef(t111, ch), ax);
+        rp[ch] = lerpf(lerpf(c00, c10, ay), lerpf(c01, c11, ay), az) * k;
+      }
+      return r;
+    }
+    const uint8_t* t = a.noise;
+    float c00 = lerpf((float)__ldg(t + r00 + x0), (float)__ldg(t + r00 + x1), ax);
+    float c10 = lerpf((float)__ldg(t + r10 + x0), (float)__ldg(t + r10 + x1), ax);
+    float c01 = lerpf((float)__ldg(t + r01 + x0), (float)__ldg(t + r01 + x1), ax);
+    float c11 = lerpf((float)__ldg(t + r11 + x0), (float)__ldg(t + r11 + x1), ax);
+    return make_float4(0.f, 0.f, 0.f, lerpf(lerpf(c00, c10, ay), lerpf(c01, c11, ay), az) * k);
+  }
+};
+
+// Noise cells (REPEAT): cell (x0,y0,z0) holds the 8 corners; RGBA: 32 bytes, value-only: 8 bytes.
+template <> struct Noise<kCell> {
+  template <bool RGBA> static __device__ __forceinline__ float4 sample(const RenderArgs& a, float3 s) {
+    int x0, x1, y0, y1, z0, z1;
+    float ax, ay, az;
+    repeat_axis(s.x, a.m[0], x0, x1, ax);
+    repeat_axis(s.y, a.m[1], y0, y1, ay);
+    repeat_axis(s.z, a.m[2], z0, z1, az);
+    const float k = 1.0f / 255.0f;
     const int cidx = (z0 * a.m[1] + y0) * a.m[0] + x0;
     if (RGBA) {
       const uint4* c = reinterpret_cast<const uint4*>(a.noise) + 2 * cidx;
@@ -228,42 +271,26 @@ template <bool RGBA> __device__ __forceinline__ float4 sample_noise(const Render
         rp[ch] = lerpf(lerpf(c00, c10, ay), lerpf(c01, c11, ay), az) * k;
       }
       return r;
-    } else {
-      uint2 q = __ldg(reinterpret_cast<const uint2*>(a.noise) + cidx);
-      float c00 = lerpf(bytef(q.x, 0), bytef(q.x, 1), ax), c10 = lerpf(bytef(q.x, 2), bytef(q.x, 3), ax);
-      float c01 = lerpf(bytef(q.y, 0), bytef(q.y, 1), ax), c11 = lerpf(bytef(q.y, 2), bytef(q.y, 3), ax);
-      return make_float4(0.f, 0.f, 0.f, lerpf(lerpf(c00, c10, ay), lerpf(c01, c11, ay), az) * k);
     }
-  }
-  const int mx = a.m[0], mxy = a.m[0] * a.m[1];
-  const int r00 = z0 * mxy + y0 * mx, r10 = z0 * mxy + y1 * mx, r01 = z1 * mxy + y0 * mx, r11 = z1 * mxy + y1 * mx;
-  if (RGBA) {
-    const uint32_t* t = reinterpret_cast<const uint32_t*>(a.noise);
-    uint32_t t000 = __ldg(t + r00 + x0), t100 = __ldg(t + r00 + x1), t010 = __ldg(t + r10 + x0),
-             t110 = __ldg(t + r10 + x1), t001 = __ldg(t + r01 + x0), t101 = __ldg(t + r01 + x1),
-             t011 = __ldg(t + r11 + x0), t111 = __ldg(t + r11 + x1);
-    float4 r;
-    float* rp = &r.x;
-#pragma unroll
-    for (int ch = 0; ch < 4; ++ch) {
-      float c00 = lerpf(bytef(t000, ch), bytef(t100, ch), ax), c10 = lerpf(bytef(t010, ch), bytef(t110, ch), ax);
-      float c01 = lerpf(bytef(t001, ch), bytef(t101, ch), ax), c11 = lerpf(bytef(t011, ch), bytef(t111, ch), ax);
-      rp[ch] = lerpf(lerpf(c00, c10, ay), lerpf(c01, c11, ay), az) * k;
-    }
-    return r;
-  } else {
-    const uint8_t* t = a.noise;
-    float c00 = lerpf((float)__ldg(t + r00 + x0), (float)__ldg(t + r00 + x1), ax);
-    float c10 = lerpf((float)__ldg(t + r10 + x0), (float)__ldg(t + r10 + x1), ax);
-    float c01 = lerpf((float)__ldg(t + r01 + x0), (float)__ldg(t + r01 + x1), ax);
-    float c11 = lerpf((float)__ldg(t + r11 + x0), (float)__ldg(t + r11 + x1), ax);
+    uint2 q = __ldg(reinterpret_cast<const uint2*>(a.noise) + cidx);
+    float c00 = lerpf(bytef(q.x, 0), bytef(q.x, 1), ax), c10 = lerpf(bytef(q.x, 2), bytef(q.x, 3), ax);
+    float c01 = lerpf(bytef(q.y, 0), bytef(q.y, 1), ax), c11 = lerpf(bytef(q.y, 2), bytef(q.y, 3), ax);
     return make_float4(0.f, 0.f, 0.f, lerpf(lerpf(c00, c10, ay), lerpf(c01, c11, ay), az) * k);
   }
-}
+};
 
-// Value-only read of an RGBA noise (its .a channel), for the non-gradient LIC over -g noise.
-__device__ __forceinline__ float noise_value(const RenderArgs& a, float3 s) {
-  return a.noise_ch == 4 ? sample_noise<true>(a, s).w : sample_noise<false>(a, s).w;
+// Noise through the texture unit: RGBA8 / R8 read as normalised float (x/255), LINEAR filter,
+// WRAP addressing on normalised coordinates — GL's REPEAT.
+template <> struct Noise<kTexture> {
+  template <bool RGBA> static __device__ __forceinline__ float4 sample(const RenderArgs& a, float3 s) {
+    if (RGBA) return tex3D<float4>(a.noise_tex, s.x, s.y, s.z);
+    return make_float4(0.f, 0.f, 0.f, tex3D<float>(a.noise_tex, s.x, s.y, s.z));
+  }
+};
+
+// Value of the noise (.a): from an RGBA (-g) noise or a one-channel one.
+template <int NL> __device__ __forceinline__ float noise_value(const RenderArgs& a, float3 s) {
+  return a.noise_ch == 4 ? Noise<NL>::template sample<true>(a, s).w : Noise<NL>::template sample<false>(a, s).w;
 }
 
 __device__ __forceinline__ float sample_scalar(const RenderArgs& a, float3 s) {
@@ -310,9 +337,9 @@ __device__ __forceinline__ float3 slope(float4 f) { return f3(2.0f * f.x - 1.0f,
 
 // One streamline step; replaces `step` with the field value at the new position (the
 // first-same-as-last reuse of the reference's `step` in/out argument).
-template <int ST, int LAYOUT, int INTEG>
+template <int ST, int FL, int INTEG>
 __device__ __forceinline__ float3 lic_step(const RenderArgs& a, float3 p, float4& step, float dirs) {
-  using F = Field<ST, LAYOUT>;
+  using F = Field<ST, FL>;
   const float hs = a.h_eff * dirs * (a.sof ? step.w : 1.0f);
   float3 k1 = scl3(slope(step), hs);
   if (INTEG == VVLIC_EULER) {
@@ -330,34 +357,18 @@ __device__ __forceinline__ float3 lic_step(const RenderArgs& a, float3 p, float4
   return p;
 }
 
-// Noise through the texture unit: RGBA8 / R8 read as normalised float (x/255), LINEAR filter,
-// WRAP addressing on normalised coordinates — GL's REPEAT (dataset.cpp:1333-1335).
-template <bool RGBA> __device__ __forceinline__ float4 sample_noise_tex(const RenderArgs& a, float3 s) {
-  if (RGBA) return tex3D<float4>(a.noise_tex, s.x, s.y, s.z);
-  return make_float4(0.f, 0.f, 0.f, tex3D<float>(a.noise_tex, s.x, s.y, s.z));
-}
-
-template <int LAYOUT> __device__ __forceinline__ float4 noise_rgba(const RenderArgs& a, float3 s) {
-  if (LAYOUT == kTexture) return sample_noise_tex<true>(a, s);
-  return sample_noise<true>(a, s);
-}
-template <int LAYOUT> __device__ __forceinline__ float noise_val(const RenderArgs& a, float3 s) {
-  if (LAYOUT == kTexture) return a.noise_ch == 4 ? sample_noise_tex<true>(a, s).w : sample_noise_tex<false>(a, s).w;
-  return noise_value(a, s);
-}
-
 // freqSampling / freqSamplingGrad (inc_lic.glsl:124-153)
-template <int LAYOUT, bool GRAD> __device__ __forceinline__ float4 noise_tap(const RenderArgs& a, float3 p) {
+template <int NL, bool GRAD> __device__ __forceinline__ float4 noise_tap(const RenderArgs& a, float3 p) {
   if (GRAD) {
     const bool nofreq = (a.quirks & VVLIC_QUIRK_GRAD_NOISE_NO_FREQ) != 0;
-    return noise_rgba<LAYOUT>(a, nofreq ? p : scl3(p, a.freq_scale));
+    return Noise<NL>::template sample<true>(a, nofreq ? p : scl3(p, a.freq_scale));
   }
   if (a.gate) {
     float s = sample_scalar(a, p);
     if (!(s > a.gate_lo && s < a.gate_hi)) return make_float4(0.f, 0.f, 0.f, 0.f);
   }
   if (a.quirks & VVLIC_QUIRK_LUMINANCE_NOISE) return make_float4(0.f, 0.f, 0.f, 1.0f);
-  return make_float4(0.f, 0.f, 0.f, noise_val<LAYOUT>(a, scl3(p, a.freq_scale)));
+  return make_float4(0.f, 0.f, 0.f, noise_value<NL>(a, scl3(p, a.freq_scale)));
 }
 
 template <bool GRAD> __device__ __forceinline__ void accumulate(float4& acc, float4 n, float w) {
@@ -373,11 +384,11 @@ template <bool GRAD> __device__ __forceinline__ void accumulate(float4& acc, flo
 // The backward and forward streamlines are independent, so they advance in the same loop
 // iteration: two dependent gather chains per thread instead of one (the sum is reassociated
 // relative to the reference's backward-then-forward order).
-template <int ST, int LAYOUT, int INTEG, bool GRAD>
+template <int ST, int FL, int NL, int INTEG, bool GRAD>
 __device__ __forceinline__ float4 compute_lic(const RenderArgs& a, float3 pos, float4 f0) {
   const int lb = a.lb, lf = a.lf;
   const int both = min(lb, lf);
-  float4 n0 = noise_tap<LAYOUT, GRAD>(a, pos);
+  float4 n0 = noise_tap<NL, GRAD>(a, pos);
   float w0 = a.taps[lb];
   float4 accb = make_float4(n0.x * w0, n0.y * w0, n0.z * w0, n0.w * w0);
   float4 accf = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -385,20 +396,20 @@ __device__ __forceinline__ float4 compute_lic(const RenderArgs& a, float3 pos, f
   float4 sb = f0, sf = f0;
   int i = 1;
   for (; i <= both; ++i) {
-    pb = lic_step<ST, LAYOUT, INTEG>(a, pb, sb, -1.0f);
-    pf = lic_step<ST, LAYOUT, INTEG>(a, pf, sf, 1.0f);
-    float4 nb = noise_tap<LAYOUT, GRAD>(a, pb);
-    float4 nf = noise_tap<LAYOUT, GRAD>(a, pf);
+    pb = lic_step<ST, FL, INTEG>(a, pb, sb, -1.0f);
+    pf = lic_step<ST, FL, INTEG>(a, pf, sf, 1.0f);
+    float4 nb = noise_tap<NL, GRAD>(a, pb);
+    float4 nf = noise_tap<NL, GRAD>(a, pf);
     accumulate<GRAD>(accb, nb, a.taps[lb - i]);
     accumulate<GRAD>(accf, nf, a.taps[lb + i]);
   }
   for (int j = i; j <= lb; ++j) {
-    pb = lic_step<ST, LAYOUT, INTEG>(a, pb, sb, -1.0f);
-    accumulate<GRAD>(accb, noise_tap<LAYOUT, GRAD>(a, pb), a.taps[lb - j]);
+    pb = lic_step<ST, FL, INTEG>(a, pb, sb, -1.0f);
+    accumulate<GRAD>(accb, noise_tap<NL, GRAD>(a, pb), a.taps[lb - j]);
   }
   for (int j = i; j <= lf; ++j) {
-    pf = lic_step<ST, LAYOUT, INTEG>(a, pf, sf, 1.0f);
-    accumulate<GRAD>(accf, noise_tap<LAYOUT, GRAD>(a, pf), a.taps[lb + j]);
+    pf = lic_step<ST, FL, INTEG>(a, pf, sf, 1.0f);
+    accumulate<GRAD>(accf, noise_tap<NL, GRAD>(a, pf), a.taps[lb + j]);
   }
   return make_float4(accb.x + accf.x, accb.y + accf.y, accb.z + accf.z, accb.w + accf.w);
 }
@@ -446,17 +457,18 @@ __device__ __forceinline__ float4 blend(float4 dest, float4 src) {
                      __saturatef(fmaf(om, src.z, dest.z)), __saturatef(fmaf(om, src.w, dest.w)));
 }
 
-// Per-pixel ray: slab test against [0, extent] and the reference's start position
-// pos = objPos * scaleVol, dir = normalize(objPos - eye) * scaleVol (lic3d_fragment.glsl:12-21).
-__device__ __forceinline__ bool ray_setup(const RenderArgs& a, int px, int py, float3& pos, float3& dir) {
+// Parametric interval of a pixel's ray inside [0, extent] (the cube faces the reference
+// rasterises, renderer.cpp:682-736); false for a miss.
+__device__ __forceinline__ bool ray_interval(const RenderArgs& a, int px, int py, float o[3], float d[3], float& tn,
+                                             float& tf) {
   const float u = (float)px + 0.5f, v = (float)py + 0.5f;
-  float o[3], d[3];
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
     o[i] = a.o0[i] + u * a.o1[i] + v * a.o2[i];
     d[i] = a.d0[i] + u * a.d1[i] + v * a.d2[i];
   }
-  float tn = -INFINITY, tf = INFINITY;
+  tn = -INFINITY;
+  tf = INFINITY;
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
     if (d[i] == 0.0f) {
@@ -473,6 +485,14 @@ __device__ __forceinline__ bool ray_setup(const RenderArgs& a, int px, int py, f
     if (!(tf > 0.0f)) return false;
     tn = fmaxf(tn, 0.0f);
   }
+  return true;
+}
+
+// Per-pixel ray start: pos = objPos * scaleVol, dir = normalize(objPos - eye) * scaleVol
+// (lic3d_fragment.glsl:12-21).
+__device__ __forceinline__ bool ray_setup(const RenderArgs& a, int px, int py, float3& pos, float3& dir) {
+  float o[3], d[3], tn, tf;
+  if (!ray_interval(a, px, py, o, d, tn, tf)) return false;
   const float3 sv = f3(a.scale_vol[0], a.scale_vol[1], a.scale_vol[2]);
   pos = mul3(f3(o[0] + tn * d[0], o[1] + tn * d[1], o[2] + tn * d[2]), sv);
   dir = mul3(norm3(f3(d[0], d[1], d[2])), sv);
@@ -481,6 +501,35 @@ __device__ __forceinline__ bool ray_setup(const RenderArgs& a, int px, int py, f
 
 __device__ __forceinline__ bool outside_box(const RenderArgs& a, float3 p) {
   return p.x < 0.0f || p.y < 0.0f || p.z < 0.0f || p.x > a.tex_max[0] || p.y > a.tex_max[1] || p.z > a.tex_max[2];
+}
+
+// The whole lic3d_fragment.glsl main() for one pixel: returns dest, counts samples.
+template <int ST, int FL, int NL, int INTEG, bool GRAD>
+__device__ __forceinline__ float4 trace_pixel(const RenderArgs& a, const float* s_tf, int px, int py,
+                                              uint32_t& samples, uint32_t& hit) {
+  float4 dest = make_float4(0.f, 0.f, 0.f, 0.f);
+  float3 pos, dir;
+  samples = 0;
+  hit = 0;
+  if (!ray_setup(a, px, py, pos, dir)) return dest;
+  hit = 1;
+  float4 src = make_float4(0.f, 0.f, 0.f, 0.f);
+  bool outside = false;
+  for (int j = 0; !outside && j < a.num_iter; ++j) {
+    for (int i = 0; i < a.num_iter; ++i) {
+      const float4 f = Field<ST, FL>::sample(a, pos);
+      const float4 tf = tf_rgba(s_tf, a.tf_index == VVLIC_TF_INDEX_MAGNITUDE ? f.w : f.z);
+      float4 il = compute_lic<ST, FL, NL, INTEG, GRAD>(a, pos, f);
+      ++samples;
+      il.w *= a.intensity_scale;
+      src = shade(a, s_tf, il, tf, pos, dir);
+      dest = blend(dest, src);
+      pos = add3(pos, scl3(dir, a.step_size));
+      outside = outside_box(a, pos) || src.w > a.alpha_thr;
+      if (outside) break;
+    }
+  }
+  return dest;
 }
 
 }  // namespace vvlic

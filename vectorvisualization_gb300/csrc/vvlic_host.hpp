@@ -100,6 +100,9 @@ struct vvlic_ctx {
   size_t image_cap = 0;
   void* d_upload = nullptr;
   size_t upload_cap = 0;
+  unsigned* d_sched = nullptr;    // tile order scratch of the queue schedule
+  size_t sched_cap = 0;           // in 4-byte words
+  int num_sms = 1;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   bool stats_pending = false;
   uint64_t stats_steps_per_sample = 0;

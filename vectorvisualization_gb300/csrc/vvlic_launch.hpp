@@ -4,14 +4,35 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
+
 namespace vvlic {
 
 struct RenderArgs;
 
-// Forward ray-cast, one launcher per field storage (render_f32.cu / render_f16.cu / render_bf16.cu).
-cudaError_t launch_raycast_f32(const RenderArgs& a, int layout, int integ, bool grad, cudaStream_t s);
-cudaError_t launch_raycast_f16(const RenderArgs& a, int layout, int integ, bool grad, cudaStream_t s);
-cudaError_t launch_raycast_bf16(const RenderArgs& a, int layout, int integ, bool grad, cudaStream_t s);
+// Work distribution of one render launch: `order` == nullptr selects the static raster grid;
+// otherwise persistent CTAs pull `ntiles` 8x4 tiles in `order` through the counter `next`.
+struct Schedule {
+  const uint32_t* order = nullptr;
+  int ntiles = 0;
+  unsigned* next = nullptr;
+  int num_sms = 1;
+};
+
+// Forward ray-cast, one launcher per field storage (render_<storage>.cu).
+cudaError_t launch_raycast_f32(const RenderArgs& a, int sampler, int integ, bool grad, const Schedule& sch,
+                               cudaStream_t s);
+cudaError_t launch_raycast_f16(const RenderArgs& a, int sampler, int integ, bool grad, const Schedule& sch,
+                               cudaStream_t s);
+cudaError_t launch_raycast_bf16(const RenderArgs& a, int sampler, int integ, bool grad, const Schedule& sch,
+                                cudaStream_t s);
+cudaError_t launch_raycast_u8(const RenderArgs& a, int sampler, int integ, bool grad, const Schedule& sch,
+                              cudaStream_t s);
+
+// Longest-first tile order for the queue schedule (render.cu): per-tile chord cost, a
+// counting sort over 1024 cost buckets, scatter.  `scratch` holds 2*ntiles + 2048 + 1 words.
+cudaError_t launch_tile_order(const RenderArgs& a, int ntiles, int tiles_x, int shift, unsigned* scratch,
+                              cudaStream_t s);
 
 // Preprocessing (preprocess.cu, compiled without FMA contraction so results match the
 // reference's CPU arithmetic bit for bit).
@@ -27,5 +48,8 @@ cudaError_t launch_build_field_cells(const void* d_texels, const int n[3], int s
                                      cudaStream_t s);
 cudaError_t launch_build_noise_cells(const uint8_t* d_texels, const int m[3], int ch, uint8_t* d_cells,
                                      cudaStream_t s);
+
+// Bytes per texel of a field storage.
+inline int texel_bytes(int storage) { return storage == 0 ? 16 : (storage == 3 ? 4 : 8); }
 
 }  // namespace vvlic
