@@ -41,8 +41,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--storage", default="f16", choices=["f32", "f16", "bf16"])
-    ap.add_argument("--sampler", default="cell", choices=["gather", "cell", "texture"])
+    ap.add_argument("--storage", default="f16", choices=["f32", "f16", "bf16", "u8"])
+    ap.add_argument("--sampler", default="hybrid", choices=["gather", "cell", "texture", "hybrid"])
+    ap.add_argument("--schedule", default="queue", choices=["queue", "static"])
     ap.add_argument("--size", type=int, default=256)
     ap.add_argument("--image", type=int, default=1024)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
@@ -269,6 +270,7 @@ def run_ours(args, dist: Dist):
     vid = wl.setup_context(ctx, w)
     p = w.params
     p.sampler = capi.SAMPLER[args.sampler]
+    p.schedule = capi.SCHEDULE[args.schedule]
     ctx.set_params(p)
     stream = torch.cuda.Stream(device=dev)
     sh = stream.cuda_stream
@@ -336,7 +338,7 @@ def run_ours(args, dist: Dist):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded SplitMix64 vortex field and noise; the reference ships no datasets)",
-        "config": {**w.describe(), "sampler": args.sampler,
+        "config": {**w.describe(), "sampler": args.sampler, "schedule": args.schedule,
                    "l2": "flushed between frames (256 MiB write); inputs > L2",
                    "sample_steps_per_frame": int(st.sample_steps), "samples_per_frame": int(st.samples),
                    "rays": int(st.rays), "parallelism": f"replicas x{dist.world}"},

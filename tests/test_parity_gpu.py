@@ -257,7 +257,7 @@ def test_lighting_uniform_scale_bug_off(ctx, oracle):
 
 
 def test_scalar_gate(ctx, oracle):
-    w = small(scalar_gate=1)
+    w = small(scalar_gate=1, sampler=capi.SAMPLER["cell"])
     nz, ny, nx = w.field.shape[:3]
     zz = (np.arange(nz) + 0.5) / nz
     scalar = np.broadcast_to(zz[:, None, None], (nz, ny, nx)).astype(np.float32).copy() * 0.5
@@ -310,7 +310,7 @@ def test_filters_and_clamp_modes(ctx, oracle):
 
 
 def test_explicit_taps(ctx, oracle):
-    w = small()
+    w = small(sampler=capi.SAMPLER["cell"])
     taps = np.linspace(0.2, 1.0, 13).astype(np.float64)
     sc = oracle.Scene(oracle.encode_field(w.field), w.noise, w.tf_rgba, w.tf_opac, taps=taps, inv_filter_area=0.7)
     ref, _ = sc.render(w.params, w.views[0], w.width, w.height)
