@@ -73,10 +73,16 @@ __device__ __forceinline__ float4 trilerp(float4 t000, float4 t100, float4 t010,
 // ------------------------------------------------------------------------------------------
 // texel decoding per storage precision
 // ------------------------------------------------------------------------------------------
+// Byte k of w as an exact float without a conversion instruction: assemble the bit pattern
+// 0x4B0000bb (= 2^23 + b) with one byte permute and subtract 2^23.
+__device__ __forceinline__ float byte_as_float(uint32_t w, int k) {
+  return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u + (unsigned)k)) - 8388608.0f;
+}
+
 __device__ __forceinline__ float4 unorm8x4(uint32_t r) {
   const float k = 1.0f / 255.0f;
-  return make_float4((float)(r & 0xffu) * k, (float)((r >> 8) & 0xffu) * k, (float)((r >> 16) & 0xffu) * k,
-                     (float)(r >> 24) * k);
+  return make_float4(byte_as_float(r, 0) * k, byte_as_float(r, 1) * k, byte_as_float(r, 2) * k,
+                     byte_as_float(r, 3) * k);
 }
 
 template <int ST> struct Texel;
@@ -249,33 +255,60 @@ template <> struct Noise<kGather> {
   }
 };
 
+// REPEAT wrap: power-of-two extents use a mask, others the integer remainder.
+__device__ __forceinline__ void repeat_axis_fast(float s, int m, int& i0, int& i1, float& a) {
+  float u = fmaf(s, (float)m, -0.5f);
+  u = fminf(fmaxf(u, -16777216.0f), 16777216.0f);
+  float fl = floorf(u);
+  a = u - fl;
+  int b = (int)fl;
+  if ((m & (m - 1)) == 0) {
+    i0 = b & (m - 1);
+    i1 = (b + 1) & (m - 1);
+  } else {
+    b %= m;
+    if (b < 0) b += m;
+    i0 = b;
+    i1 = (b + 1 == m) ? 0 : b + 1;
+  }
+}
+
 // Noise cells (REPEAT): cell (x0,y0,z0) holds the 8 corners; RGBA: 32 bytes, value-only: 8 bytes.
+// The eight trilinear weights are formed once and applied to every channel.
 template <> struct Noise<kCell> {
   template <bool RGBA> static __device__ __forceinline__ float4 sample(const RenderArgs& a, float3 s) {
     int x0, x1, y0, y1, z0, z1;
     float ax, ay, az;
-    repeat_axis(s.x, a.m[0], x0, x1, ax);
-    repeat_axis(s.y, a.m[1], y0, y1, ay);
-    repeat_axis(s.z, a.m[2], z0, z1, az);
+    repeat_axis_fast(s.x, a.m[0], x0, x1, ax);
+    repeat_axis_fast(s.y, a.m[1], y0, y1, ay);
+    repeat_axis_fast(s.z, a.m[2], z0, z1, az);
     const float k = 1.0f / 255.0f;
+    const float bx = 1.0f - ax, by = 1.0f - ay, bz = 1.0f - az;
+    const float w00 = by * bz, w10 = ay * bz, w01 = by * az, w11 = ay * az;
+    const float w[8] = {bx * w00, ax * w00, bx * w10, ax * w10, bx * w01, ax * w01, bx * w11, ax * w11};
     const int cidx = (z0 * a.m[1] + y0) * a.m[0] + x0;
     if (RGBA) {
       const uint4* c = reinterpret_cast<const uint4*>(a.noise) + 2 * cidx;
-      uint4 q0 = __ldg(c), q1 = __ldg(c + 1);
-      float4 r;
-      float* rp = &r.x;
+      const uint4 q0 = __ldg(c), q1 = __ldg(c + 1);
+      const uint32_t t[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
+      float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-      for (int ch = 0; ch < 4; ++ch) {
-        float c00 = lerpf(bytef(q0.x, ch), bytef(q0.y, ch), ax), c10 = lerpf(bytef(q0.z, ch), bytef(q0.w, ch), ax);
-        float c01 = lerpf(bytef(q1.x, ch), bytef(q1.y, ch), ax), c11 = lerpf(bytef(q1.z, ch), bytef(q1.w, ch), ax);
-        rp[ch] = lerpf(lerpf(c00, c10, ay), lerpf(c01, c11, ay), az) * k;
+      for (int i = 0; i < 8; ++i) {
+        r.x = fmaf(w[i], byte_as_float(t[i], 0), r.x);
+        r.y = fmaf(w[i], byte_as_float(t[i], 1), r.y);
+        r.z = fmaf(w[i], byte_as_float(t[i], 2), r.z);
+        r.w = fmaf(w[i], byte_as_float(t[i], 3), r.w);
       }
-      return r;
+      return make_float4(r.x * k, r.y * k, r.z * k, r.w * k);
     }
-    uint2 q = __ldg(reinterpret_cast<const uint2*>(a.noise) + cidx);
-    float c00 = lerpf(bytef(q.x, 0), bytef(q.x, 1), ax), c10 = lerpf(bytef(q.x, 2), bytef(q.x, 3), ax);
-    float c01 = lerpf(bytef(q.y, 0), bytef(q.y, 1), ax), c11 = lerpf(bytef(q.y, 2), bytef(q.y, 3), ax);
-    return make_float4(0.f, 0.f, 0.f, lerpf(lerpf(c00, c10, ay), lerpf(c01, c11, ay), az) * k);
+    const uint2 q = __ldg(reinterpret_cast<const uint2*>(a.noise) + cidx);
+    float v = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      v = fmaf(w[i], byte_as_float(q.x, i), v);
+      v = fmaf(w[4 + i], byte_as_float(q.y, i), v);
+    }
+    return make_float4(0.f, 0.f, 0.f, v * k);
   }
 };
 
