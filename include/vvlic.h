@@ -143,7 +143,7 @@ typedef struct vvlic_params {
   float light_specular[3];/* (1,1,1) */
   float light_ambient[3]; /* (0,0,0) */
   /* kernel selection (no reference counterpart) */
-  int32_t sampler;        /* VVLIC_SAMPLER_* (TEXTURE) */
+  int32_t sampler;        /* VVLIC_SAMPLER_* (HYBRID) */
   int32_t schedule;       /* VVLIC_SCHEDULE_* (QUEUE) */
   int32_t reserved[6];
 } vvlic_params;

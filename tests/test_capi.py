@@ -54,7 +54,7 @@ def test_params_default_is_reference_licparams(vvlic_lib):
     assert p.quirks == capi.QUIRKS_REFERENCE and p.spec_exp == 40.0
     assert list(p.light_pos) == [0.5, 0.5, 1.5]
     assert list(p.light_ambient) == [0.0, 0.0, 0.0] and list(p.light_specular) == [1.0, 1.0, 1.0]
-    assert p.sampler == capi.SAMPLER["texture"] and p.schedule == capi.SCHEDULE["queue"]
+    assert p.sampler == capi.SAMPLER["hybrid"] and p.schedule == capi.SCHEDULE["queue"]
 
 
 def test_view_default_is_reference_camera(vvlic_lib):

@@ -198,7 +198,7 @@ extern "C" void vvlic_params_default(vvlic_params* p) {
     p->light_specular[i] = 1.0f;
     p->light_ambient[i] = 0.0f;
   }
-  p->sampler = VVLIC_SAMPLER_TEXTURE;
+  p->sampler = VVLIC_SAMPLER_HYBRID;
   p->schedule = VVLIC_SCHEDULE_QUEUE;
 }
 
