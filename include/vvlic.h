@@ -302,6 +302,28 @@ vvlic_status vvlic_noise_gradients_device(const uint8_t* d_noise, int32_t mx, in
                                           int32_t mz, int32_t mode, const float* slice_dist,
                                           uint8_t* d_rgba, void* stream);
 
+/* Largest noise (voxels) vvlic_noise_gradients_device_noalloc accepts: its fixed 12 MiB
+ * gradient scratch holds three floats per voxel. */
+#define VVLIC_NOALLOC_MAX_VOXELS (1u << 20)
+
+/* No counterpart in the reference.  The same computation and output as
+ * vvlic_noise_gradients_device, for callers that must not allocate device memory during the
+ * call: applications that reserve their GPU memory budget at start-up and forbid later
+ * allocations, or frame loops that cannot afford allocator latency and cudaFree's implicit
+ * synchronisation.  The temporary gradients live in a fixed device array compiled into the
+ * library (VVLIC_NOALLOC_MAX_VOXELS * 12 bytes, held on every GPU that loads the library until
+ * the process exits); the caller still passes the input and output buffers.
+ *   - Runs on the current CUDA device.  The first call on a device looks up that array's
+ *     device address (cudaGetSymbolAddress) and caches it; make that first call before any
+ *     stream capture.
+ *   - mx*my*mz above VVLIC_NOALLOC_MAX_VOXELS (or an axis below 2) returns
+ *     VVLIC_ERR_INVALID_ARGUMENT without launching anything.
+ *   - Every call shares the array and it keeps the last call's contents; calls that overlap on
+ *     the GPU (different streams or threads) race on it and must be ordered by the caller. */
+vvlic_status vvlic_noise_gradients_device_noalloc(const uint8_t* d_noise, int32_t mx, int32_t my,
+                                                  int32_t mz, int32_t mode, const float* slice_dist,
+                                                  uint8_t* d_rgba, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

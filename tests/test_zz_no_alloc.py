@@ -1,0 +1,71 @@
+"""The no-allocation noise-gradient entry point, called through the C ABI.
+
+vvlic_noise_gradients_device_noalloc serves callers that may not allocate GPU memory while it
+runs (hosts that fix their memory budget at start-up, frame loops that cannot take allocator
+latency or cudaFree's synchronisation).  It keeps its temporary gradients in a fixed array
+inside the library instead.  Its output must equal the allocating entry point's bit for bit —
+the tolerance of every preprocessing test here — on consecutive calls that reuse the shared
+array, and it must refuse sizes above its fixed maximum.
+
+This file is named to be collected last, so a run that stops at the first failure has run
+every other test before it.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from vectorvisualization_gb300 import capi, workloads as wl
+
+pytestmark = pytest.mark.gpu
+
+
+def _run(lib, fn, d_in, dims, mode, d_out, sd):
+    sd_arr = np.asarray(sd, np.float32)
+    mx, my, mz = dims
+    return fn(d_in, mx, my, mz, mode, sd_arr.ctypes.data, d_out, None)
+
+
+def test_noalloc_matches_allocating_entry_on_consecutive_calls(vvlic_lib):
+    import torch
+
+    lib = vvlic_lib
+    # two different volumes back to back: the second call reuses the array holding the first
+    # call's gradients, so a stale value would show up as a mismatch
+    cases = [(wl.dense_noise((48, 40, 36), seed=31), (1.0, 1.0, 1.0)),
+             (wl.sparse_noise((29, 23, 17), seed=32), (1.0, 0.5, 2.0))]
+    for mode in (capi.NOISE_GRAD_SOBEL, capi.NOISE_GRAD_CENTRAL):
+        for noise, sd in cases:
+            dims = noise.shape[::-1]
+            d_in = torch.from_numpy(noise).cuda()
+            want = torch.zeros(noise.shape + (4,), dtype=torch.uint8, device="cuda")
+            got = torch.full(noise.shape + (4,), 7, dtype=torch.uint8, device="cuda")
+            assert _run(lib, lib.vvlic_noise_gradients_device, d_in.data_ptr(), dims, mode, want.data_ptr(), sd) == 0
+            assert _run(lib, lib.vvlic_noise_gradients_device_noalloc, d_in.data_ptr(), dims, mode,
+                        got.data_ptr(), sd) == 0
+            torch.cuda.synchronize()
+            np.testing.assert_array_equal(got.cpu().numpy(), want.cpu().numpy())
+
+
+def test_noalloc_rejects_sizes_above_its_maximum(vvlic_lib):
+    import torch
+
+    lib = vvlic_lib
+    d = torch.zeros(16, dtype=torch.uint8, device="cuda")
+    too_big = 1 << 20  # VVLIC_NOALLOC_MAX_VOXELS
+    st = lib.vvlic_noise_gradients_device_noalloc(d.data_ptr(), too_big, 2, 1, capi.NOISE_GRAD_SOBEL, None,
+                                                  d.data_ptr(), None)
+    assert st == capi.ERR_INVALID_ARGUMENT
+    st = lib.vvlic_noise_gradients_device_noalloc(d.data_ptr(), 1025, 1024, 1, capi.NOISE_GRAD_SOBEL, None,
+                                                  d.data_ptr(), None)
+    assert st == capi.ERR_INVALID_ARGUMENT
+    # the largest accepted size still runs (exactly the maximum number of voxels)
+    big = torch.from_numpy(wl.dense_noise((128, 128, 64), seed=33)).cuda()
+    out_a = torch.zeros((64, 128, 128, 4), dtype=torch.uint8, device="cuda")
+    out_b = torch.ones((64, 128, 128, 4), dtype=torch.uint8, device="cuda")
+    assert lib.vvlic_noise_gradients_device_noalloc(big.data_ptr(), 128, 128, 64, capi.NOISE_GRAD_CENTRAL, None,
+                                                    out_a.data_ptr(), None) == 0
+    assert lib.vvlic_noise_gradients_device(big.data_ptr(), 128, 128, 64, capi.NOISE_GRAD_CENTRAL, None,
+                                            out_b.data_ptr(), None) == 0
+    torch.cuda.synchronize()
+    assert torch.equal(out_a, out_b)

@@ -126,6 +126,7 @@ _SIGS = {
     "vvlic_get_stats": (_I, [_P, C.POINTER(Stats)]),
     "vvlic_composite_background": (_I, [_P, _I, _I, _P]),
     "vvlic_noise_gradients_device": (_I, [_P, _I, _I, _I, _I, _P, _P, _P]),
+    "vvlic_noise_gradients_device_noalloc": (_I, [_P, _I, _I, _I, _I, _P, _P, _P]),
     "vvlic_download_field": (_I, [_P, _I, _P, C.c_uint64]),
     "vvlic_download_noise": (_I, [_P, _P, C.c_uint64]),
 }
