@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     return ap.parse_args()
 
 
@@ -256,6 +257,83 @@ def run_reference(args, dist: Dist):
     return 0
 
 
+def bench_adjoint(ctx, torch, stream, flush, args):
+    """C4: 128^3 vortex field, dense noise, Heun L=30 (61 taps), 512^2 x 4 views, L2 loss to a
+    target rendered from a hidden seeded TF; gradients w.r.t. TF (256x4), opacity (256) and the
+    61 taps.  Times the plain forward, the recording forward and the adjoint per view."""
+    from vectorvisualization_gb300 import capi, workloads as wl
+
+    w = wl.c4()
+    w.storage = args.storage
+    vid = wl.setup_context(ctx, w)
+    L = w.params.steps_forward
+    taps, inv_area = ctx.filter_taps()
+    W, H = w.width, w.height
+    p = w.params
+    p.sampler = capi.SAMPLER[args.sampler]
+    p.schedule = capi.SCHEDULE[args.schedule]
+    sh = stream.cuda_stream
+    img = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+    # the hidden target: the same views rendered with another seeded TF
+    ctx.set_tf(*wl.random_tf(seed=4040))
+    ctx.set_params(p)
+    targets = []
+    for v in w.views:
+        ctx.set_view(v)
+        ctx.render_device(vid, img.data_ptr(), W, H, None, sh)
+        stream.synchronize()
+        targets.append(img.clone())
+    ctx.set_tf(w.tf_rgba, w.tf_opac)
+    d_tf = torch.empty((256, 4), dtype=torch.float32, device="cuda")
+    d_op = torch.empty(256, dtype=torch.float32, device="cuda")
+    d_taps = torch.empty(2 * L + 1, dtype=torch.float32, device="cuda")
+    g = torch.empty_like(img)
+
+    def timed(fn):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
+    fwd_ms, rec_ms, adj_ms, steps = 0.0, 0.0, 0.0, 0
+    for rep in range(2):  # first pass warms up
+        f_ms = r_ms = a_ms = 0.0
+        for v, tgt in zip(w.views, targets):
+            ctx.set_view(v)
+            p.record_tape = 0
+            ctx.set_params(p)
+            f_ms += timed(lambda: ctx.render_device(vid, img.data_ptr(), W, H, None, sh))
+            steps_v = ctx.stats().sample_steps
+            p.record_tape = 1
+            ctx.set_params(p)
+            r_ms += timed(lambda: ctx.render_device(vid, img.data_ptr(), W, H, None, sh))
+            torch.mul(img - tgt, 2.0, out=g)
+
+            def adj():
+                ctx.render_adjoint(vid, g.data_ptr(), W, H, d_tf.data_ptr(), d_op.data_ptr(), d_taps.data_ptr(), sh)
+
+            a_ms += timed(adj)
+            if rep == 1:
+                steps += steps_v
+        fwd_ms, rec_ms, adj_ms = f_ms, r_ms, a_ms
+    p.record_tape = 0
+    ctx.set_params(p)
+    ctx.free_volume(vid)
+    return {
+        "workload": "C4 vortex 128^3 dense-noise Heun L=30 (61 taps) 512^2 x 4 views, L2 to hidden-TF target",
+        "storage": w.storage, "sampler": args.sampler,
+        "fwd_ms": fwd_ms, "fwd_recording_ms": rec_ms, "adjoint_ms": adj_ms,
+        "fwd_plus_adjoint_over_fwd": (rec_ms + adj_ms) / fwd_ms,
+        "gss_fwd": steps / (fwd_ms / 1e3) / 1e9,
+        "gss_fwd_adjoint": steps / ((rec_ms + adj_ms) / 1e3) / 1e9,
+        "grad_norms": {"tf": float(d_tf.norm()), "opacity": float(d_op.norm()), "taps": float(d_taps.norm())},
+    }
+
+
 def run_ours(args, dist: Dist):
     import torch
 
@@ -371,6 +449,10 @@ def run_ours(args, dist: Dist):
             variants[storage] = {"gss": s2.sample_steps / (ms / 1e3) / 1e9, "ms": ms}
             ctx.free_volume(vid2)
         line["storage_variants"] = variants
+
+    # forward + adjoint on the differentiable-fit configuration (unlit; 4 views)
+    if not args.no_adjoint and dist.rank == 0:
+        line["fwd_adjoint"] = bench_adjoint(ctx, torch, stream, flush, args)
 
     # end to end through the C ABI with host buffers
     if not args.no_e2e:

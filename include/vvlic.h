@@ -145,7 +145,8 @@ typedef struct vvlic_params {
   /* kernel selection (no reference counterpart) */
   int32_t sampler;        /* VVLIC_SAMPLER_* (HYBRID) */
   int32_t schedule;       /* VVLIC_SCHEDULE_* (QUEUE) */
-  int32_t reserved[6];
+  int32_t record_tape;    /* renders record what vvlic_render_adjoint needs (0) */
+  int32_t reserved[5];
 } vvlic_params;
 
 /* Work distribution of a render launch:
@@ -285,6 +286,18 @@ vvlic_status vvlic_render(vvlic_ctx* ctx, int32_t vol_id, float* out_rgba, int32
  * the number of LIC samples of each ray. */
 vvlic_status vvlic_render_device(vvlic_ctx* ctx, int32_t vol_id, float* d_out_rgba,
                                  int32_t w, int32_t h, uint32_t* d_samples, void* stream);
+/* Adjoint of the last render (no counterpart in the reference, which has no differentiation):
+ * given the image cotangent dL/d(rgba) in device memory (w*h*4 floats, the same layout as the
+ * image), writes dL/dTF (256*4 RGBA entries), dL/dopacity (256) and dL/dtaps (L_b+L_f+1, the
+ * explicit or table-derived tap weights) to device memory; any output pointer may be NULL.
+ * The last render on this context must have been vvlic_render_device of the same volume and
+ * size with params.record_tape = 1; that render recorded, per ray sample, the LIC intensity and
+ * TF coordinate and, every 32 samples, a compositing checkpoint.  Unlit shading only
+ * (VVLIC_ILLUM_NONE).  Results are deterministic (fixed-point accumulation); they are NaN if
+ * the tape was too short for a ray.  Asynchronous on `stream`. */
+vvlic_status vvlic_render_adjoint(vvlic_ctx* ctx, int32_t vol_id, const float* d_dl_drgba, int32_t w, int32_t h,
+                                  float* d_dl_dtf, float* d_dl_dopacity, float* d_dl_dtaps, void* stream);
+
 /* Statistics of the last render (samples are counted on the device every render). */
 vvlic_status vvlic_get_stats(vvlic_ctx* ctx, vvlic_stats* stats);
 

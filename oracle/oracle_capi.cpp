@@ -122,6 +122,43 @@ int32_t vvo_render(const vvo_inputs* vi, const vvlic_params* p, const double* ra
   return 0;
 }
 
+/* FP64 adjoint of the unlit render: accumulates dL/dTF (256*4), dL/dopacity (256) and
+ * dL/dtaps (L_b+L_f+1) for the image cotangent g_img (h*w*4). */
+int32_t vvo_adjoint(const vvo_inputs* vi, const vvlic_params* p, const double* ray_coeffs, int32_t w, int32_t h,
+                    const float* g_img, double* d_tf, double* d_opac, double* d_taps, int32_t threads) {
+  if (p->illum != VVLIC_ILLUM_NONE) return -2;
+  int lb, lf;
+  int ntaps = effective_steps(p, &lb, &lf);
+  std::vector<double> taps(ntaps);
+  double inv_area;
+  if (vi->taps) {
+    for (int i = 0; i < ntaps; ++i) taps[i] = vi->taps[i];
+    inv_area = vi->inv_filter_area;
+  } else {
+    if (!vi->filter_table) return -1;
+    vvo::filter_taps<double>(vi->filter_table, vi->filter_width, vi->filter_clamp, lb, lf, taps.data());
+    inv_area = vvo::filter_inv_area(vi->filter_table, vi->filter_width, vi->filter_is_box != 0);
+  }
+  vvo::Inputs in;
+  in.field = vi->field;
+  for (int i = 0; i < 3; ++i) {
+    in.n[i] = vi->n[i];
+    in.slice_dist[i] = vi->slice_dist[i];
+    in.m[i] = vi->m[i];
+    in.sn[i] = vi->sn[i];
+  }
+  in.noise = vi->noise;
+  in.noise_channels = vi->noise_channels;
+  in.scalar = vi->scalar;
+  in.tf_rgba = vi->tf_rgba;
+  in.tf_opac = vi->tf_opac;
+  in.taps = taps.data();
+  in.inv_filter_area = inv_area;
+  vvo::AdjointOut out{d_tf, d_opac, d_taps};
+  vvo::adjoint<double>(in, *p, ray_coeffs, w, h, g_img, out, threads);
+  return 0;
+}
+
 int32_t vvo_max_threads(void) {
 #if defined(_OPENMP)
   return omp_get_max_threads();

@@ -68,6 +68,8 @@ def lib() -> C.CDLL:
         l.vvo_render.argtypes = [C.POINTER(Inputs), P, P, I, I, P, I, P, P, I, I]
         l.vvo_render.restype = I
         l.vvo_max_threads.restype = I
+        l.vvo_adjoint.argtypes = [C.POINTER(Inputs), P, P, I, I, P, P, P, P, I]
+        l.vvo_adjoint.restype = I
         _lib = l
     return _lib
 
@@ -196,6 +198,22 @@ class Scene:
         if st != 0:
             raise RuntimeError(f"oracle render failed ({st})")
         return img, smp
+
+
+def adjoint(scene: "Scene", params: capi.Params, view: capi.View, w: int, h: int, g_img: np.ndarray,
+            threads: int = 0):
+    """FP64 adjoint of the unlit render: (dL/dTF (256,4), dL/dopacity (256,), dL/dtaps)."""
+    rc = view_rays(view, scene.dims, w, h, list(scene.inputs.slice_dist))
+    g = np.ascontiguousarray(g_img, dtype=np.float32).reshape(h, w, 4)
+    lb, lf = (15, 15) if params.low_res else (params.steps_backward, params.steps_forward)
+    d_tf = np.zeros(1024, np.float64)
+    d_op = np.zeros(256, np.float64)
+    d_taps = np.zeros(lb + lf + 1, np.float64)
+    st = lib().vvo_adjoint(C.byref(scene.inputs), C.byref(params), rc.ctypes.data, w, h, g.ctypes.data,
+                           d_tf.ctypes.data, d_op.ctypes.data, d_taps.ctypes.data, threads)
+    if st != 0:
+        raise RuntimeError(f"oracle adjoint failed ({st})")
+    return d_tf.reshape(256, 4), d_op, d_taps
 
 
 def max_threads() -> int:

@@ -743,6 +743,207 @@ template <class R> static inline uint32_t render_pixel(const Inputs& in, const v
   return samples;
 }
 
+/* ------------------------------------------------------------------------------------- */
+/* adjoint: reverse mode through the unlit ray (illumLIC + blend) with respect to the TF    */
+/* RGBA table, the opacity table and the filter taps.  Conventions shared with the kernel: */
+/* d clamp(u)/du = 1 on [0, 1] and 0 outside; the alpha-correction derivative is 0 where   */
+/* its base 1 - a is <= 0; a 1D lookup's derivative in its coordinate is 0 where the       */
+/* coordinate is clamped; the termination test is not differentiated.                     */
+/* ------------------------------------------------------------------------------------- */
+template <class R> struct Lookup {  /* LINEAR + CLAMP_TO_EDGE 1D lookup decomposition */
+  int i0, i1;
+  R t;           /* weight of i1 */
+  R dvds_scale;  /* d(coordinate u)/ds where u is inside the interpolation range, else 0 */
+};
+template <class R> static inline Lookup<R> lookup1d(R s) {
+  const int N = VVLIC_TF_ENTRIES;
+  Lookup<R> L;
+  R u = s * R(N) - R(0.5);
+  bool inside = u > R(0) && u < R(N - 1);
+  if (!(u > R(-1))) u = R(-1);
+  if (u > R(N)) u = R(N);
+  R fl = std::floor(u);
+  L.t = u - fl;
+  int b = (int)fl;
+  L.i0 = std::min(std::max(b, 0), N - 1);
+  L.i1 = std::min(std::max(b + 1, 0), N - 1);
+  L.dvds_scale = inside ? R(N) : R(0);
+  return L;
+}
+
+struct AdjointOut {
+  double* tf;    /* 256*4 */
+  double* opac;  /* 256 */
+  double* taps;  /* L_b + L_f + 1 */
+};
+
+/* noise values n_j of every tap of the LIC at `pos` (order: index j + L_b) */
+template <class R> static inline void lic_noise_taps(const LicCtx<R>& c, V3<R> pos, V4<R> f0, std::vector<R>& n) {
+  const int lb = c.u->lb, lf = c.u->lf;
+  n.assign(lb + lf + 1, R(0));
+  n[lb] = noise_tap<R>(c, pos).w;
+  for (int half = 0; half < 2; ++half) {
+    R dirs = half == 0 ? R(-1) : R(1);
+    int L = half == 0 ? lb : lf;
+    V3<R> p = pos;
+    V4<R> step = f0;
+    for (int i = 1; i <= L; ++i) {
+      p = lic_step<R>(c, p, step, dirs);
+      n[half == 0 ? lb - i : lb + i] = noise_tap<R>(c, p).w;
+    }
+  }
+}
+
+/* One pixel: forward (storing every sample), then the reverse pass with cotangent g_out. */
+template <class R> static inline void adjoint_pixel(const Inputs& in, const vvlic_params& p, const Uniforms<R>& u,
+                                                    const double* rc, int px, int py, const float g_out[4],
+                                                    AdjointOut& out) {
+  R o[3], d[3];
+  R uu = R(px) + R(0.5), vv = R(py) + R(0.5);
+  for (int i = 0; i < 3; ++i) {
+    o[i] = R(rc[0 + i]) + uu * R(rc[3 + i]) + vv * R(rc[6 + i]);
+    d[i] = R(rc[9 + i]) + uu * R(rc[12 + i]) + vv * R(rc[15 + i]);
+  }
+  R te;
+  if (!ray_entry<R>(o, d, u.extent, rc[18] != 0.0, &te)) return;
+  V3<R> sv{u.scale_vol[0], u.scale_vol[1], u.scale_vol[2]};
+  V3<R> pos = mul(V3<R>{o[0] + te * d[0], o[1] + te * d[1], o[2] + te * d[2]}, sv);
+  V3<R> dir = mul(normalize(V3<R>{d[0], d[1], d[2]}), sv);
+  LicCtx<R> c{&in, &p, &u, false};
+  struct Sample {
+    V3<R> pos;
+    V4<R> f;
+    R I, idx;
+  };
+  std::vector<Sample> smp;
+  V4<R> src{R(0), R(0), R(0), R(0)};
+  bool outside = false;
+  const R thr = R(p.alpha_threshold);
+  for (int j = 0; !outside && j < u.num_iterations; ++j) {
+    for (int i = 0; i < u.num_iterations; ++i) {
+      V4<R> f = tex3d_field<R>(in, pos);
+      R idx = p.tf_index == VVLIC_TF_INDEX_MAGNITUDE ? f.w : f.z;
+      V4<R> il = compute_lic<R>(c, pos, f);
+      R I = il.w * u.intensity_scale;
+      smp.push_back(Sample{pos, f, I, idx});
+      /* shade to evaluate the termination test */
+      Lookup<R> lt = lookup1d<R>(idx), lo = lookup1d<R>(I * R(1.3));
+      R tfa = (R(1) - lt.t) * R(in.tf_rgba[4 * lt.i0 + 3]) + lt.t * R(in.tf_rgba[4 * lt.i1 + 3]);
+      R op = (R(1) - lo.t) * R(in.tf_opac[lo.i0]) + lo.t * R(in.tf_opac[lo.i1]);
+      src.w = alpha_correct<R>(op * tfa, u.alpha_correction);
+      pos = pos + dir * u.step_size;
+      outside = pos.x < R(0) || pos.y < R(0) || pos.z < R(0) || pos.x > u.tex_max[0] || pos.y > u.tex_max[1] ||
+                pos.z > u.tex_max[2] || src.w > thr;
+      if (outside) break;
+    }
+  }
+  const size_t S = smp.size();
+  /* forward compositing states D[k] = dest before sample k */
+  std::vector<V4<R>> D(S + 1);
+  D[0] = V4<R>{R(0), R(0), R(0), R(0)};
+  struct Sh {
+    Lookup<R> lt, lo;
+    V4<R> tf;
+    R op, a0, base, alpha;
+    V3<R> col;
+  };
+  std::vector<Sh> sh(S);
+  for (size_t k = 0; k < S; ++k) {
+    Sh& h = sh[k];
+    h.lt = lookup1d<R>(smp[k].idx);
+    for (int ch = 0; ch < 4; ++ch)
+      (&h.tf.x)[ch] = (R(1) - h.lt.t) * R(in.tf_rgba[4 * h.lt.i0 + ch]) + h.lt.t * R(in.tf_rgba[4 * h.lt.i1 + ch]);
+    h.lo = lookup1d<R>(smp[k].I * R(1.3));
+    h.op = (R(1) - h.lo.t) * R(in.tf_opac[h.lo.i0]) + h.lo.t * R(in.tf_opac[h.lo.i1]);
+    h.a0 = h.op * h.tf.w;
+    h.base = R(1) - h.a0;
+    h.alpha = R(1) - std::pow(h.base > R(0) ? h.base : R(0), u.alpha_correction);
+    h.col = V3<R>{smp[k].I * h.tf.x * u.illum_scale, smp[k].I * h.tf.y * u.illum_scale,
+                  smp[k].I * h.tf.z * u.illum_scale};
+    V4<R> s{h.col.x * h.alpha, h.col.y * h.alpha, h.col.z * h.alpha, h.alpha};
+    R om = R(1) - D[k].w;
+    D[k + 1] = V4<R>{clamp01(om * s.x + D[k].x), clamp01(om * s.y + D[k].y), clamp01(om * s.z + D[k].z),
+                     clamp01(om * s.w + D[k].w)};
+  }
+  /* reverse */
+  V4<R> g{R(g_out[0]), R(g_out[1]), R(g_out[2]), R(g_out[3])};
+  std::vector<R> n;
+  for (size_t kk = S; kk-- > 0;) {
+    const Sh& h = sh[kk];
+    const V4<R>& Dp = D[kk];
+    V4<R> s{h.col.x * h.alpha, h.col.y * h.alpha, h.col.z * h.alpha, h.alpha};
+    R om = R(1) - Dp.w;
+    R uarr[4] = {om * s.x + Dp.x, om * s.y + Dp.y, om * s.z + Dp.z, om * s.w + Dp.w};
+    R gu[4];
+    for (int ch = 0; ch < 4; ++ch) gu[ch] = (uarr[ch] >= R(0) && uarr[ch] <= R(1)) ? (&g.x)[ch] : R(0);
+    R ds[4];
+    for (int ch = 0; ch < 4; ++ch) ds[ch] = om * gu[ch];
+    V4<R> gp{gu[0], gu[1], gu[2], gu[3]};
+    gp.w -= gu[0] * s.x + gu[1] * s.y + gu[2] * s.z + gu[3] * s.w;
+    /* s = (col*alpha, alpha) */
+    R dcol[3] = {ds[0] * h.alpha, ds[1] * h.alpha, ds[2] * h.alpha};
+    R dalpha = ds[0] * h.col.x + ds[1] * h.col.y + ds[2] * h.col.z + ds[3];
+    R dbase_da0 = h.base > R(0) ? u.alpha_correction * std::pow(h.base, u.alpha_correction - R(1)) : R(0);
+    R da0 = dalpha * dbase_da0;
+    /* a0 = op(1.3 I) * tf.a */
+    R dop = da0 * h.tf.w;
+    R dtfa = da0 * h.op;
+    out.opac[h.lo.i0] += double(dop * (R(1) - h.lo.t));
+    out.opac[h.lo.i1] += double(dop * h.lo.t);
+    R dI = dop * (R(in.tf_opac[h.lo.i1]) - R(in.tf_opac[h.lo.i0])) * h.lo.dvds_scale * R(1.3);
+    /* col = I * tf.rgb * illumScale */
+    R dtf[4] = {dcol[0] * smp[kk].I * u.illum_scale, dcol[1] * smp[kk].I * u.illum_scale,
+                dcol[2] * smp[kk].I * u.illum_scale, dtfa};
+    dI += (dcol[0] * h.tf.x + dcol[1] * h.tf.y + dcol[2] * h.tf.z) * u.illum_scale;
+    for (int ch = 0; ch < 4; ++ch) {
+      out.tf[4 * h.lt.i0 + ch] += double(dtf[ch] * (R(1) - h.lt.t));
+      out.tf[4 * h.lt.i1 + ch] += double(dtf[ch] * h.lt.t);
+    }
+    /* I = intensity_scale * sum_j w_j n_j */
+    R dIraw = dI * u.intensity_scale;
+    if (dIraw != R(0)) {
+      lic_noise_taps<R>(c, smp[kk].pos, smp[kk].f, n);
+      for (size_t j = 0; j < n.size(); ++j) out.taps[j] += double(dIraw * n[j]);
+    }
+    g = gp;
+  }
+}
+
+template <class R> static inline void adjoint(const Inputs& in, const vvlic_params& p, const double* rc, int W,
+                                              int H, const float* g_img, AdjointOut& out, int threads) {
+  Uniforms<R> u = uniforms<R>(in, p);
+  const int ntaps = u.lb + u.lf + 1;
+  int nt = 1;
+#if defined(_OPENMP)
+  if (threads > 0) omp_set_num_threads(threads);
+  nt = omp_get_max_threads();
+#endif
+  std::vector<double> acc((size_t)nt * (1024 + 256 + ntaps), 0.0);
+#if defined(_OPENMP)
+#pragma omp parallel
+#endif
+  {
+    int tid = 0;
+#if defined(_OPENMP)
+    tid = omp_get_thread_num();
+#endif
+    double* base = acc.data() + (size_t)tid * (1024 + 256 + ntaps);
+    AdjointOut mine{base, base + 1024, base + 1280};
+#if defined(_OPENMP)
+#pragma omp for schedule(dynamic, 1)
+#endif
+    for (int py = 0; py < H; ++py)
+      for (int px = 0; px < W; ++px)
+        adjoint_pixel<R>(in, p, u, rc, px, py, g_img + 4 * ((size_t)py * W + px), mine);
+  }
+  for (int t = 0; t < nt; ++t) {
+    const double* b = acc.data() + (size_t)t * (1024 + 256 + ntaps);
+    for (int i = 0; i < 1024; ++i) out.tf[i] += b[i];
+    for (int i = 0; i < 256; ++i) out.opac[i] += b[1024 + i];
+    for (int i = 0; i < ntaps; ++i) out.taps[i] += b[1280 + i];
+  }
+}
+
 /* Render the rows listed in `rows` (all rows when rows == NULL) into out (nrows x W x 4). */
 template <class R> static inline void render(const Inputs& in, const vvlic_params& p, const double* rc, int W, int H,
                                              const int32_t* rows, int nrows, float* out, uint32_t* samples,

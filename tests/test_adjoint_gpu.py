@@ -1,0 +1,158 @@
+"""GPU adjoint (vvlic_render_adjoint) against the FP64 oracle adjoint and against central finite
+differences of the GPU forward, plus determinism and a small transfer-function fit through the
+torch.autograd.Function wrapper.
+
+Tolerances: the FP32 kernel's gradients match the FP64 adjoint to 2e-3 of the largest gradient
+magnitude (relative, every entry); finite differences (h = 1e-3, FP32 forward) match to 5% on
+the most sensitive entries; repeated adjoints are bitwise identical.
+"""
+import numpy as np
+import pytest
+
+from vectorvisualization_gb300 import capi, workloads as wl
+
+pytestmark = pytest.mark.gpu
+
+
+def case(size=24, image=32, L=6, sampler="cell", storage="f32"):
+    w = wl.c4(size=size, image=image, views=1)
+    w.params.steps_forward = w.params.steps_backward = L
+    w.params.step_size_vol = 1.0 / 48.0
+    w.params.gradient_scale = 8.0
+    w.params.sampler = capi.SAMPLER[sampler]
+    w.storage = storage
+    taps = np.linspace(0.5, 1.0, 2 * L + 1).astype(np.float64)
+    return w, taps
+
+
+def gpu_forward_adjoint(ctx, w, taps, target, inv_area=0.7):
+    import torch
+
+    vid = wl.setup_context(ctx, w)
+    ctx.set_filter_taps(taps.astype(np.float32), w.params.steps_backward, w.params.steps_forward, inv_area)
+    p = w.params
+    p.record_tape = 1
+    ctx.set_params(p)
+    img = torch.empty((w.height, w.width, 4), dtype=torch.float32, device="cuda")
+    ctx.render_device(vid, img.data_ptr(), w.width, w.height)
+    torch.cuda.synchronize()
+    g = 2.0 * (img - torch.from_numpy(target).cuda())
+    d_tf = torch.empty((256, 4), dtype=torch.float32, device="cuda")
+    d_op = torch.empty(256, dtype=torch.float32, device="cuda")
+    d_taps = torch.empty(taps.size, dtype=torch.float32, device="cuda")
+    ctx.render_adjoint(vid, g.contiguous().data_ptr(), w.width, w.height, d_tf.data_ptr(), d_op.data_ptr(),
+                       d_taps.data_ptr())
+    torch.cuda.synchronize()
+    return vid, img.cpu().numpy(), d_tf.cpu().numpy(), d_op.cpu().numpy(), d_taps.cpu().numpy()
+
+
+def target_image(oracle, w, taps, storage="f32"):
+    enc = oracle.encode_field(w.field)
+    if storage != "f32":
+        enc = oracle.round_storage(enc, storage)
+    rgba_t, op_t = wl.random_tf(seed=909)
+    sc = oracle.Scene(enc, w.noise, rgba_t, op_t, taps=taps[::-1].copy(), inv_filter_area=0.7)
+    return sc.render(w.params, w.views[0], w.width, w.height)[0]
+
+
+@pytest.mark.parametrize("sampler,storage", [("cell", "f32"), ("hybrid", "f16"), ("gather", "f32")])
+def test_adjoint_matches_fp64_oracle(ctx, oracle, sampler, storage):
+    w, taps = case(sampler=sampler, storage=storage)
+    target = target_image(oracle, w, taps, storage)
+    vid, img, d_tf, d_op, d_taps = gpu_forward_adjoint(ctx, w, taps, target)
+    enc = oracle.encode_field(w.field)
+    if storage != "f32":
+        enc = oracle.round_storage(enc, storage)
+    sc = oracle.Scene(enc, w.noise, w.tf_rgba, w.tf_opac, taps=taps, inv_filter_area=0.7)
+    ref_img, _ = sc.render(w.params, w.views[0], w.width, w.height)
+    assert float(np.sqrt(np.mean((img - ref_img) ** 2))) < 1e-4
+    # the oracle adjoint with the GPU's own cotangent
+    g = (2.0 * (img.astype(np.float64) - target)).astype(np.float32)
+    r_tf, r_op, r_taps = oracle.adjoint(sc, w.params, w.views[0], w.width, w.height, g)
+    for got, ref in ((d_tf, r_tf), (d_op, r_op), (d_taps, r_taps)):
+        scale = max(float(np.abs(ref).max()), 1e-6)
+        err = float(np.abs(got - ref).max())
+        assert err <= 2e-3 * scale, (err, scale)
+    assert float(np.abs(r_taps).max()) > 0 and float(np.abs(r_tf).max()) > 0
+
+
+def test_adjoint_is_deterministic(ctx, oracle):
+    w, taps = case(sampler="hybrid", storage="f16")
+    target = target_image(oracle, w, taps, "f16")
+    a = gpu_forward_adjoint(ctx, w, taps, target)
+    b = gpu_forward_adjoint(ctx, w, taps, target)
+    for x, y in zip(a[2:], b[2:]):
+        np.testing.assert_array_equal(x, y)
+
+
+def test_adjoint_matches_gpu_finite_differences(ctx, oracle):
+    import torch
+
+    w, taps = case(size=32, image=40, L=8)
+    target = target_image(oracle, w, taps)
+    vid, img, d_tf, d_op, d_taps = gpu_forward_adjoint(ctx, w, taps, target)
+    p = w.params
+    p.record_tape = 0
+    ctx.set_params(p)
+    tgt = torch.from_numpy(target).cuda()
+
+    def loss(rgba, op, tp):
+        ctx.set_tf(rgba, op)
+        ctx.set_filter_taps(tp.astype(np.float32), p.steps_backward, p.steps_forward, 0.7)
+        out = torch.empty((w.height, w.width, 4), dtype=torch.float32, device="cuda")
+        ctx.render_device(vid, out.data_ptr(), w.width, w.height)
+        torch.cuda.synchronize()
+        return float(torch.sum((out.double() - tgt.double()) ** 2))
+
+    h = 1e-3
+    for idx in np.argsort(-np.abs(d_tf.reshape(-1)))[:4]:
+        e, ch = divmod(int(idx), 4)
+        r1, r2 = w.tf_rgba.copy(), w.tf_rgba.copy()
+        r1[e, ch] += h
+        r2[e, ch] -= h
+        fd = (loss(r1, w.tf_opac, taps) - loss(r2, w.tf_opac, taps)) / (2 * h)
+        assert abs(fd - d_tf[e, ch]) <= 0.05 * abs(fd) + 1e-3, (e, ch, fd, d_tf[e, ch])
+    for j in np.argsort(-np.abs(d_taps))[:4]:
+        t1, t2 = taps.copy(), taps.copy()
+        t1[j] += h
+        t2[j] -= h
+        fd = (loss(w.tf_rgba, w.tf_opac, t1) - loss(w.tf_rgba, w.tf_opac, t2)) / (2 * h)
+        assert abs(fd - d_taps[j]) <= 0.05 * abs(fd) + 1e-3, (j, fd, d_taps[j])
+
+
+def test_adjoint_requires_a_recorded_tape(ctx):
+    import torch
+
+    w, taps = case()
+    vid = wl.setup_context(ctx, w)
+    g = torch.zeros((w.height, w.width, 4), dtype=torch.float32, device="cuda")
+    with pytest.raises(capi.VVLICError) as e:
+        ctx.render_adjoint(vid, g.data_ptr(), w.width, w.height, None, None, None)
+    assert e.value.status == capi.ERR_NOT_READY
+
+
+def test_tf_fit_reduces_loss(ctx, oracle):
+    """A few Adam steps on the TF table through the autograd wrapper lower the L2 loss."""
+    import torch
+
+    from lic_autograd import render
+
+    w, taps = case(size=24, image=32, L=6, sampler="hybrid", storage="f16")
+    target = torch.from_numpy(target_image(oracle, w, taps, "f16")).cuda()
+    vid = wl.setup_context(ctx, w)
+    tf = torch.tensor(w.tf_rgba, device="cuda", requires_grad=True)
+    op = torch.tensor(w.tf_opac, device="cuda", requires_grad=True)
+    tp = torch.tensor(taps[::-1].copy(), dtype=torch.float32, device="cuda", requires_grad=False)
+    opt = torch.optim.Adam([tf, op], lr=0.02)
+    losses = []
+    for _ in range(15):
+        opt.zero_grad()
+        img = render(tf, op, tp, ctx, vid, w.params, w.width, w.height, 0.7)
+        loss = torch.sum((img - target) ** 2)
+        loss.backward()
+        opt.step()
+        with torch.no_grad():
+            tf.clamp_(0.0, 1.0)
+            op.clamp_(0.0, 1.0)
+        losses.append(float(loss))
+    assert losses[-1] < 0.5 * losses[0], losses

@@ -220,3 +220,66 @@ def test_row_subset_matches_full(oracle):
     rows = [0, 7, 19]
     sub, _ = sc.render(w.params, w.views[0], 20, 20, rows=rows)
     np.testing.assert_array_equal(sub, full[rows])
+
+
+# ---------------------------------------------------------------------------------------------
+# the FP64 adjoint against central finite differences of the FP64 forward
+# ---------------------------------------------------------------------------------------------
+def _adjoint_case(oracle):
+    w = wl.c1(size=12, image=14)
+    w.field = wl.vortex_field((12, 12, 12), seed=6)
+    w.noise = wl.dense_noise(12, seed=61)
+    w.params.integrator = capi.HEUN
+    w.params.steps_forward = w.params.steps_backward = 4
+    w.params.gradient_scale = 6.0
+    w.params.step_size_vol = 1.0 / 24.0
+    rgba, op = wl.random_tf(seed=7)
+    taps = np.linspace(0.6, 1.0, 9)
+    view = wl.perspective_view(wl.quat_axis_angle((1, 1, 0), 25.0), distance=2.2)
+    enc = oracle.encode_field(w.field)
+
+    def render(rgba_, op_, taps_):
+        sc = oracle.Scene(enc, w.noise, rgba_, op_, taps=taps_, inv_filter_area=0.8)
+        return sc.render(w.params, view, w.width, w.height)[0].astype(np.float64), sc
+
+    target, _ = render(*wl.random_tf(seed=8), taps[::-1].copy())
+    return w, view, enc, rgba, op, taps, target, render
+
+
+def test_oracle_adjoint_matches_finite_differences(oracle):
+    w, view, enc, rgba, op, taps, target, render = _adjoint_case(oracle)
+    img, sc = render(rgba, op, taps)
+    g = (2.0 * (img - target)).astype(np.float32)
+    d_tf, d_op, d_taps = oracle.adjoint(sc, w.params, view, w.width, w.height, g)
+
+    def loss(rgba_, op_, taps_):
+        im, _ = render(rgba_, op_, taps_)
+        return float(np.sum((im - target) ** 2))
+
+    h = 1e-4
+    checked = 0
+    # the most sensitive entries of each parameter group
+    for idx in np.argsort(-np.abs(d_tf.reshape(-1)))[:6]:
+        e, ch = divmod(int(idx), 4)
+        p1, p2 = rgba.copy(), rgba.copy()
+        p1[e, ch] += h
+        p2[e, ch] -= h
+        fd = (loss(p1, op, taps) - loss(p2, op, taps)) / (2 * h)
+        assert abs(fd - d_tf[e, ch]) <= 2e-3 * max(1.0, abs(fd)), (e, ch, fd, d_tf[e, ch])
+        checked += 1
+    for e in np.argsort(-np.abs(d_op))[:4]:
+        p1, p2 = op.copy(), op.copy()
+        p1[e] += h
+        p2[e] -= h
+        fd = (loss(rgba, p1, taps) - loss(rgba, p2, taps)) / (2 * h)
+        assert abs(fd - d_op[e]) <= 2e-3 * max(1.0, abs(fd)), (e, fd, d_op[e])
+        checked += 1
+    for j in range(taps.size):
+        t1, t2 = taps.copy(), taps.copy()
+        t1[j] += h
+        t2[j] -= h
+        fd = (loss(rgba, op, t1) - loss(rgba, op, t2)) / (2 * h)
+        assert abs(fd - d_taps[j]) <= 2e-3 * max(1.0, abs(fd)), (j, fd, d_taps[j])
+        checked += 1
+    assert checked == 6 + 4 + taps.size
+    assert np.abs(d_tf).max() > 0 and np.abs(d_taps).max() > 0

@@ -66,7 +66,8 @@ class Params(C.Structure):
         ("light_ambient", _f3),
         ("sampler", C.c_int32),
         ("schedule", C.c_int32),
-        ("reserved", C.c_int32 * 6),
+        ("record_tape", C.c_int32),
+        ("reserved", C.c_int32 * 5),
     ]
 
 
@@ -124,6 +125,7 @@ _SIGS = {
     "vvlic_render": (_I, [_P, _I, _P, _I, _I]),
     "vvlic_render_device": (_I, [_P, _I, _P, _I, _I, _P, _P]),
     "vvlic_get_stats": (_I, [_P, C.POINTER(Stats)]),
+    "vvlic_render_adjoint": (_I, [_P, _I, _P, _I, _I, _P, _P, _P, _P]),
     "vvlic_composite_background": (_I, [_P, _I, _I, _P]),
     "vvlic_noise_gradients_device": (_I, [_P, _I, _I, _I, _I, _P, _P, _P]),
     "vvlic_noise_gradients_device_noalloc": (_I, [_P, _I, _I, _I, _I, _P, _P, _P]),
@@ -342,6 +344,12 @@ class Context:
 
     def render_device(self, vid: int, d_out: int, w: int, h: int, d_samples: int | None = None, stream: int = 0):
         self._check(self._lib.vvlic_render_device(self.h, vid, d_out, w, h, d_samples, stream or None), "render_device")
+
+    def render_adjoint(self, vid: int, d_grad_img: int, w: int, h: int, d_tf: int | None, d_opac: int | None,
+                       d_taps: int | None, stream: int = 0):
+        """Gradients of the last recording render (params.record_tape = 1) into device buffers."""
+        self._check(self._lib.vvlic_render_adjoint(self.h, vid, d_grad_img, w, h, d_tf, d_opac, d_taps, stream or None),
+                    "render_adjoint")
 
     def stats(self) -> Stats:
         s = Stats()

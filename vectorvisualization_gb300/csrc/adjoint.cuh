@@ -1,0 +1,253 @@
+// Adjoint of the unlit LIC ray-cast (illumLIC + front-to-back blend) with respect to the
+// transfer-function table (256 RGBA), the opacity table (256) and the filter taps.
+//
+// The forward render records a tape: per sample (intensity I, TF coordinate) and every
+// kSegment samples a checkpoint (position, dest before the sample).  Per ray this kernel walks
+// the segments last to first: it recomputes the segment's compositing states from its
+// checkpoint into a local array (cheap: no streamline work), then backpropagates sample by
+// sample through clamp, blend, alpha correction, the opacity lookup and the TF lookup.  The
+// intensity's cotangent is pushed onto the filter taps by walking the sample's streamlines once
+// more (dL/dw_j = S * sum_k dL/dI_k * n_kj).
+//
+// Reductions are deterministic: per-tap sums are formed by a fixed-order warp butterfly, and
+// every contribution enters 64-bit fixed-point accumulators (scale 2^30) by integer atomics,
+// which are associative — so the result does not depend on scheduling.
+#pragma once
+
+#include "render_fwd.cuh"
+
+namespace vvlic {
+
+constexpr float kFixedScale = 1073741824.0f;  // 2^30
+constexpr int kAccTF = 0, kAccOpac = 4 * VVLIC_TF_ENTRIES, kAccTaps = 5 * VVLIC_TF_ENTRIES;
+constexpr int kAccSize = kAccTaps + kMaxTaps;
+
+__device__ __forceinline__ void fixed_add(long long* slot, float v) {
+  if (v != 0.0f) atomicAdd(reinterpret_cast<unsigned long long*>(slot), (unsigned long long)__float2ll_rn(v * kFixedScale));
+}
+
+// Sum over the warp (fixed butterfly order); lane 0 adds it to the block accumulator.
+__device__ __forceinline__ void warp_fixed_add(long long* slot, float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) fixed_add(slot, v);
+}
+
+// 1D LINEAR + CLAMP_TO_EDGE lookup decomposed: entries i0, i1, weight t of i1, and whether the
+// coordinate lies strictly inside the interpolation range (derivative in s = 256 there, else 0).
+struct Lut {
+  int i0, i1;
+  float t;
+  bool inside;
+};
+__device__ __forceinline__ Lut lut(float s) {
+  Lut L;
+  float u = fmaf(s, (float)VVLIC_TF_ENTRIES, -0.5f);
+  L.inside = u >= 0.0f && u < (float)(VVLIC_TF_ENTRIES - 1);
+  u = fminf(fmaxf(u, -1.0f), (float)VVLIC_TF_ENTRIES);
+  const float fl = floorf(u);
+  L.t = u - fl;
+  const int b = (int)fl;
+  L.i0 = min(max(b, 0), VVLIC_TF_ENTRIES - 1);
+  L.i1 = min(max(b + 1, 0), VVLIC_TF_ENTRIES - 1);
+  return L;
+}
+
+// Unlit source of one sample from its tape record (illumLIC, inc_illum.glsl:257-271).
+struct Src {
+  Lut lt, lo;
+  float4 tf;
+  float op, base, alpha;
+  float3 col;
+};
+__device__ __forceinline__ Src unlit_source(const RenderArgs& a, const float* s_tf, float I, float tfc) {
+  Src r;
+  r.lt = lut(tfc);
+  const float4 t0 = reinterpret_cast<const float4*>(s_tf)[r.lt.i0], t1 = reinterpret_cast<const float4*>(s_tf)[r.lt.i1];
+  r.tf = lerp4(t0, t1, r.lt.t);
+  r.lo = lut(I * 1.3f);
+  const float* op = s_tf + 4 * VVLIC_TF_ENTRIES;
+  r.op = lerpf(op[r.lo.i0], op[r.lo.i1], r.lo.t);
+  const float a0 = r.op * r.tf.w;
+  r.base = 1.0f - a0;
+  r.alpha = 1.0f - powf(fmaxf(r.base, 0.0f), a.alpha_corr);
+  r.col = f3(I * r.tf.x * a.illum_scale, I * r.tf.y * a.illum_scale, I * r.tf.z * a.illum_scale);
+  return r;
+}
+__device__ __forceinline__ float4 premultiplied(const Src& s) {
+  return make_float4(s.col.x * s.alpha, s.col.y * s.alpha, s.col.z * s.alpha, s.alpha);
+}
+// The source as blend() takes it (colour not yet multiplied by alpha), matching shade().
+__device__ __forceinline__ float4 unlit_source_rgba(const RenderArgs& a, const float* s_tf, float I, float tfc) {
+  const Src s = unlit_source(a, s_tf, I, tfc);
+  return make_float4(s.col.x, s.col.y, s.col.z, s.alpha);
+}
+
+// Walk the streamlines of the LIC at `pos` once more and add gI * n_j to the tap accumulators.
+// Every lane of the warp takes part in each reduction; lanes with gI == 0 skip the fetches.
+template <int ST, int FL, int NL, int INTEG>
+__device__ __forceinline__ void tap_gradients(const RenderArgs& a, float3 pos, float gI, long long* s_taps) {
+  const bool act = gI != 0.0f;
+  const int lb = a.lb, lf = a.lf, L = max(lb, lf);
+  float4 f0 = make_float4(0.f, 0.f, 0.f, 0.f);
+  float n0 = 0.0f;
+  if (act) {
+    f0 = Field<ST, FL>::sample(a, pos);
+    n0 = noise_tap<NL, false>(a, pos).w;
+  }
+  warp_fixed_add(s_taps + lb, gI * n0);
+  float3 pb = pos, pf = pos;
+  float4 sb = f0, sf = f0;
+  for (int i = 1; i <= L; ++i) {
+    float vb = 0.0f, vf = 0.0f;
+    if (act) {
+      if (i <= lb) {
+        pb = lic_step<ST, FL, INTEG>(a, pb, sb, -1.0f);
+        vb = gI * noise_tap<NL, false>(a, pb).w;
+      }
+      if (i <= lf) {
+        pf = lic_step<ST, FL, INTEG>(a, pf, sf, 1.0f);
+        vf = gI * noise_tap<NL, false>(a, pf).w;
+      }
+    }
+    if (i <= lb) warp_fixed_add(s_taps + lb - i, vb);
+    if (i <= lf) warp_fixed_add(s_taps + lb + i, vf);
+  }
+}
+
+template <int ST, int FL, int NL, int INTEG>
+__global__ void __launch_bounds__(kThreads) adjoint_kernel(const __grid_constant__ RenderArgs a,
+                                                           const float4* __restrict__ g_img, long long* acc,
+                                                           const uint32_t* __restrict__ order, int ntiles,
+                                                           unsigned* __restrict__ next) {
+  __shared__ __align__(16) float s_tf[5 * VVLIC_TF_ENTRIES];
+  __shared__ long long s_acc[kAccSize];
+  for (int i = threadIdx.x; i < kAccSize; i += blockDim.x) s_acc[i] = 0;
+  load_tf(a, s_tf);  // includes __syncthreads
+  const int lane = threadIdx.x & 31;
+  const int tiles_x = (a.W + kWarpTileW - 1) / kWarpTileW;
+  float4 Dloc[kSegment];
+  float3 Ploc[kSegment];
+  for (;;) {
+    unsigned t = 0;
+    if (lane == 0) t = atomicAdd(next, 1u);
+    t = __shfl_sync(0xffffffffu, t, 0);
+    if (t >= (unsigned)ntiles) break;
+    const unsigned tile = __ldg(order + t);
+    const int px = (int)(tile % tiles_x) * kWarpTileW + (lane & (kWarpTileW - 1));
+    const int py = (int)(tile / tiles_x) * kWarpTileH + (lane / kWarpTileW);
+    const bool in_image = px < a.W && py < a.H;
+    const size_t ray = in_image ? (size_t)py * a.W + px : 0;
+    float3 pos0 = f3(0.f, 0.f, 0.f), dir = f3(0.f, 0.f, 0.f);
+    int S = 0;
+    float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (in_image && ray_setup(a, px, py, pos0, dir)) {
+      S = (int)min(a.tape_n[ray], (uint32_t)a.tape_stride);
+      g = g_img[ray];
+    }
+    const int nseg = (S + kSegment - 1) / kSegment;
+    const int nseg_warp = __reduce_max_sync(0xffffffffu, (unsigned)nseg);
+    for (int seg = nseg_warp - 1; seg >= 0; --seg) {
+      const bool act_seg = seg < nseg;
+      int cnt = 0;
+      if (act_seg) {
+        const float4* ck = a.tape_ck + 2 * (ray * a.tape_nck + seg);
+        const float4 p4 = ck[0];
+        float3 p = f3(p4.x, p4.y, p4.z);
+        float4 D = ck[1];
+        cnt = min(kSegment, S - seg * kSegment);
+        for (int kk = 0; kk < cnt; ++kk) {
+          Ploc[kk] = p;
+          Dloc[kk] = D;
+          const float2 rec = a.tape_is[ray * a.tape_stride + seg * kSegment + kk];
+          D = blend(D, unlit_source_rgba(a, s_tf, rec.x, rec.y));
+          p = add3(p, scl3(dir, a.step_size));
+        }
+      }
+      for (int kk = kSegment - 1; kk >= 0; --kk) {
+        float gIraw = 0.0f;
+        float3 pk = f3(0.f, 0.f, 0.f);
+        if (kk < cnt) {
+          const float2 rec = a.tape_is[ray * a.tape_stride + seg * kSegment + kk];
+          const float I = rec.x;
+          const Src s = unlit_source(a, s_tf, I, rec.y);
+          const float4 sv = premultiplied(s);
+          const float4 Dp = Dloc[kk];
+          pk = Ploc[kk];
+          const float om = 1.0f - Dp.w;
+          // clamp((1 - Dp.a) * s + Dp) per channel: derivative 1 on [0, 1]
+          const float ux = fmaf(om, sv.x, Dp.x), uy = fmaf(om, sv.y, Dp.y), uz = fmaf(om, sv.z, Dp.z),
+                      uw = fmaf(om, sv.w, Dp.w);
+          const float gx = (ux >= 0.f && ux <= 1.f) ? g.x : 0.f, gy = (uy >= 0.f && uy <= 1.f) ? g.y : 0.f,
+                      gz = (uz >= 0.f && uz <= 1.f) ? g.z : 0.f, gw = (uw >= 0.f && uw <= 1.f) ? g.w : 0.f;
+          const float4 ds = make_float4(om * gx, om * gy, om * gz, om * gw);
+          float4 gp = make_float4(gx, gy, gz, gw);
+          gp.w -= gx * sv.x + gy * sv.y + gz * sv.z + gw * sv.w;
+          // s = (col * alpha, alpha)
+          const float dcx = ds.x * s.alpha, dcy = ds.y * s.alpha, dcz = ds.z * s.alpha;
+          const float dalpha = ds.x * s.col.x + ds.y * s.col.y + ds.z * s.col.z + ds.w;
+          const float dba = s.base > 0.0f ? a.alpha_corr * powf(s.base, a.alpha_corr - 1.0f) : 0.0f;
+          const float da0 = dalpha * dba;
+          // a0 = opacity(1.3 I) * tf.a
+          const float dop = da0 * s.tf.w, dtfa = da0 * s.op;
+          fixed_add(s_acc + kAccOpac + s.lo.i0, dop * (1.0f - s.lo.t));
+          fixed_add(s_acc + kAccOpac + s.lo.i1, dop * s.lo.t);
+          const float* op = s_tf + 4 * VVLIC_TF_ENTRIES;
+          float dI = s.lo.inside ? dop * (op[s.lo.i1] - op[s.lo.i0]) * (float)VVLIC_TF_ENTRIES * 1.3f : 0.0f;
+          // col = I * tf.rgb * illumScale
+          const float ci = I * a.illum_scale;
+          const float dtf[4] = {dcx * ci, dcy * ci, dcz * ci, dtfa};
+          dI += (dcx * s.tf.x + dcy * s.tf.y + dcz * s.tf.z) * a.illum_scale;
+#pragma unroll
+          for (int ch = 0; ch < 4; ++ch) {
+            fixed_add(s_acc + kAccTF + 4 * s.lt.i0 + ch, dtf[ch] * (1.0f - s.lt.t));
+            fixed_add(s_acc + kAccTF + 4 * s.lt.i1 + ch, dtf[ch] * s.lt.t);
+          }
+          gIraw = dI * a.intensity_scale;
+          g = gp;
+        }
+        if (__any_sync(0xffffffffu, gIraw != 0.0f)) tap_gradients<ST, FL, NL, INTEG>(a, pk, gIraw, s_acc + kAccTaps);
+      }
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < kAccSize; i += blockDim.x)
+    if (s_acc[i] != 0) atomicAdd(reinterpret_cast<unsigned long long*>(acc + i), (unsigned long long)s_acc[i]);
+}
+
+template <int ST, int FL, int NL, int INTEG>
+static cudaError_t launch_adjoint_one(const RenderArgs& a, const float4* g_img, long long* acc, const Schedule& sch,
+                                      cudaStream_t s) {
+  auto kern = adjoint_kernel<ST, FL, NL, INTEG>;
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, 0);
+  if (e != cudaSuccess) return e;
+  kern<<<std::max(1, per_sm) * sch.num_sms, kThreads, 0, s>>>(a, g_img, acc, sch.order, sch.ntiles, sch.next);
+  return cudaGetLastError();
+}
+
+template <int ST, int FL, int NL>
+static cudaError_t launch_adjoint_layout(const RenderArgs& a, int integ, const float4* g_img, long long* acc,
+                                         const Schedule& sch, cudaStream_t s) {
+  if (integ == VVLIC_EULER) return launch_adjoint_one<ST, FL, NL, VVLIC_EULER>(a, g_img, acc, sch, s);
+  if (integ == VVLIC_HEUN) return launch_adjoint_one<ST, FL, NL, VVLIC_HEUN>(a, g_img, acc, sch, s);
+  return launch_adjoint_one<ST, FL, NL, VVLIC_RK4>(a, g_img, acc, sch, s);
+}
+
+template <int ST>
+static cudaError_t launch_adjoint_storage(const RenderArgs& a, int sampler, int integ, const float4* g_img,
+                                         long long* acc, const Schedule& sch, cudaStream_t s) {
+  switch (sampler) {
+    case VVLIC_SAMPLER_GATHER: return launch_adjoint_layout<ST, kGather, kGather>(a, integ, g_img, acc, sch, s);
+    case VVLIC_SAMPLER_CELL: return launch_adjoint_layout<ST, kCell, kCell>(a, integ, g_img, acc, sch, s);
+    case VVLIC_SAMPLER_TEXTURE:
+      if constexpr (ST == VVLIC_STORAGE_BF16) return cudaErrorNotSupported;
+      else return launch_adjoint_layout<ST, kTexture, kTexture>(a, integ, g_img, acc, sch, s);
+    case VVLIC_SAMPLER_HYBRID:
+      if constexpr (ST == VVLIC_STORAGE_BF16) return cudaErrorNotSupported;
+      else return launch_adjoint_layout<ST, kTexture, kCell>(a, integ, g_img, acc, sch, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace vvlic

@@ -1,0 +1,11 @@
+// Adjoint instantiations for field storage VVLIC_STORAGE_BF16.
+#include "adjoint.cuh"
+
+namespace vvlic {
+
+cudaError_t launch_adjoint_bf16(const RenderArgs& a, int sampler, int integ, const float4* g_img, long long* acc,
+                               const Schedule& sch, cudaStream_t s) {
+  return launch_adjoint_storage<VVLIC_STORAGE_BF16>(a, sampler, integ, g_img, acc, sch, s);
+}
+
+}  // namespace vvlic

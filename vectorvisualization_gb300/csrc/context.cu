@@ -329,6 +329,9 @@ extern "C" vvlic_status vvlic_destroy(vvlic_ctx* c) {
   if (c->d_image) cudaFree(c->d_image);
   if (c->d_upload) cudaFree(c->d_upload);
   if (c->d_sched) cudaFree(c->d_sched);
+  if (c->d_tape) cudaFree(c->d_tape);
+  if (c->d_tape_flag) cudaFree(c->d_tape_flag);
+  if (c->d_acc) cudaFree(c->d_acc);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->stream) cudaStreamDestroy(c->stream);

@@ -284,6 +284,75 @@ cudaError_t launch_tile_order(const RenderArgs& a, int ntiles, int tiles_x, int 
 
 }  // namespace vvlic
 
+namespace {
+
+// Queue schedule for one image: longest-first tile order in the context's scratch.
+vvlic_status make_schedule(vvlic_ctx* c, const RenderArgs& a, const Geometry& gm, int w, int h, cudaStream_t s,
+                           Schedule& sch) {
+  const int tiles_x = (w + 7) / 8, ntiles = tiles_x * ((h + 3) / 4);
+  const size_t words = 2 * (size_t)ntiles + 2 * 1024 + 1;
+  if (c->sched_cap < words) {
+    if (c->d_sched) cudaFree(c->d_sched);
+    c->d_sched = nullptr;
+    c->sched_cap = 0;
+    cudaError_t e = cudaMalloc(&c->d_sched, words * sizeof(unsigned));
+    if (e != cudaSuccess) return cuda_fail(c, e, "schedule allocation");
+    c->sched_cap = words;
+  }
+  // cost buckets of 2^shift samples so the longest possible chord fits 1024 buckets
+  const double diag = std::sqrt((double)gm.extent[0] * gm.extent[0] + (double)gm.extent[1] * gm.extent[1] +
+                                (double)gm.extent[2] * gm.extent[2]);
+  const double maxcost = diag / a.step_size + 2.0;
+  int shift = 0;
+  while ((maxcost / (double)(1u << shift)) >= 1024.0 && shift < 31) ++shift;
+  unsigned* scratch = c->d_sched;
+  cudaError_t e = launch_tile_order(a, ntiles, tiles_x, shift, scratch, s);
+  sch.order = scratch + ntiles;
+  sch.ntiles = ntiles;
+  sch.next = scratch + 2 * (size_t)ntiles + 2 * 1024;
+  if (e == cudaSuccess) e = cudaMemsetAsync(sch.next, 0, sizeof(unsigned), s);
+  if (e != cudaSuccess) return cuda_fail(c, e, "schedule");
+  return VVLIC_OK;
+}
+
+// Tape buffers for a recording render: per ray `stride` samples (the longest chord / spacing,
+// capped by the two loop bounds) and a checkpoint every kSegment samples.
+vvlic_status prepare_tape(vvlic_ctx* c, const Geometry& gm, int w, int h, RenderArgs& a, cudaStream_t s) {
+  const double diag = std::sqrt((double)gm.extent[0] * gm.extent[0] + (double)gm.extent[1] * gm.extent[1] +
+                                (double)gm.extent[2] * gm.extent[2]);
+  const double bound = std::min(diag / a.step_size + 3.0, (double)a.num_iter * (double)a.num_iter);
+  const int stride = std::max(1, (int)std::ceil(bound));
+  const int nck = (stride + kSegment - 1) / kSegment;
+  const size_t rays = (size_t)w * h;
+  const size_t b_is = rays * stride * sizeof(float2), b_ck = rays * nck * 2 * sizeof(float4),
+               b_n = rays * sizeof(uint32_t);
+  const size_t bytes = b_ck + b_is + b_n;
+  if (c->tape_cap < bytes) {
+    if (c->d_tape) cudaFree(c->d_tape);
+    c->d_tape = nullptr;
+    c->tape_cap = 0;
+    cudaError_t e = cudaMalloc(&c->d_tape, bytes);
+    if (e != cudaSuccess) return cuda_fail(c, e, "adjoint tape allocation");
+    c->tape_cap = bytes;
+  }
+  if (!c->d_tape_flag) {
+    cudaError_t e = cudaMalloc(&c->d_tape_flag, sizeof(unsigned long long));
+    if (e != cudaSuccess) return cuda_fail(c, e, "adjoint tape flag");
+  }
+  char* base = (char*)c->d_tape;
+  a.tape_ck = (float4*)base;
+  a.tape_is = (float2*)(base + b_ck);
+  a.tape_n = (uint32_t*)(base + b_ck + b_is);
+  a.tape_overflow = c->d_tape_flag;
+  a.tape_stride = stride;
+  a.tape_nck = nck;
+  cudaError_t e = cudaMemsetAsync(c->d_tape_flag, 0, sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return cuda_fail(c, e, "adjoint tape flag");
+  return VVLIC_OK;
+}
+
+}  // namespace
+
 extern "C" vvlic_status vvlic_render_device(vvlic_ctx* c, int32_t vol_id, float* d_out, int32_t w, int32_t h,
                                            uint32_t* d_samples, void* stream) {
   if (!c) return VVLIC_ERR_BAD_HANDLE;
@@ -298,35 +367,18 @@ extern "C" vvlic_status vvlic_render_device(vvlic_ctx* c, int32_t vol_id, float*
   if (st) return st;
   a.out = d_out;
   a.samples = d_samples;
+  const bool record = c->params.record_tape != 0;
+  if (record) {
+    c->tape_valid = false;
+    if ((st = prepare_tape(c, it->second.geom, w, h, a, s))) return st;
+  }
   Schedule sch;
   sch.num_sms = c->num_sms;
   cudaError_t e = cudaMemsetAsync(c->d_counters, 0, 4 * sizeof(unsigned long long), s);
-  if (e == cudaSuccess && c->params.schedule == VVLIC_SCHEDULE_QUEUE) {
-    const int tiles_x = (w + 7) / 8, ntiles = tiles_x * ((h + 3) / 4);
-    const size_t words = 2 * (size_t)ntiles + 2 * 1024 + 1;
-    if (c->sched_cap < words) {
-      if (c->d_sched) cudaFree(c->d_sched);
-      c->d_sched = nullptr;
-      c->sched_cap = 0;
-      e = cudaMalloc(&c->d_sched, words * sizeof(unsigned));
-      if (e != cudaSuccess) return cuda_fail(c, e, "schedule allocation");
-      c->sched_cap = words;
-    }
-    // cost buckets of 2^shift samples so the longest possible chord fits 1024 buckets
-    const Geometry& gm = it->second.geom;
-    const double diag = std::sqrt((double)gm.extent[0] * gm.extent[0] + (double)gm.extent[1] * gm.extent[1] +
-                                  (double)gm.extent[2] * gm.extent[2]);
-    const double maxcost = diag / a.step_size + 2.0;
-    int shift = 0;
-    while ((maxcost / (double)(1u << shift)) >= 1024.0 && shift < 31) ++shift;
-    unsigned* scratch = c->d_sched;
-    e = launch_tile_order(a, ntiles, tiles_x, shift, scratch, s);
-    sch.order = scratch + ntiles;
-    sch.ntiles = ntiles;
-    sch.next = scratch + 2 * (size_t)ntiles + 2 * 1024;
-    if (e == cudaSuccess) e = cudaMemsetAsync(sch.next, 0, sizeof(unsigned), s);
-  }
-  if (e == cudaSuccess) e = cudaEventRecord(c->ev0, s);
+  if (e != cudaSuccess) return cuda_fail(c, e, "render");
+  if (c->params.schedule == VVLIC_SCHEDULE_QUEUE && (st = make_schedule(c, a, it->second.geom, w, h, s, sch)))
+    return st;
+  e = cudaEventRecord(c->ev0, s);
   if (e == cudaSuccess)
     e = launch_raycast(a, it->second.storage, c->params.sampler, c->params.integrator,
                        c->params.illum == VVLIC_ILLUM_GRADIENT, sch, s);
@@ -335,6 +387,88 @@ extern "C" vvlic_status vvlic_render_device(vvlic_ctx* c, int32_t vol_id, float*
   c->stats_pending = true;
   c->stats.sample_steps = 0;
   c->stats_steps_per_sample = (uint64_t)(a.lb + a.lf);
+  if (record) {
+    c->tape_valid = true;
+    c->tape_vol = vol_id;
+    c->tape_w = w;
+    c->tape_h = h;
+    c->tape_storage = it->second.storage;
+    c->tape_sampler = c->params.sampler;
+    c->tape_integ = c->params.integrator;
+    c->tape_illum = c->params.illum;
+    c->tape_args = a;
+  }
+  return VVLIC_OK;
+}
+
+namespace vvlic_adjoint_out {
+
+__global__ void fixed_to_float_kernel(const long long* acc, int n_tf, int n_op, int n_taps, float* tf, float* op,
+                                      float* taps, const unsigned long long* overflow) {
+  const float nan = __int_as_float(0x7fc00000);
+  const bool bad = *overflow != 0;
+  const double k = 1.0 / 1073741824.0;  // 2^-30
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_tf + n_op + n_taps; i += gridDim.x * blockDim.x) {
+    const float v = bad ? nan : (float)((double)acc[i] * k);
+    if (i < n_tf) {
+      if (tf) tf[i] = v;
+    } else if (i < n_tf + n_op) {
+      if (op) op[i - n_tf] = v;
+    } else if (taps) {
+      taps[i - n_tf - n_op] = v;
+    }
+  }
+}
+
+}  // namespace vvlic_adjoint_out
+
+extern "C" vvlic_status vvlic_render_adjoint(vvlic_ctx* c, int32_t vol_id, const float* d_dl_drgba, int32_t w,
+                                            int32_t h, float* d_dl_dtf, float* d_dl_dopacity, float* d_dl_dtaps,
+                                            void* stream) {
+  if (!c) return VVLIC_ERR_BAD_HANDLE;
+  if (!d_dl_drgba) return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "render_adjoint: null cotangent");
+  if (!c->tape_valid || c->tape_vol != vol_id || c->tape_w != w || c->tape_h != h)
+    return fail(c, VVLIC_ERR_NOT_READY,
+                "render_adjoint: the last render of this context did not record a tape for volume %d at %dx%d "
+                "(set params.record_tape)", vol_id, w, h);
+  if (c->tape_illum != VVLIC_ILLUM_NONE)
+    return fail(c, VVLIC_ERR_UNSUPPORTED, "render_adjoint: only the unlit shading (illumLIC) is differentiated");
+  if (c->vols.find(vol_id) == c->vols.end())
+    return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "render_adjoint: unknown volume %d", vol_id);
+  DeviceGuard g(c->device);
+  cudaStream_t s = (cudaStream_t)stream;
+  const int acc_size = 5 * VVLIC_TF_ENTRIES + kMaxTaps;
+  cudaError_t e = cudaSuccess;
+  if (!c->d_acc) {
+    e = cudaMalloc(&c->d_acc, acc_size * sizeof(long long));
+    if (e != cudaSuccess) return cuda_fail(c, e, "adjoint accumulators");
+  }
+  e = cudaMemsetAsync(c->d_acc, 0, acc_size * sizeof(long long), s);
+  if (e != cudaSuccess) return cuda_fail(c, e, "adjoint");
+  const RenderArgs& a = c->tape_args;
+  Schedule sch;
+  sch.num_sms = c->num_sms;
+  vvlic_status st = make_schedule(c, a, c->vols[vol_id].geom, w, h, s, sch);
+  if (st) return st;
+  e = cudaEventRecord(c->ev0, s);
+  const float4* gi = (const float4*)d_dl_drgba;
+  if (e == cudaSuccess) {
+    switch (c->tape_storage) {
+      case VVLIC_STORAGE_F32: e = launch_adjoint_f32(a, c->tape_sampler, c->tape_integ, gi, c->d_acc, sch, s); break;
+      case VVLIC_STORAGE_F16: e = launch_adjoint_f16(a, c->tape_sampler, c->tape_integ, gi, c->d_acc, sch, s); break;
+      case VVLIC_STORAGE_UNORM8: e = launch_adjoint_u8(a, c->tape_sampler, c->tape_integ, gi, c->d_acc, sch, s); break;
+      default: e = launch_adjoint_bf16(a, c->tape_sampler, c->tape_integ, gi, c->d_acc, sch, s); break;
+    }
+  }
+  if (e == cudaSuccess) e = cudaEventRecord(c->ev1, s);
+  if (e == cudaSuccess) {
+    const int n_taps = a.lb + a.lf + 1;
+    vvlic_adjoint_out::fixed_to_float_kernel<<<8, 256, 0, s>>>(c->d_acc, 4 * VVLIC_TF_ENTRIES, VVLIC_TF_ENTRIES, n_taps, d_dl_dtf,
+                                            d_dl_dopacity, d_dl_dtaps, c->d_tape_flag);
+    e = cudaGetLastError();
+  }
+  if (e != cudaSuccess) return cuda_fail(c, e, "render_adjoint launch");
+  c->stats_pending = true;
   return VVLIC_OK;
 }
 

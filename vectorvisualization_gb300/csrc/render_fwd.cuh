@@ -25,6 +25,10 @@ __device__ __forceinline__ void store_pixel(const RenderArgs& a, int px, int py,
   const size_t pix = (size_t)py * a.W + px;
   reinterpret_cast<float4*>(a.out)[pix] = dest;
   if (a.samples) a.samples[pix] = samples;
+  if (a.tape_n) {
+    a.tape_n[pix] = samples;
+    if (samples > (uint32_t)a.tape_stride) atomicAdd(a.tape_overflow, 1ull);  // tape too short
+  }
 }
 
 __device__ __forceinline__ void flush_counters(const RenderArgs& a, uint32_t samples, uint32_t hits) {

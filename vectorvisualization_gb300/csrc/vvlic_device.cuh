@@ -42,8 +42,18 @@ struct RenderArgs {
   float gate_lo, gate_hi;
   int num_iter, lb, lf, illum, tf_index, sof, gate, quirks;
   float light_pos[3], spec_exp, light_diff[3], light_spec[3], light_amb[3];
+  // adjoint tape (recording forward / adjoint only): per ray `tape_stride` samples of
+  // (intensity, TF coordinate), `tape_nck` checkpoints of (position, dest before the sample)
+  // every kSegment samples, and the sample count
+  float2* tape_is;
+  float4* tape_ck;
+  uint32_t* tape_n;
+  unsigned long long* tape_overflow;  // rays with more samples than tape_stride
+  int tape_stride, tape_nck;
   float taps[kMaxTaps];
 };
+
+constexpr int kSegment = 32;  // adjoint checkpoint interval (samples)
 
 // ------------------------------------------------------------------------------------------
 // small vector helpers
@@ -548,13 +558,23 @@ __device__ __forceinline__ float4 trace_pixel(const RenderArgs& a, const float* 
   hit = 1;
   float4 src = make_float4(0.f, 0.f, 0.f, 0.f);
   bool outside = false;
+  const size_t ray = (size_t)py * a.W + px;
   for (int j = 0; !outside && j < a.num_iter; ++j) {
     for (int i = 0; i < a.num_iter; ++i) {
       const float4 f = Field<ST, FL>::sample(a, pos);
-      const float4 tf = tf_rgba(s_tf, a.tf_index == VVLIC_TF_INDEX_MAGNITUDE ? f.w : f.z);
+      const float tfc = a.tf_index == VVLIC_TF_INDEX_MAGNITUDE ? f.w : f.z;
+      const float4 tf = tf_rgba(s_tf, tfc);
       float4 il = compute_lic<ST, FL, NL, INTEG, GRAD>(a, pos, f);
-      ++samples;
       il.w *= a.intensity_scale;
+      if (a.tape_is) {  // record for the adjoint
+        if (samples % kSegment == 0 && samples / kSegment < (uint32_t)a.tape_nck) {
+          float4* ck = a.tape_ck + 2 * (ray * a.tape_nck + samples / kSegment);
+          ck[0] = make_float4(pos.x, pos.y, pos.z, 0.f);
+          ck[1] = dest;
+        }
+        if (samples < (uint32_t)a.tape_stride) a.tape_is[ray * a.tape_stride + samples] = make_float2(il.w, tfc);
+      }
+      ++samples;
       src = shade(a, s_tf, il, tf, pos, dir);
       dest = blend(dest, src);
       pos = add3(pos, scl3(dir, a.step_size));

@@ -103,6 +103,14 @@ struct vvlic_ctx {
   unsigned* d_sched = nullptr;    // tile order scratch of the queue schedule
   size_t sched_cap = 0;           // in 4-byte words
   int num_sms = 1;
+  // adjoint tape of the last recording render
+  void* d_tape = nullptr;
+  size_t tape_cap = 0;
+  unsigned long long* d_tape_flag = nullptr;  // overflow count of the recording render
+  long long* d_acc = nullptr;                 // fixed-point gradient accumulators
+  bool tape_valid = false;
+  int tape_vol = 0, tape_w = 0, tape_h = 0, tape_storage = 0, tape_sampler = 0, tape_integ = 0, tape_illum = 0;
+  vvlic::RenderArgs tape_args;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   bool stats_pending = false;
   uint64_t stats_steps_per_sample = 0;
