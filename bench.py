@@ -433,6 +433,9 @@ def run_ours(args, dist: Dist):
             if storage == w.storage:
                 variants[storage] = {"gss": value / dist.world, "ms": ms_per_step}
                 continue
+            if storage == "bf16" and args.sampler in ("texture", "hybrid"):
+                variants[storage] = {"unsupported": "no bf16 texture format"}
+                continue
             vid2 = ctx.upload_field(w.field, storage=storage)
             with torch.cuda.stream(stream):
                 frame2 = lambda: ctx.render_device(vid2, out.data_ptr(), W, H, None, sh)  # noqa: E731

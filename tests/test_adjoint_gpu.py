@@ -65,14 +65,18 @@ def test_adjoint_matches_fp64_oracle(ctx, oracle, sampler, storage):
         enc = oracle.round_storage(enc, storage)
     sc = oracle.Scene(enc, w.noise, w.tf_rgba, w.tf_opac, taps=taps, inv_filter_area=0.7)
     ref_img, _ = sc.render(w.params, w.views[0], w.width, w.height)
-    assert float(np.sqrt(np.mean((img - ref_img) ** 2))) < 1e-4
+    # the texture unit filters the field with 8-bit weights: its images (and so the gradients)
+    # carry that error; the exact samplers are held to the tight bound
+    hw = sampler in ("texture", "hybrid")
+    assert float(np.sqrt(np.mean((img - ref_img) ** 2))) < (1e-3 if hw else 1e-4)
     # the oracle adjoint with the GPU's own cotangent
     g = (2.0 * (img.astype(np.float64) - target)).astype(np.float32)
     r_tf, r_op, r_taps = oracle.adjoint(sc, w.params, w.views[0], w.width, w.height, g)
     for got, ref in ((d_tf, r_tf), (d_op, r_op), (d_taps, r_taps)):
         scale = max(float(np.abs(ref).max()), 1e-6)
         err = float(np.abs(got - ref).max())
-        assert err <= 2e-3 * scale, (err, scale)
+        print(f"adjoint {sampler}/{storage}: max err {err:.3e} of scale {scale:.3e}")
+        assert err <= (2e-2 if hw else 2e-3) * scale, (err, scale)
     assert float(np.abs(r_taps).max()) > 0 and float(np.abs(r_tf).max()) > 0
 
 
