@@ -455,7 +455,8 @@ def run_ours(args, dist: Dist):
 
     # forward + adjoint on the differentiable-fit configuration (unlit; 4 views)
     if not args.no_adjoint and dist.rank == 0:
-        line["fwd_adjoint"] = bench_adjoint(ctx, torch, stream, flush, args)
+        with capi.Context(dev) as actx:
+            line["fwd_adjoint"] = bench_adjoint(actx, torch, stream, flush, args)
 
     # end to end through the C ABI with host buffers
     if not args.no_e2e:

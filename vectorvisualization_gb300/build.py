@@ -59,7 +59,9 @@ def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -
     os.makedirs(BUILD_DIR, exist_ok=True)
     os.makedirs(OUT_DIR, exist_ok=True)
     stamp = os.path.join(OUT_DIR, "libvvlic.stamp")
-    digest = _digest(" ".join(ARCH + COMMON) + os.uname().machine)
+    # extra nvcc flags (e.g. -DVVLIC_MIN_BLOCKS=8 to trade registers for occupancy)
+    extra = os.environ.get("VVLIC_NVCC_EXTRA", "").split()
+    digest = _digest(" ".join(ARCH + COMMON + extra) + os.uname().machine)
     if not force and os.path.exists(LIB) and os.path.exists(stamp):
         with open(stamp) as fh:
             if fh.read().strip() == digest:
@@ -67,7 +69,7 @@ def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -
 
     def compile_one(src: str) -> str:
         obj = os.path.join(BUILD_DIR, src.replace(".cu", ".o"))
-        cmd = [nvcc, *ARCH, *COMMON, "-I", INCLUDE, "-c", os.path.join(CSRC, src), "-o", obj]
+        cmd = [nvcc, *ARCH, *COMMON, *extra, "-I", INCLUDE, "-c", os.path.join(CSRC, src), "-o", obj]
         if src in NO_FMA:
             cmd.insert(1, "-fmad=false")
         if verbose:

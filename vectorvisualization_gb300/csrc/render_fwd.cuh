@@ -15,6 +15,11 @@ namespace vvlic {
 constexpr int kTileW = 16, kTileH = 8;  // static schedule: 128 threads, a warp covers 16x2 pixels
 constexpr int kWarpTileW = 8, kWarpTileH = 4;  // queue schedule: one warp per 8x4 pixel tile
 constexpr int kThreads = 128;
+// Minimum resident CTAs per SM requested from the compiler for the render kernels (a register
+// cap of 65536 / (kThreads * VVLIC_MIN_BLOCKS) per thread); 1 leaves the choice to ptxas.
+#ifndef VVLIC_MIN_BLOCKS
+#define VVLIC_MIN_BLOCKS 1
+#endif
 
 __device__ __forceinline__ void load_tf(const RenderArgs& a, float* s_tf) {
   for (int i = threadIdx.x; i < 5 * VVLIC_TF_ENTRIES; i += blockDim.x) s_tf[i] = __ldg(a.tf + i);
@@ -41,7 +46,7 @@ __device__ __forceinline__ void flush_counters(const RenderArgs& a, uint32_t sam
 }
 
 template <int ST, int FL, int NL, int INTEG, bool GRAD>
-__global__ void __launch_bounds__(kThreads) raycast_kernel(const __grid_constant__ RenderArgs a) {
+__global__ void __launch_bounds__(kThreads, VVLIC_MIN_BLOCKS) raycast_kernel(const __grid_constant__ RenderArgs a) {
   __shared__ __align__(16) float s_tf[5 * VVLIC_TF_ENTRIES];
   load_tf(a, s_tf);
   const int px = blockIdx.x * kTileW + (threadIdx.x % kTileW);
@@ -55,7 +60,7 @@ __global__ void __launch_bounds__(kThreads) raycast_kernel(const __grid_constant
 }
 
 template <int ST, int FL, int NL, int INTEG, bool GRAD>
-__global__ void __launch_bounds__(kThreads) raycast_queue_kernel(const __grid_constant__ RenderArgs a,
+__global__ void __launch_bounds__(kThreads, VVLIC_MIN_BLOCKS) raycast_queue_kernel(const __grid_constant__ RenderArgs a,
                                                                  const uint32_t* __restrict__ order, int ntiles,
                                                                  unsigned* __restrict__ next) {
   __shared__ __align__(16) float s_tf[5 * VVLIC_TF_ENTRIES];
