@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--c3", action="store_true", help="also time the 64-volume batch")
+    ap.add_argument("--c3-volumes", type=int, default=64)
     return ap.parse_args()
 
 
@@ -334,6 +336,57 @@ def bench_adjoint(ctx, torch, stream, flush, args):
     }
 
 
+def bench_batch(ctx, torch, stream, flush, args):
+    """C3: 64 volumes with per-axis dims from {64, 80, ..., 192} (ABC or vortex, own seeds), 1-8
+    random views each at 512^2, filters mixed box / triangle / cos^2, L in [15, 60], FP16
+    storage, Heun; one persistent launch per batch, replayed from a CUDA graph."""
+    from vectorvisualization_gb300 import capi, workloads as wl
+
+    t0 = time.perf_counter()
+    vols, noise, base = wl.c3(volumes=args.c3_volumes)
+    gen_s = time.perf_counter() - t0
+    ctx.upload_noise(noise)
+    ctx.set_tf(*wl.default_tf())
+    jobs, outs = [], []
+    voxels = 0
+    for bv in vols:
+        vid = ctx.upload_field(bv.field, storage=args.storage)
+        voxels += bv.field.shape[0] * bv.field.shape[1] * bv.field.shape[2]
+        table = capi.make_filter_table(bv.filter_kind, 256)
+        for v in bv.views:
+            p = capi.Params.from_buffer_copy(base)
+            p.steps_forward = p.steps_backward = bv.L
+            p.sampler = capi.SAMPLER[args.sampler]
+            out = torch.empty((512, 512, 4), dtype=torch.float32, device="cuda")
+            outs.append(out)
+            jobs.append(capi.make_job(vid, out.data_ptr(), 512, 512, v, p, table))
+    sh = stream.cuda_stream
+    tw, smp, tune_ms = ctx.batch_autotune(jobs, sh)
+    ctx.batch_render(jobs, sh)  # capture with the tuned shape
+    stream.synchronize()
+    times = []
+    for _ in range(2):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            e0.record(stream)
+            ctx.batch_render(jobs, sh)
+            e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    st = ctx.stats()
+    ms = min(times)
+    return {
+        "workload": f"C3 {len(vols)} volumes (dims 64..192 per axis), {len(jobs)} views at 512^2, L 15..60, "
+                    f"mixed box/triangle/cos2, {args.storage}",
+        "jobs": len(jobs), "voxels": voxels, "ms_per_batch": ms, "frames_per_s": len(jobs) / (ms / 1e3),
+        "gss": st.sample_steps / (ms / 1e3) / 1e9, "sample_steps": int(st.sample_steps),
+        "autotune": {"tile": f"{tw}x{32 // tw}", "sampler": [k for k, v in capi.SAMPLER.items() if v == smp][0],
+                     "best_ms": tune_ms},
+        "cuda_graph": True, "generation_s": gen_s,
+    }
+
+
 def run_ours(args, dist: Dist):
     import torch
 
@@ -457,6 +510,9 @@ def run_ours(args, dist: Dist):
     if not args.no_adjoint and dist.rank == 0:
         with capi.Context(dev) as actx:
             line["fwd_adjoint"] = bench_adjoint(actx, torch, stream, flush, args)
+    if args.c3 and dist.rank == 0:
+        with capi.Context(dev) as bctx:
+            line["batch"] = bench_batch(bctx, torch, stream, flush, args)
 
     # end to end through the C ABI with host buffers
     if not args.no_e2e:

@@ -298,6 +298,38 @@ vvlic_status vvlic_render_device(vvlic_ctx* ctx, int32_t vol_id, float* d_out_rg
 vvlic_status vvlic_render_adjoint(vvlic_ctx* ctx, int32_t vol_id, const float* d_dl_drgba, int32_t w, int32_t h,
                                   float* d_dl_dtf, float* d_dl_dopacity, float* d_dl_dtaps, void* stream);
 
+/* ---- batches (no reference counterpart: the reference renders one volume per frame) ---- */
+
+/* One render job of a batch: a volume seen from a view into a device image, with its own
+ * parameters and, optionally, its own filter table (else the context's filter). */
+typedef struct vvlic_job {
+  int32_t vol_id;
+  int32_t w, h;
+  float* d_out;                 /* device RGBA image, w*h*4 floats */
+  vvlic_view view;
+  vvlic_params params;
+  const uint8_t* filter_table;  /* host table (centred in the next power of two) or NULL */
+  int32_t filter_width;
+  int32_t filter_clamp;
+} vvlic_job;
+
+/* Render n jobs in one persistent launch: every (job, 8x4 tile) item goes into one device work
+ * queue ordered longest-first over the whole batch.  All jobs must share the field storage,
+ * sampler, integrator and lighting (they are compiled variants); LIC length, step sizes,
+ * filter, view, image size, TF index and the other runtime parameters may differ.  The noise,
+ * scalar volume and transfer function are the context's.  The launch sequence is captured in a
+ * CUDA graph the first time a batch of a given shape is rendered and replayed afterwards
+ * (only the job table is re-uploaded).  `stream` must not be the legacy default stream (NULL
+ * selects the context's stream).  Asynchronous; vvlic_get_stats reports the batch totals. */
+vvlic_status vvlic_batch_render(vvlic_ctx* ctx, const vvlic_job* jobs, int32_t n, void* stream);
+
+/* Time the batch under each warp tile shape (8x4, 4x8, 16x2, 32x1 pixels) and each exact-noise
+ * sampler (HYBRID, CELL) that the jobs' storage supports, keep the fastest for later batches of
+ * this context and report it (tile width, sampler, milliseconds).  Renders the batch several
+ * times.  Synchronous. */
+vvlic_status vvlic_batch_autotune(vvlic_ctx* ctx, const vvlic_job* jobs, int32_t n, void* stream,
+                                  int32_t* best_tile_w, int32_t* best_sampler, float* best_ms);
+
 /* Statistics of the last render (samples are counted on the device every render). */
 vvlic_status vvlic_get_stats(vvlic_ctx* ctx, vvlic_stats* stats);
 

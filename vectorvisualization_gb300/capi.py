@@ -88,6 +88,22 @@ class View(C.Structure):
     ]
 
 
+class Job(C.Structure):
+    """vvlic_job (include/vvlic.h)."""
+
+    _fields_ = [
+        ("vol_id", C.c_int32),
+        ("w", C.c_int32),
+        ("h", C.c_int32),
+        ("d_out", C.c_void_p),
+        ("view", View),
+        ("params", Params),
+        ("filter_table", C.c_void_p),
+        ("filter_width", C.c_int32),
+        ("filter_clamp", C.c_int32),
+    ]
+
+
 class Stats(C.Structure):
     _fields_ = [
         ("samples", C.c_uint64),
@@ -126,6 +142,8 @@ _SIGS = {
     "vvlic_render_device": (_I, [_P, _I, _P, _I, _I, _P, _P]),
     "vvlic_get_stats": (_I, [_P, C.POINTER(Stats)]),
     "vvlic_render_adjoint": (_I, [_P, _I, _P, _I, _I, _P, _P, _P, _P]),
+    "vvlic_batch_render": (_I, [_P, C.POINTER(Job), _I, _P]),
+    "vvlic_batch_autotune": (_I, [_P, C.POINTER(Job), _I, _P, C.POINTER(_I), C.POINTER(_I), C.POINTER(C.c_float)]),
     "vvlic_composite_background": (_I, [_P, _I, _I, _P]),
     "vvlic_noise_gradients_device": (_I, [_P, _I, _I, _I, _I, _P, _P, _P]),
     "vvlic_noise_gradients_device_noalloc": (_I, [_P, _I, _I, _I, _I, _P, _P, _P]),
@@ -188,6 +206,22 @@ def make_filter_table(kind: str | int, width: int = 256) -> np.ndarray:
 
 def _ptr(a: np.ndarray | None):
     return None if a is None else a.ctypes.data
+
+
+def make_job(vol_id: int, d_out: int, w: int, h: int, view: View, params: Params,
+             filter_table: np.ndarray | None = None, clamp: int = KERNEL_CLAMP_BORDER) -> Job:
+    """A vvlic_job; keeps a reference to the filter table for the call's lifetime."""
+    j = Job()
+    j.vol_id, j.w, j.h, j.d_out = vol_id, w, h, d_out
+    j.view = view
+    j.params = params
+    if filter_table is not None:
+        t = np.ascontiguousarray(filter_table, dtype=np.uint8)
+        j._table = t
+        j.filter_table = t.ctypes.data
+        j.filter_width = t.size
+        j.filter_clamp = clamp
+    return j
 
 
 class Context:
@@ -350,6 +384,18 @@ class Context:
         """Gradients of the last recording render (params.record_tape = 1) into device buffers."""
         self._check(self._lib.vvlic_render_adjoint(self.h, vid, d_grad_img, w, h, d_tf, d_opac, d_taps, stream or None),
                     "render_adjoint")
+
+    def batch_render(self, jobs: "list[Job]", stream: int = 0):
+        arr = (Job * len(jobs))(*jobs)
+        self._keep = (arr, [getattr(j, "_table", None) for j in jobs])
+        self._check(self._lib.vvlic_batch_render(self.h, arr, len(jobs), stream or None), "batch_render")
+
+    def batch_autotune(self, jobs: "list[Job]", stream: int = 0):
+        arr = (Job * len(jobs))(*jobs)
+        tw, smp, ms = _I(0), _I(0), C.c_float(0)
+        self._check(self._lib.vvlic_batch_autotune(self.h, arr, len(jobs), stream or None, C.byref(tw), C.byref(smp),
+                                                   C.byref(ms)), "batch_autotune")
+        return tw.value, smp.value, ms.value
 
     def stats(self) -> Stats:
         s = Stats()

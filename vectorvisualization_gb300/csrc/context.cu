@@ -94,6 +94,28 @@ static void effective_steps(const vvlic_params& p, int* lb, int* lf) {
 }
 
 // Tap weights w[j], j = -L_b..L_f, at the offsets computeLIC walks (inc_lic.glsl:219-262).
+void derive_taps_from_table(const uint8_t* t, int W, int clamp, bool is_box, int lb, int lf, float* taps,
+                            float* inv_area) {
+  taps[lb] = (float)kernel_lookup(t, W, 0.5, clamp);
+  double off = 0.5, kb = lb > 0 ? 0.5 / lb : 0.0, kf = lf > 0 ? 0.5 / lf : 0.0;
+  for (int i = 1; i <= lb; ++i) {
+    off -= kb;
+    taps[lb - i] = (float)kernel_lookup(t, W, off, clamp);
+  }
+  off = 0.5;
+  for (int i = 1; i <= lf; ++i) {
+    off += kf;
+    taps[lb + i] = (float)kernel_lookup(t, W, off, clamp);
+  }
+  if (is_box) {
+    *inv_area = 0.5f;  // LICFilter::createBoxFilter (dataset.cpp:1412)
+  } else {
+    float area = 0.0f;  // calcFilterKernelInvArea (dataset.cpp:1503-1512)
+    for (int i = 0; i < W; ++i) area += t[i];
+    *inv_area = 0.5f * W * 255.0f / area;
+  }
+}
+
 vvlic_status derive_taps(const vvlic_ctx* c, int lb, int lf, float* taps, float* inv_area) {
   if (c->taps_override) {
     if (c->taps_lb != lb || c->taps_lf != lf) return VVLIC_ERR_INVALID_ARGUMENT;
@@ -101,27 +123,19 @@ vvlic_status derive_taps(const vvlic_ctx* c, int lb, int lf, float* taps, float*
     *inv_area = c->taps_inv_area;
     return VVLIC_OK;
   }
-  const uint8_t* t = c->filter;
-  const int W = c->filter_width;
-  taps[lb] = (float)kernel_lookup(t, W, 0.5, c->filter_clamp);
-  double off = 0.5, kb = lb > 0 ? 0.5 / lb : 0.0, kf = lf > 0 ? 0.5 / lf : 0.0;
-  for (int i = 1; i <= lb; ++i) {
-    off -= kb;
-    taps[lb - i] = (float)kernel_lookup(t, W, off, c->filter_clamp);
-  }
-  off = 0.5;
-  for (int i = 1; i <= lf; ++i) {
-    off += kf;
-    taps[lb + i] = (float)kernel_lookup(t, W, off, c->filter_clamp);
-  }
-  if (c->filter_is_box) {
-    *inv_area = 0.5f;  // LICFilter::createBoxFilter (dataset.cpp:1412)
-  } else {
-    float area = 0.0f;  // calcFilterKernelInvArea (dataset.cpp:1503-1512)
-    for (int i = 0; i < W; ++i) area += t[i];
-    *inv_area = 0.5f * W * 255.0f / area;
-  }
+  derive_taps_from_table(c->filter, c->filter_width, c->filter_clamp, c->filter_is_box, lb, lf, taps, inv_area);
   return VVLIC_OK;
+}
+
+// A filter table as vvlic_set_filter_table stores it: centred in the next power of two.
+int centre_filter_table(const uint8_t* table, int width, uint8_t* out1024, bool* is_box) {
+  const int W = next_pow2(width), shift = (W - width) / 2;
+  std::memset(out1024, 0, 1024);
+  std::memcpy(out1024 + shift, table, width);
+  bool box = true;
+  for (int i = 0; i < W; ++i) box = box && out1024[i] == 255;
+  *is_box = box;
+  return W;
 }
 
 // Rays of the view for a volume (camera.cpp:56-67 followed by glTranslatef(-center),
@@ -332,6 +346,11 @@ extern "C" vvlic_status vvlic_destroy(vvlic_ctx* c) {
   if (c->d_tape) cudaFree(c->d_tape);
   if (c->d_tape_flag) cudaFree(c->d_tape_flag);
   if (c->d_acc) cudaFree(c->d_acc);
+  if (c->batch_graph) cudaGraphExecDestroy(c->batch_graph);
+  if (c->h_jobs) cudaFreeHost(c->h_jobs);
+  if (c->d_jobs) cudaFree(c->d_jobs);
+  if (c->d_batch) cudaFree(c->d_batch);
+  if (c->ev_jobs) cudaEventDestroy(c->ev_jobs);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->stream) cudaStreamDestroy(c->stream);

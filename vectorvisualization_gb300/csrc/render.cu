@@ -108,7 +108,11 @@ namespace vvlic {
 
 // Fill the kernel argument block for one volume and image size.
 vvlic_status build_render_args(vvlic_ctx* c, Volume& v, int W, int H, cudaStream_t s, RenderArgs& a) {
-  const vvlic_params& p = c->params;
+  return build_render_args_ex(c, v, W, H, s, c->params, c->view, nullptr, a);
+}
+
+vvlic_status build_render_args_ex(vvlic_ctx* c, Volume& v, int W, int H, cudaStream_t s, const vvlic_params& p,
+                                  const vvlic_view& view, const JobFilter* filter, RenderArgs& a) {
   std::memset(&a, 0, sizeof a);
   if (!c->noise.d_texels) return fail(c, VVLIC_ERR_NOT_READY, "render: no noise uploaded");
   if (p.illum == VVLIC_ILLUM_GRADIENT && c->noise.ch != 4)
@@ -116,9 +120,12 @@ vvlic_status build_render_args(vvlic_ctx* c, Volume& v, int W, int H, cudaStream
   if (p.scalar_gate && !c->d_scalar) return fail(c, VVLIC_ERR_NOT_READY, "render: scalar gate on, no scalar volume");
   int lb = p.low_res ? 15 : p.steps_backward, lf = p.low_res ? 15 : p.steps_forward;
   float inv_area = 0.5f;
-  if (derive_taps(c, lb, lf, a.taps, &inv_area))
+  if (filter) {
+    derive_taps_from_table(filter->table, filter->width, filter->clamp, filter->is_box, lb, lf, a.taps, &inv_area);
+  } else if (derive_taps(c, lb, lf, a.taps, &inv_area)) {
     return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "render: explicit taps were set for L_b=%d L_f=%d, params have %d/%d",
                 c->taps_lb, c->taps_lf, lb, lf);
+  }
   vvlic_status st;
   a.n[0] = v.n[0];
   a.n[1] = v.n[1];
@@ -157,7 +164,7 @@ vvlic_status build_render_args(vvlic_ctx* c, Volume& v, int W, int H, cudaStream
   a.W = W;
   a.H = H;
   double rc[21];
-  derive_rays(c->view, v.geom, W, H, rc);
+  derive_rays(view, v.geom, W, H, rc);
   for (int i = 0; i < 3; ++i) {
     a.o0[i] = (float)rc[i];
     a.o1[i] = (float)rc[3 + i];
@@ -385,6 +392,7 @@ extern "C" vvlic_status vvlic_render_device(vvlic_ctx* c, int32_t vol_id, float*
   if (e == cudaSuccess) e = cudaEventRecord(c->ev1, s);
   if (e != cudaSuccess) return cuda_fail(c, e, "render launch");
   c->stats_pending = true;
+  c->last_was_batch = false;
   c->stats.sample_steps = 0;
   c->stats_steps_per_sample = (uint64_t)(a.lb + a.lf);
   if (record) {
@@ -507,7 +515,8 @@ extern "C" vvlic_status vvlic_get_stats(vvlic_ctx* c, vvlic_stats* out) {
     if (e != cudaSuccess) return cuda_fail(c, e, "get_stats");
     c->stats.samples = h[0];
     c->stats.rays = h[1];
-    c->stats.sample_steps = h[0] * c->stats_steps_per_sample;
+    // a batch mixes LIC lengths and counts its sample-steps on the device
+    c->stats.sample_steps = c->last_was_batch ? h[2] : h[0] * c->stats_steps_per_sample;
     c->stats.kernel_ms = ms;
     c->stats_pending = false;
   }

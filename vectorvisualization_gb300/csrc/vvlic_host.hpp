@@ -111,6 +111,19 @@ struct vvlic_ctx {
   bool tape_valid = false;
   int tape_vol = 0, tape_w = 0, tape_h = 0, tape_storage = 0, tape_sampler = 0, tape_integ = 0, tape_illum = 0;
   vvlic::RenderArgs tape_args;
+  // batches
+  vvlic::RenderArgs* h_jobs = nullptr;  // pinned staging of the job table
+  size_t h_jobs_cap = 0;
+  vvlic::RenderArgs* d_jobs = nullptr;
+  size_t d_jobs_cap = 0;
+  unsigned* d_batch = nullptr;          // job tile starts + order scratch
+  size_t batch_cap = 0;                 // words
+  cudaEvent_t ev_jobs = nullptr;        // the staging buffer may be rewritten after this
+  cudaGraphExec_t batch_graph = nullptr;
+  uint64_t batch_key[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  int batch_tile_w = 8;                 // warp tile width (autotuned)
+  int batch_sampler_override = -1;      // sampler chosen by the autotuner (-1: the jobs')
+  bool last_was_batch = false;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   bool stats_pending = false;
   uint64_t stats_steps_per_sample = 0;
@@ -123,5 +136,17 @@ vvlic_status fail(vvlic_ctx* c, vvlic_status s, const char* fmt, ...);
 vvlic_status cuda_fail(vvlic_ctx* c, cudaError_t e, const char* what);
 Geometry make_geometry(const int n[3], const float* slice_dist);
 vvlic_status derive_taps(const vvlic_ctx* c, int lb, int lf, float* taps, float* inv_area);
+void derive_taps_from_table(const uint8_t* t, int W, int clamp, bool is_box, int lb, int lf, float* taps,
+                            float* inv_area);
+int centre_filter_table(const uint8_t* table, int width, uint8_t* out1024, bool* is_box);
+// Argument block of one render job.  `params`/`view` default to the context's; `filter` (a
+// centred 1024-entry table of width `fw`), when given, replaces the context's filter.
+struct JobFilter {
+  const uint8_t* table = nullptr;
+  int width = 0, clamp = 0;
+  bool is_box = false;
+};
+vvlic_status build_render_args_ex(vvlic_ctx* c, Volume& v, int W, int H, cudaStream_t s, const vvlic_params& p,
+                                  const vvlic_view& view, const JobFilter* filter, RenderArgs& a);
 void derive_rays(const vvlic_view& v, const Geometry& g, int W, int H, double* coeffs);
 }  // namespace vvlic

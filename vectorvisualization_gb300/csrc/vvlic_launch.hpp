@@ -40,6 +40,50 @@ cudaError_t launch_adjoint_bf16(const RenderArgs& a, int sampler, int integ, con
 cudaError_t launch_adjoint_u8(const RenderArgs& a, int sampler, int integ, const float4* g_img, long long* acc,
                               const Schedule& sch, cudaStream_t s);
 
+// Batched render (batch_<storage>.cu): one persistent launch over (job, tile) items.
+struct BatchLaunch {
+  const RenderArgs* jobs;
+  const uint2* order;
+  int nitems;
+  unsigned* next;
+  const float* tf;
+  unsigned long long* counters;  // [0] samples, [1] rays, [2] sample-steps
+  int tw;                        // tile width in pixels (a warp covers tw x 32/tw)
+  int num_sms;
+};
+cudaError_t launch_batch_f32(const BatchLaunch& b, int sampler, int integ, bool grad, cudaStream_t s);
+cudaError_t launch_batch_f16(const BatchLaunch& b, int sampler, int integ, bool grad, cudaStream_t s);
+cudaError_t launch_batch_bf16(const BatchLaunch& b, int sampler, int integ, bool grad, cudaStream_t s);
+cudaError_t launch_batch_u8(const BatchLaunch& b, int sampler, int integ, bool grad, cudaStream_t s);
+// Word layout of the batch scratch: job tile starts (njobs+1), per-tile buckets, the (job,
+// tile) order as 8-byte aligned uint2 pairs, the bucket histogram and offsets, the queue
+// counter.
+struct BatchScratch {
+  unsigned* start;
+  unsigned* bucket;
+  uint2* order;
+  unsigned* hist;
+  unsigned* offsets;
+  unsigned* next;
+  size_t words;
+};
+inline BatchScratch batch_scratch(unsigned* base, int njobs, int ntiles) {
+  BatchScratch b;
+  const size_t s0 = ((size_t)njobs + 2) & ~(size_t)1, nb = ((size_t)ntiles + 1) & ~(size_t)1;
+  b.start = base;
+  b.bucket = base ? base + s0 : nullptr;
+  b.order = base ? reinterpret_cast<uint2*>(base + s0 + nb) : nullptr;
+  b.hist = base ? base + s0 + nb + 2 * (size_t)ntiles : nullptr;
+  b.offsets = base ? b.hist + 1024 : nullptr;
+  b.next = base ? b.offsets + 1024 : nullptr;
+  b.words = s0 + nb + 2 * (size_t)ntiles + 2048 + 2;
+  return b;
+}
+// Longest-first (job, tile) order over a batch (batch.cu); start[] holds njobs+1 entries
+// (exclusive prefix of tiles per job).
+cudaError_t launch_batch_order(const RenderArgs* jobs, const BatchScratch& b, int njobs, int ntiles, int tw,
+                               int shift, cudaStream_t s);
+
 // Longest-first tile order for the queue schedule (render.cu): per-tile chord cost, a
 // counting sort over 1024 cost buckets, scatter.  `scratch` holds 2*ntiles + 2048 + 1 words.
 cudaError_t launch_tile_order(const RenderArgs& a, int ntiles, int tiles_x, int shift, unsigned* scratch,

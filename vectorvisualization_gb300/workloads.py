@@ -360,6 +360,42 @@ def c4(size: int = 128, image: int = 512, views: int = 4) -> Workload:
     )
 
 
+@dataclass
+class BatchVolume:
+    field: np.ndarray
+    kind: str
+    seed: int
+    views: list
+    L: int
+    filter_kind: str
+
+
+def c3(volumes: int = 64, image: int = 512, seed: int = 3, max_views: int = 8, dims=tuple(range(64, 193, 16))):
+    """Batched uneven volumes: per-axis dims from {64, 80, ..., 192}, each an ABC or a vortex field
+    from its own seed, 1..max_views random views at image^2, filters mixed box / triangle / cos^2,
+    L in [15, 60].  Returns (volumes, shared noise, base params)."""
+    rng = SplitMix64(seed)
+    out = []
+    kinds = ("box", "triangle", "cos2")
+    for v in range(volumes):
+        u = rng.uniform(7)
+        n = tuple(int(dims[min(int(u[i] * len(dims)), len(dims) - 1)]) for i in range(3))
+        vseed = 1000 + v
+        kind = "abc" if u[3] < 0.5 else "vortex"
+        field = abc_field(n) if kind == "abc" else vortex_field(n, seed=vseed)
+        nviews = 1 + min(int(u[4] * max_views), max_views - 1)
+        vr = SplitMix64(vseed * 7 + 1)
+        views = [random_view(vr) for _ in range(nviews)]
+        L = 15 + min(int(u[5] * 46), 45)
+        out.append(BatchVolume(field, kind, vseed, views, L, kinds[min(int(u[6] * 3), 2)]))
+    p = capi.params_default()
+    p.integrator = capi.HEUN
+    p.step_size_lic = 0.01
+    p.step_size_vol = 1.0 / 128.0
+    p.tf_index = capi.TF_INDEX_MAGNITUDE
+    return out, dense_noise(128, seed=seed * 10), p
+
+
 def c5(size: int = 512, image: int = 2048, frames: int = 64, device: str | None = None) -> Workload:
     """Large turbulence orbit."""
     p = capi.params_default()
