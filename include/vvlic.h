@@ -146,8 +146,17 @@ typedef struct vvlic_params {
   int32_t sampler;        /* VVLIC_SAMPLER_* (HYBRID) */
   int32_t schedule;       /* VVLIC_SCHEDULE_* (QUEUE) */
   int32_t record_tape;    /* renders record what vvlic_render_adjoint needs (0) */
-  int32_t reserved[5];
+  int32_t technique;      /* VVLIC_TECHNIQUE_* = the reference's RenderTechnique (RAYCAST) */
+  int32_t reserved[4];
 } vvlic_params;
+
+/* Render technique, numbered like the reference's RenderTechnique (types.h:63-72):
+ *   VOLUME    - direct volume rendering of the encoded vector field (vectorfield_fragment.glsl);
+ *   RAYCAST   - the LIC ray-cast (lic3d_fragment.glsl);
+ *   SLICING   - LIC on view-aligned slices (lic3d_slicing_fragment.glsl);
+ *   LICVOLUME - ray-cast of a precomputed LIC volume (raycast_lic3d_fragment.glsl), see
+ *               vvlic_compute_lic_volume. */
+enum { VVLIC_TECHNIQUE_VOLUME = 0, VVLIC_TECHNIQUE_RAYCAST = 1, VVLIC_TECHNIQUE_SLICING = 2, VVLIC_TECHNIQUE_LICVOLUME = 3 };
 
 /* Work distribution of a render launch:
  *   QUEUE  - persistent CTAs pull 8x4-pixel ray tiles from a device work queue, tiles ordered
@@ -297,6 +306,15 @@ vvlic_status vvlic_render_device(vvlic_ctx* ctx, int32_t vol_id, float* d_out_rg
  * the tape was too short for a ray.  Asynchronous on `stream`. */
 vvlic_status vvlic_render_adjoint(vvlic_ctx* ctx, int32_t vol_id, const float* d_dl_drgba, int32_t w, int32_t h,
                                   float* d_dl_dtf, float* d_dl_dopacity, float* d_dl_dtaps, void* stream);
+
+/* LIC-volume precompute: Renderer::renderLICVolume (renderer.cpp:1311-1374) with
+ * lic3d_volume_fragment.glsl — computeLIC * licKernel.b * gradientScale at every voxel centre of
+ * an nx*ny*nz grid (the reference uses 512^3, renderer.cpp:97) with the current parameters,
+ * kept with the volume (FP32; the reference's buffer is RGBA16F) for VVLIC_TECHNIQUE_LICVOLUME
+ * renders.  Synchronous. */
+vvlic_status vvlic_compute_lic_volume(vvlic_ctx* ctx, int32_t vol_id, int32_t nx, int32_t ny, int32_t nz);
+/* Copy a volume's LIC volume (nx*ny*nz floats, x fastest) to host memory. */
+vvlic_status vvlic_download_lic_volume(vvlic_ctx* ctx, int32_t vol_id, float* out, uint64_t capacity);
 
 /* ---- batches (no reference counterpart: the reference renders one volume per frame) ---- */
 

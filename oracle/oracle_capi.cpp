@@ -27,6 +27,8 @@ typedef struct vvo_inputs {
   int32_t filter_is_box;
   const double* taps;          /* explicit taps (L_b+L_f+1) or NULL */
   double inv_filter_area;      /* used with explicit taps */
+  const float* licvol;         /* LIC volume for the LICVOLUME technique, or NULL */
+  int32_t ln[3];
 } vvo_inputs;
 
 int32_t vvo_abi(void) { return 1; }
@@ -87,7 +89,7 @@ static int effective_steps(const vvlic_params* p, int* lb, int* lf) {
  * precision: 64 = double oracle, 32 = float CPU baseline.  threads <= 0: OpenMP default. */
 int32_t vvo_render(const vvo_inputs* vi, const vvlic_params* p, const double* ray_coeffs, int32_t w, int32_t h,
                    const int32_t* rows, int32_t nrows, float* out, uint32_t* samples, int32_t precision,
-                   int32_t threads) {
+                   int32_t threads, const vvlic_view* view) {
   int lb, lf;
   int ntaps = effective_steps(p, &lb, &lf);
   std::vector<double> taps(ntaps);
@@ -115,10 +117,56 @@ int32_t vvo_render(const vvo_inputs* vi, const vvlic_params* p, const double* ra
   in.tf_opac = vi->tf_opac;
   in.taps = taps.data();
   in.inv_filter_area = inv_area;
+  in.licvol = vi->licvol;
+  for (int i = 0; i < 3; ++i) in.ln[i] = vi->ln[i];
+  if (p->technique == VVLIC_TECHNIQUE_LICVOLUME && !in.licvol) return -3;
+  double slicing[5] = {0, 0, 0, 0, 0};
+  if (p->technique == VVLIC_TECHNIQUE_SLICING) {
+    if (!view) return -4;
+    int ns = 0;
+    float spacing = p->low_res ? 2.0f * p->step_size_vol : p->step_size_vol;
+    vvo::slicing_setup(*view, in.n, in.slice_dist, spacing, slicing, &slicing[3], &ns);
+    slicing[4] = ns;
+  }
   if (precision == 32)
-    vvo::render<float>(in, *p, ray_coeffs, w, h, rows, nrows, out, samples, threads);
+    vvo::render<float>(in, *p, ray_coeffs, w, h, rows, nrows, out, samples, threads, slicing);
   else
-    vvo::render<double>(in, *p, ray_coeffs, w, h, rows, nrows, out, samples, threads);
+    vvo::render<double>(in, *p, ray_coeffs, w, h, rows, nrows, out, samples, threads, slicing);
+  return 0;
+}
+
+/* LIC volume (lic3d_volume_fragment.glsl) of ln[0]*ln[1]*ln[2] voxels into out. */
+int32_t vvo_lic_volume(const vvo_inputs* vi, const vvlic_params* p, const int32_t ln[3], float* out) {
+  int lb, lf;
+  int ntaps = effective_steps(p, &lb, &lf);
+  std::vector<double> taps(ntaps);
+  double inv_area;
+  if (vi->taps) {
+    for (int i = 0; i < ntaps; ++i) taps[i] = vi->taps[i];
+    inv_area = vi->inv_filter_area;
+  } else {
+    if (!vi->filter_table) return -1;
+    vvo::filter_taps<double>(vi->filter_table, vi->filter_width, vi->filter_clamp, lb, lf, taps.data());
+    inv_area = vvo::filter_inv_area(vi->filter_table, vi->filter_width, vi->filter_is_box != 0);
+  }
+  vvo::Inputs in;
+  in.field = vi->field;
+  for (int i = 0; i < 3; ++i) {
+    in.n[i] = vi->n[i];
+    in.slice_dist[i] = vi->slice_dist[i];
+    in.m[i] = vi->m[i];
+    in.sn[i] = vi->sn[i];
+  }
+  in.noise = vi->noise;
+  in.noise_channels = vi->noise_channels;
+  in.scalar = vi->scalar;
+  in.tf_rgba = vi->tf_rgba;
+  in.tf_opac = vi->tf_opac;
+  in.taps = taps.data();
+  in.inv_filter_area = inv_area;
+  in.licvol = nullptr;
+  int l[3] = {ln[0], ln[1], ln[2]};
+  vvo::lic_volume<double>(in, *p, l, out);
   return 0;
 }
 

@@ -37,6 +37,8 @@ class Inputs(C.Structure):
         ("filter_is_box", C.c_int32),
         ("taps", C.c_void_p),
         ("inv_filter_area", C.c_double),
+        ("licvol", C.c_void_p),
+        ("ln", C.c_int32 * 3),
     ]
 
 
@@ -65,7 +67,9 @@ def lib() -> C.CDLL:
         l.vvo_filter_taps.argtypes = [P, I, I, I, I, P]
         l.vvo_view_rays.argtypes = [P, P, P, I, I, P]
         l.vvo_geometry.argtypes = [P, P, P]
-        l.vvo_render.argtypes = [C.POINTER(Inputs), P, P, I, I, P, I, P, P, I, I]
+        l.vvo_render.argtypes = [C.POINTER(Inputs), P, P, I, I, P, I, P, P, I, I, P]
+        l.vvo_lic_volume.argtypes = [C.POINTER(Inputs), P, P, P]
+        l.vvo_lic_volume.restype = I
         l.vvo_render.restype = I
         l.vvo_max_threads.restype = I
         l.vvo_adjoint.argtypes = [C.POINTER(Inputs), P, P, I, I, P, P, P, P, I]
@@ -194,10 +198,25 @@ class Scene:
         smp = np.zeros((nr, w), np.uint32)
         st = lib().vvo_render(C.byref(self.inputs), C.byref(params), rc.ctypes.data, w, h,
                               None if r is None else r.ctypes.data, nr, img.ctypes.data, smp.ctypes.data, precision,
-                              threads)
+                              threads, C.byref(view))
         if st != 0:
             raise RuntimeError(f"oracle render failed ({st})")
         return img, smp
+
+    def lic_volume(self, params: capi.Params, dims) -> np.ndarray:
+        """LIC volume of dims (nx, ny, nz), returned (nz, ny, nx)."""
+        ln = np.asarray(dims, np.int32)
+        out = np.empty((dims[2], dims[1], dims[0]), np.float32)
+        st = lib().vvo_lic_volume(C.byref(self.inputs), C.byref(params), ln.ctypes.data, out.ctypes.data)
+        if st != 0:
+            raise RuntimeError(f"oracle LIC volume failed ({st})")
+        return out
+
+    def attach_lic_volume(self, licvol: np.ndarray):
+        self._licvol = np.ascontiguousarray(licvol, dtype=np.float32)
+        self.inputs.licvol = self._licvol.ctypes.data
+        for k, v in enumerate(self._licvol.shape[::-1]):
+            self.inputs.ln[k] = int(v)
 
 
 def adjoint(scene: "Scene", params: capi.Params, view: capi.View, w: int, h: int, g_img: np.ndarray,

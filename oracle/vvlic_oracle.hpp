@@ -354,6 +354,8 @@ struct Inputs {
   const float* tf_opac;    /* 256 */
   const double* taps;      /* L_b + L_f + 1 kernel weights */
   double inv_filter_area;
+  const float* licvol = nullptr; /* LIC volume (LICVOLUME technique), ln[0]*ln[1]*ln[2] */
+  int ln[3] = {0, 0, 0};
 };
 
 /* LINEAR + CLAMP_TO_EDGE trilinear at texture coordinate s (GL 2.1 eq. 3.23/3.27). */
@@ -544,7 +546,8 @@ static inline void view_rays(const vvlic_view& v, const int n[3], const float sd
 }
 
 /* Slab test against [0, extent]: returns false for a miss; t_entry on hit. */
-template <class R> static inline bool ray_entry(const R o[3], const R d[3], const R ext[3], bool clamp0, R* t_entry) {
+template <class R> static inline bool ray_entry(const R o[3], const R d[3], const R ext[3], bool clamp0, R* t_entry,
+                                               R* t_exit = nullptr) {
   R tn = -INFINITY, tf = INFINITY;
   for (int i = 0; i < 3; ++i) {
     if (d[i] == R(0)) {
@@ -563,6 +566,7 @@ template <class R> static inline bool ray_entry(const R o[3], const R d[3], cons
     tn = std::max(tn, R(0));
   }
   *t_entry = tn;
+  if (t_exit) *t_exit = tf;
   return true;
 }
 
@@ -689,10 +693,128 @@ template <class R> static inline V4<R> shade(const LicCtx<R>& c, V4<R> illum, V4
 }
 
 /* ------------------------------------------------------------------------------------- */
+/* other techniques                                                                        */
+/* ------------------------------------------------------------------------------------- */
+/* Slab planes of ViewSlicing::setupSlicing (slicing.cpp:42-103): unit view direction v in
+ * object space (modelview row 2 / its z translation), depth D = 2 sum |v_i| ext_i/2, N slices. */
+static inline void slicing_setup(const vvlic_view& v, const int n[3], const float sd[3], float spacing, double vout[3],
+                                 double* depth, int* ns) {
+  Geometry g = geometry(n, sd);
+  double dv[3];
+  if (v.projection == VVLIC_ORTHOGRAPHIC) {
+    for (int i = 0; i < 3; ++i) dv[i] = v.ortho_dir[i];
+  } else {
+    double qx = v.quat[0], qy = v.quat[1], qz = v.quat[2], qw = v.quat[3];
+    double qn = std::sqrt(qx * qx + qy * qy + qz * qz + qw * qw);
+    if (qn > 0) { qx /= qn; qy /= qn; qz /= qn; qw /= qn; } else { qw = 1; }
+    double row2[3] = {2 * (qx * qz - qy * qw), 2 * (qy * qz + qx * qw), 1 - 2 * (qx * qx + qy * qy)};
+    double m14 = (double)v.pan[2] - v.distance - (row2[0] * g.center[0] + row2[1] * g.center[1] + row2[2] * g.center[2]);
+    for (int i = 0; i < 3; ++i) dv[i] = row2[i] / m14;
+  }
+  double nn = std::sqrt(dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2]);
+  double d6 = 0.0;
+  for (int i = 0; i < 3; ++i) {
+    vout[i] = dv[i] / nn;
+    d6 += std::fabs(vout[i]) * 0.5 * g.extent[i];
+  }
+  *depth = 2.0 * d6;
+  *ns = (int)(*depth / spacing) + 1;
+}
+
+/* texture3D(licVolumeSampler, s).r with LINEAR + REPEAT (VolumeBuffer.cpp:43-57) */
+template <class R> static inline R tex3d_licvol(const Inputs& in, V3<R> s) {
+  const int* m = in.ln;
+  R u[3] = {s.x * R(m[0]) - R(0.5), s.y * R(m[1]) - R(0.5), s.z * R(m[2]) - R(0.5)};
+  int i0[3], i1[3];
+  R a[3];
+  for (int d = 0; d < 3; ++d) {
+    R fl = std::floor(u[d]);
+    a[d] = u[d] - fl;
+    long long b = (long long)fl, md = m[d];
+    i0[d] = (int)(((b % md) + md) % md);
+    i1[d] = (int)((((b + 1) % md) + md) % md);
+  }
+  R r = R(0);
+  for (int c = 0; c < 8; ++c) {
+    int xi = (c & 1) ? i1[0] : i0[0], yi = (c & 2) ? i1[1] : i0[1], zi = (c & 4) ? i1[2] : i0[2];
+    R w = ((c & 1) ? a[0] : R(1) - a[0]) * ((c & 2) ? a[1] : R(1) - a[1]) * ((c & 4) ? a[2] : R(1) - a[2]);
+    r += w * R(in.licvol[((size_t)zi * m[1] + yi) * m[0] + xi]);
+  }
+  return r;
+}
+
+/* LIC volume precompute (lic3d_volume_fragment.glsl:2-21) at voxel centres of an ln grid. */
+template <class R> static inline void lic_volume(const Inputs& in, const vvlic_params& p, const int ln[3], float* out) {
+  Uniforms<R> u = uniforms<R>(in, p);
+  Geometry g = geometry(in.n, in.slice_dist);
+  vvlic_params q = p;
+  q.illum = VVLIC_ILLUM_NONE;
+  LicCtx<R> c{&in, &q, &u, false};
+#if defined(_OPENMP)
+#pragma omp parallel for schedule(dynamic, 1)
+#endif
+  for (int z = 0; z < ln[2]; ++z)
+    for (int y = 0; y < ln[1]; ++y)
+      for (int x = 0; x < ln[0]; ++x) {
+        V3<R> pos{(R(x) + R(0.5)) / R(ln[0]) * R(g.scale[0]), (R(y) + R(0.5)) / R(ln[1]) * R(g.scale[1]),
+                  (R(z) + R(0.5)) / R(ln[2]) * R(g.scale[2])};
+        V4<R> f = tex3d_field<R>(in, pos);
+        out[((size_t)z * ln[1] + y) * ln[0] + x] = float(compute_lic<R>(c, pos, f).w * u.intensity_scale);
+      }
+}
+
+/* slicing (lic3d_slicing_fragment.glsl:5-74 over the planes of slicing.cpp:106-114) */
+template <class R> static inline uint32_t slice_pixel(const Inputs& in, const vvlic_params& p, const Uniforms<R>& u,
+                                                      const R o[3], const R d[3], R tn, R tfar, const double* vv,
+                                                      double depth, int ns, float out[4]) {
+  Geometry g = geometry(in.n, in.slice_dist);
+  LicCtx<R> c{&in, &p, &u, p.illum == VVLIC_ILLUM_GRADIENT};
+  V3<R> sv{u.scale_vol[0], u.scale_vol[1], u.scale_vol[2]};
+  V3<R> D{d[0], d[1], d[2]};
+  V3<R> dir = mul(normalize(D), sv);
+  V3<R> V{R(vv[0]), R(vv[1]), R(vv[2])};
+  R vd = dot(V, D);
+  V4<R> dest{R(0), R(0), R(0), R(0)};
+  uint32_t samples = 0;
+  if (vd == R(0)) return 0;
+  V3<R> oc{o[0] - R(g.center[0]), o[1] - R(g.center[1]), o[2] - R(g.center[2])};
+  R voc = dot(V, oc);
+  R step = R(depth) / R(ns);
+  for (int i = 0; i < ns; ++i) {
+    if (dest.w >= R(0.95)) break;
+    R di = R(-0.5) * R(depth) + (R(i) + R(0.5)) * step;
+    R ti = (di - voc) / vd;
+    if (!(ti >= tn && ti <= tfar)) continue;
+    V3<R> x{o[0] + ti * d[0], o[1] + ti * d[1], o[2] + ti * d[2]};
+    V3<R> pos = mul(x, sv);
+    V4<R> f = tex3d_field<R>(in, pos);
+    V4<R> tf{tex1d<R>(in.tf_rgba, 4, 0, f.w), tex1d<R>(in.tf_rgba, 4, 1, f.w), tex1d<R>(in.tf_rgba, 4, 2, f.w),
+             tex1d<R>(in.tf_rgba, 4, 3, f.w)};
+    if (!(tf.w > R(0.05))) continue;
+    V4<R> il = compute_lic<R>(c, pos, f);
+    ++samples;
+    il.w *= u.intensity_scale;
+    V4<R> src = shade<R>(c, il, tf, pos, dir);
+    src.x *= src.w;
+    src.y *= src.w;
+    src.z *= src.w;
+    R om = R(1) - dest.w;
+    dest = V4<R>{clamp01(om * src.x + dest.x), clamp01(om * src.y + dest.y), clamp01(om * src.z + dest.z),
+                 clamp01(om * src.w + dest.w)};
+  }
+  out[0] = (float)dest.x;
+  out[1] = (float)dest.y;
+  out[2] = (float)dest.z;
+  out[3] = (float)dest.w;
+  return samples;
+}
+
+/* ------------------------------------------------------------------------------------- */
 /* the ray: lic3d_fragment.glsl:5-99                                                       */
 /* ------------------------------------------------------------------------------------- */
 template <class R> static inline uint32_t render_pixel(const Inputs& in, const vvlic_params& p, const Uniforms<R>& u,
-                                                       const double* rc, int px, int py, float out[4]) {
+                                                       const double* rc, int px, int py, float out[4],
+                                                       const double* slicing = nullptr) {
   out[0] = out[1] = out[2] = out[3] = 0.0f;
   R o[3], d[3], ext[3];
   R uu = R(px) + R(0.5), vv = R(py) + R(0.5);
@@ -701,8 +823,10 @@ template <class R> static inline uint32_t render_pixel(const Inputs& in, const v
     d[i] = R(rc[9 + i]) + uu * R(rc[12 + i]) + vv * R(rc[15 + i]);
     ext[i] = u.extent[i];
   }
-  R te;
-  if (!ray_entry<R>(o, d, ext, rc[18] != 0.0, &te)) return 0;
+  R te, tx;
+  if (!ray_entry<R>(o, d, ext, rc[18] != 0.0, &te, &tx)) return 0;
+  if (p.technique == VVLIC_TECHNIQUE_SLICING)
+    return slice_pixel<R>(in, p, u, o, d, te, tx, slicing, slicing[3], (int)slicing[4], out);
   V3<R> sv{u.scale_vol[0], u.scale_vol[1], u.scale_vol[2]};
   V3<R> obj{o[0] + te * d[0], o[1] + te * d[1], o[2] + te * d[2]};
   V3<R> pos = mul(obj, sv);
@@ -712,6 +836,42 @@ template <class R> static inline uint32_t render_pixel(const Inputs& in, const v
   uint32_t samples = 0;
   bool outside = false;
   const R thr = R(p.alpha_threshold);
+  if (p.technique == VVLIC_TECHNIQUE_VOLUME || p.technique == VVLIC_TECHNIQUE_LICVOLUME) {
+    /* vectorfield_fragment.glsl:67-97 / raycast_lic3d_fragment.glsl:55-89: stop on dest.a */
+    vvlic_params q = p;
+    q.illum = VVLIC_ILLUM_NONE;
+    LicCtx<R> cq{&in, &q, &u, false};
+    for (int j = 0; !outside && j < u.num_iterations; ++j) {
+      for (int i = 0; i < u.num_iterations; ++i) {
+        V4<R> f = tex3d_field<R>(in, pos);
+        if (p.technique == VVLIC_TECHNIQUE_LICVOLUME) {
+          R idx = p.tf_index == VVLIC_TF_INDEX_MAGNITUDE ? f.w : f.z;
+          V4<R> tf{tex1d<R>(in.tf_rgba, 4, 0, idx), tex1d<R>(in.tf_rgba, 4, 1, idx), tex1d<R>(in.tf_rgba, 4, 2, idx),
+                   tex1d<R>(in.tf_rgba, 4, 3, idx)};
+          V4<R> il{R(0), R(0), R(0), tex3d_licvol<R>(in, pos)};
+          src = shade<R>(cq, il, tf, pos, dir);
+        } else {
+          src = V4<R>{f.x, f.y, f.z, tex1d<R>(in.tf_rgba, 4, 3, f.w)};
+        }
+        ++samples;
+        src.x *= src.w;
+        src.y *= src.w;
+        src.z *= src.w;
+        R om = R(1) - dest.w;
+        dest = V4<R>{clamp01(om * src.x + dest.x), clamp01(om * src.y + dest.y), clamp01(om * src.z + dest.z),
+                     clamp01(om * src.w + dest.w)};
+        pos = pos + dir * u.step_size;
+        outside = pos.x < R(0) || pos.y < R(0) || pos.z < R(0) || pos.x > u.tex_max[0] || pos.y > u.tex_max[1] ||
+                  pos.z > u.tex_max[2] || dest.w > thr;
+        if (outside) break;
+      }
+    }
+    out[0] = (float)dest.x;
+    out[1] = (float)dest.y;
+    out[2] = (float)dest.z;
+    out[3] = (float)dest.w;
+    return samples;
+  }
   for (int j = 0; !outside && j < u.num_iterations; ++j) {
     for (int i = 0; i < u.num_iterations; ++i) {
       V4<R> f = tex3d_field<R>(in, pos);
@@ -947,7 +1107,7 @@ template <class R> static inline void adjoint(const Inputs& in, const vvlic_para
 /* Render the rows listed in `rows` (all rows when rows == NULL) into out (nrows x W x 4). */
 template <class R> static inline void render(const Inputs& in, const vvlic_params& p, const double* rc, int W, int H,
                                              const int32_t* rows, int nrows, float* out, uint32_t* samples,
-                                             int threads) {
+                                             int threads, const double* slicing = nullptr) {
   Uniforms<R> u = uniforms<R>(in, p);
   int nr = rows ? nrows : H;
 #if defined(_OPENMP)
@@ -957,7 +1117,7 @@ template <class R> static inline void render(const Inputs& in, const vvlic_param
   for (int r = 0; r < nr; ++r) {
     int py = rows ? rows[r] : r;
     for (int px = 0; px < W; ++px) {
-      uint32_t s = render_pixel<R>(in, p, u, rc, px, py, out + 4 * ((size_t)r * W + px));
+      uint32_t s = render_pixel<R>(in, p, u, rc, px, py, out + 4 * ((size_t)r * W + px), slicing);
       if (samples) samples[(size_t)r * W + px] = s;
     }
   }

@@ -23,6 +23,7 @@ DTYPE_FLOAT32, DTYPE_UINT8 = 0, 1
 STORAGE = {"f32": 0, "f16": 1, "bf16": 2, "u8": 3}
 SAMPLER = {"gather": 0, "cell": 1, "texture": 2, "hybrid": 3}
 SCHEDULE = {"queue": 0, "static": 1}
+TECHNIQUE = {"volume": 0, "raycast": 1, "slicing": 2, "licvolume": 3}
 NOISE_SCALAR, NOISE_GRAD_SOBEL, NOISE_GRAD_CENTRAL = 0, 1, 2
 EULER, HEUN, RK4 = 0, 1, 2
 ILLUM_NONE, ILLUM_GRADIENT, ILLUM_ZOECKLER, ILLUM_MALLO = 0, 1, 2, 3
@@ -67,7 +68,8 @@ class Params(C.Structure):
         ("sampler", C.c_int32),
         ("schedule", C.c_int32),
         ("record_tape", C.c_int32),
-        ("reserved", C.c_int32 * 5),
+        ("technique", C.c_int32),
+        ("reserved", C.c_int32 * 4),
     ]
 
 
@@ -142,6 +144,8 @@ _SIGS = {
     "vvlic_render_device": (_I, [_P, _I, _P, _I, _I, _P, _P]),
     "vvlic_get_stats": (_I, [_P, C.POINTER(Stats)]),
     "vvlic_render_adjoint": (_I, [_P, _I, _P, _I, _I, _P, _P, _P, _P]),
+    "vvlic_compute_lic_volume": (_I, [_P, _I, _I, _I, _I]),
+    "vvlic_download_lic_volume": (_I, [_P, _I, _P, C.c_uint64]),
     "vvlic_batch_render": (_I, [_P, C.POINTER(Job), _I, _P]),
     "vvlic_batch_autotune": (_I, [_P, C.POINTER(Job), _I, _P, C.POINTER(_I), C.POINTER(_I), C.POINTER(C.c_float)]),
     "vvlic_composite_background": (_I, [_P, _I, _I, _P]),
@@ -384,6 +388,16 @@ class Context:
         """Gradients of the last recording render (params.record_tape = 1) into device buffers."""
         self._check(self._lib.vvlic_render_adjoint(self.h, vid, d_grad_img, w, h, d_tf, d_opac, d_taps, stream or None),
                     "render_adjoint")
+
+    def compute_lic_volume(self, vid: int, dims) -> None:
+        nx, ny, nz = dims
+        self._check(self._lib.vvlic_compute_lic_volume(self.h, vid, nx, ny, nz), "compute_lic_volume")
+
+    def download_lic_volume(self, vid: int, dims) -> np.ndarray:
+        nx, ny, nz = dims
+        out = np.empty((nz, ny, nx), np.float32)
+        self._check(self._lib.vvlic_download_lic_volume(self.h, vid, out.ctypes.data, out.nbytes), "download_lic_volume")
+        return out
 
     def batch_render(self, jobs: "list[Job]", stream: int = 0):
         arr = (Job * len(jobs))(*jobs)

@@ -179,6 +179,40 @@ void derive_rays(const vvlic_view& v, const Geometry& g, int W, int H, double* c
   c[18] = 1.0;
 }
 
+// Slicing set-up of ViewSlicing::setupSlicing (slicing.cpp:42-103): the unit view direction in
+// object space (the third row of the modelview matrix divided by its z translation, pointing
+// into the scene), the slab depth D = 2 * sum |v_i| * extent_i / 2 and N = (int)(D / spacing) + 1.
+void derive_slicing(const vvlic_view& v, const Geometry& g, float spacing, float vdir[3], float* depth, int* n) {
+  double dv[3];
+  if (v.projection == VVLIC_ORTHOGRAPHIC) {
+    for (int i = 0; i < 3; ++i) dv[i] = v.ortho_dir[i];
+  } else {
+    double x = v.quat[0], y = v.quat[1], z = v.quat[2], w = v.quat[3];
+    double qn = std::sqrt(x * x + y * y + z * z + w * w);
+    if (qn > 0) {
+      x /= qn;
+      y /= qn;
+      z /= qn;
+      w /= qn;
+    } else {
+      w = 1.0;
+    }
+    const double R2[3] = {2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)};  // row 2 of R(q)
+    const double Rc_z = R2[0] * g.center[0] + R2[1] * g.center[1] + R2[2] * g.center[2];
+    const double m14 = (double)v.pan[2] - v.distance - Rc_z;
+    for (int i = 0; i < 3; ++i) dv[i] = R2[i] / m14;
+  }
+  float f[3] = {(float)dv[0], (float)dv[1], (float)dv[2]};
+  const float inv = 1.0f / std::sqrt(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]);
+  float d6 = 0.0f;
+  for (int i = 0; i < 3; ++i) {
+    vdir[i] = f[i] * inv;
+    d6 += std::fabs(vdir[i]) * (0.5f * g.extent[i]);
+  }
+  *depth = 2.0f * d6;
+  *n = (int)(*depth / spacing) + 1;
+}
+
 }  // namespace vvlic
 
 // ------------------------------------------------------------------------------------------
@@ -214,6 +248,7 @@ extern "C" void vvlic_params_default(vvlic_params* p) {
   }
   p->sampler = VVLIC_SAMPLER_HYBRID;
   p->schedule = VVLIC_SCHEDULE_QUEUE;
+  p->technique = VVLIC_TECHNIQUE_RAYCAST;
 }
 
 extern "C" void vvlic_view_default(vvlic_view* v) {
@@ -315,6 +350,7 @@ extern "C" vvlic_status vvlic_create(vvlic_ctx** out, int32_t device) {
 }
 
 static void free_volume(Volume& v) {
+  if (v.d_licvol) cudaFree(v.d_licvol);
   if (v.tex) cudaDestroyTextureObject(v.tex);
   if (v.array) cudaFreeArray(v.array);
   if (v.d_texels) cudaFree(v.d_texels);
@@ -621,6 +657,8 @@ static vvlic_status check_params(vvlic_ctx* c, const vvlic_params& p) {
     return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "params: sampler %d", p.sampler);
   if (p.schedule != VVLIC_SCHEDULE_QUEUE && p.schedule != VVLIC_SCHEDULE_STATIC)
     return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "params: schedule %d", p.schedule);
+  if (p.technique < VVLIC_TECHNIQUE_VOLUME || p.technique > VVLIC_TECHNIQUE_LICVOLUME)
+    return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "params: technique %d", p.technique);
   return VVLIC_OK;
 }
 

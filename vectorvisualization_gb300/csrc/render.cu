@@ -211,6 +211,16 @@ vvlic_status build_render_args_ex(vvlic_ctx* c, Volume& v, int W, int H, cudaStr
   return VVLIC_OK;
 }
 
+cudaError_t launch_technique(int storage, const RenderArgs& a, const TechArgs& t, int sampler, int integ, bool grad,
+                             cudaStream_t s) {
+  switch (storage) {
+    case VVLIC_STORAGE_F32: return launch_technique_f32(a, t, sampler, integ, grad, s);
+    case VVLIC_STORAGE_F16: return launch_technique_f16(a, t, sampler, integ, grad, s);
+    case VVLIC_STORAGE_UNORM8: return launch_technique_u8(a, t, sampler, integ, grad, s);
+    default: return launch_technique_bf16(a, t, sampler, integ, grad, s);
+  }
+}
+
 cudaError_t launch_raycast(const RenderArgs& a, int storage, int sampler, int integ, bool grad, const Schedule& sch,
                            cudaStream_t s) {
   switch (storage) {
@@ -374,6 +384,35 @@ extern "C" vvlic_status vvlic_render_device(vvlic_ctx* c, int32_t vol_id, float*
   if (st) return st;
   a.out = d_out;
   a.samples = d_samples;
+  if (c->params.technique != VVLIC_TECHNIQUE_RAYCAST) {
+    if (c->params.record_tape)
+      return fail(c, VVLIC_ERR_UNSUPPORTED, "render: the adjoint tape is recorded by the RAYCAST technique only");
+    TechArgs t;
+    std::memset(&t, 0, sizeof t);
+    t.technique = c->params.technique;
+    const Volume& v = it->second;
+    if (t.technique == VVLIC_TECHNIQUE_SLICING) {
+      derive_slicing(c->view, v.geom, a.step_size, t.v, &t.depth, &t.nslices);
+      for (int i = 0; i < 3; ++i) t.c[i] = v.geom.center[i];
+    } else if (t.technique == VVLIC_TECHNIQUE_LICVOLUME) {
+      if (!v.d_licvol)
+        return fail(c, VVLIC_ERR_NOT_READY, "render: LICVOLUME needs vvlic_compute_lic_volume for volume %d", vol_id);
+      t.licvol = v.d_licvol;
+      for (int i = 0; i < 3; ++i) t.ln[i] = v.ln[i];
+      a.illum = VVLIC_ILLUM_NONE;  // raycast_lic3d_fragment.glsl shades with illumLIC
+    }
+    cudaError_t e = cudaMemsetAsync(c->d_counters, 0, 4 * sizeof(unsigned long long), s);
+    if (e == cudaSuccess) e = cudaEventRecord(c->ev0, s);
+    if (e == cudaSuccess)
+      e = launch_technique(v.storage, a, t, c->params.sampler, c->params.integrator,
+                           c->params.illum == VVLIC_ILLUM_GRADIENT && t.technique == VVLIC_TECHNIQUE_SLICING, s);
+    if (e == cudaSuccess) e = cudaEventRecord(c->ev1, s);
+    if (e != cudaSuccess) return cuda_fail(c, e, "render launch");
+    c->stats_pending = true;
+    c->last_was_batch = false;
+    c->stats_steps_per_sample = t.technique == VVLIC_TECHNIQUE_SLICING ? (uint64_t)(a.lb + a.lf) : 0;
+    return VVLIC_OK;
+  }
   const bool record = c->params.record_tape != 0;
   if (record) {
     c->tape_valid = false;
@@ -521,5 +560,60 @@ extern "C" vvlic_status vvlic_get_stats(vvlic_ctx* c, vvlic_stats* out) {
     c->stats_pending = false;
   }
   *out = c->stats;
+  return VVLIC_OK;
+}
+
+extern "C" vvlic_status vvlic_compute_lic_volume(vvlic_ctx* c, int32_t vol_id, int32_t nx, int32_t ny, int32_t nz) {
+  if (!c) return VVLIC_ERR_BAD_HANDLE;
+  auto it = c->vols.find(vol_id);
+  if (it == c->vols.end()) return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "compute_lic_volume: unknown volume %d", vol_id);
+  if (nx < 1 || ny < 1 || nz < 1 || nx > 2048 || ny > 2048 || nz > 2048)
+    return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "compute_lic_volume: dims");
+  DeviceGuard g(c->device);
+  Volume& v = it->second;
+  cudaStream_t s = c->stream;
+  RenderArgs a;
+  vvlic_status st = build_render_args(c, v, 1, 1, s, a);
+  if (st) return st;
+  const size_t count = (size_t)nx * ny * nz;
+  if (v.d_licvol && (size_t)v.ln[0] * v.ln[1] * v.ln[2] != count) {
+    cudaStreamSynchronize(s);
+    cudaFree(v.d_licvol);
+    v.d_licvol = nullptr;
+  }
+  if (!v.d_licvol) {
+    cudaError_t e = cudaMalloc(&v.d_licvol, count * sizeof(float));
+    if (e != cudaSuccess) return cuda_fail(c, e, "LIC volume allocation");
+  }
+  v.ln[0] = nx;
+  v.ln[1] = ny;
+  v.ln[2] = nz;
+  TechArgs t;
+  std::memset(&t, 0, sizeof t);
+  t.technique = VVLIC_TECHNIQUE_LICVOLUME;
+  t.licvol_out = v.d_licvol;
+  t.ln[0] = nx;
+  t.ln[1] = ny;
+  t.ln[2] = nz;
+  // lic3d_volume_fragment.glsl composes inc_lic without inc_illum: the uniform scaleVol is the
+  // volume's scale whatever the shading variant
+  for (int i = 0; i < 3; ++i) a.scale_vol[i] = v.geom.scale[i];
+  cudaError_t e = launch_technique(v.storage, a, t, c->params.sampler, c->params.integrator, false, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(c, e, "compute_lic_volume");
+  return VVLIC_OK;
+}
+
+extern "C" vvlic_status vvlic_download_lic_volume(vvlic_ctx* c, int32_t vol_id, float* out, uint64_t capacity) {
+  if (!c) return VVLIC_ERR_BAD_HANDLE;
+  auto it = c->vols.find(vol_id);
+  if (it == c->vols.end() || !it->second.d_licvol)
+    return fail(c, VVLIC_ERR_NOT_READY, "download_lic_volume: no LIC volume for volume %d", vol_id);
+  const size_t bytes = (size_t)it->second.ln[0] * it->second.ln[1] * it->second.ln[2] * sizeof(float);
+  if (!out || capacity < bytes) return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "download_lic_volume: need %zu bytes", bytes);
+  DeviceGuard g(c->device);
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e == cudaSuccess) e = cudaMemcpy(out, it->second.d_licvol, bytes, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(c, e, "download_lic_volume");
   return VVLIC_OK;
 }

@@ -55,6 +55,18 @@ struct RenderArgs {
 
 constexpr int kSegment = 32;  // adjoint checkpoint interval (samples)
 
+// Extra arguments of the non-raycast techniques (techniques.cuh).
+struct TechArgs {
+  int technique;
+  // slicing: unit plane normal (view direction, object space), volume centre, depth, count
+  float v[3], c[3], depth;
+  int nslices;
+  // LIC volume: ln[0]*ln[1]*ln[2] intensities, x fastest
+  const float* licvol;  // read by LICVOLUME renders
+  float* licvol_out;    // written by the precompute
+  int ln[3];
+};
+
 // ------------------------------------------------------------------------------------------
 // small vector helpers
 // ------------------------------------------------------------------------------------------

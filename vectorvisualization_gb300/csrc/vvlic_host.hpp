@@ -30,6 +30,8 @@ struct Volume {
   cudaArray_t array = nullptr;    // texture copy, built on first TEXTURE render
   cudaTextureObject_t tex = 0;
   size_t array_bytes = 0;
+  float* d_licvol = nullptr;      // precomputed LIC volume (vvlic_compute_lic_volume)
+  int ln[3] = {0, 0, 0};
 };
 
 struct NoiseTex {
@@ -149,4 +151,5 @@ struct JobFilter {
 vvlic_status build_render_args_ex(vvlic_ctx* c, Volume& v, int W, int H, cudaStream_t s, const vvlic_params& p,
                                   const vvlic_view& view, const JobFilter* filter, RenderArgs& a);
 void derive_rays(const vvlic_view& v, const Geometry& g, int W, int H, double* coeffs);
+void derive_slicing(const vvlic_view& v, const Geometry& g, float spacing, float vdir[3], float* depth, int* n);
 }  // namespace vvlic

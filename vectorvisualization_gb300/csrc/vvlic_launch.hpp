@@ -9,6 +9,17 @@
 namespace vvlic {
 
 struct RenderArgs;
+struct TechArgs;
+
+// Slicing, vector-field DVR, LIC-volume precompute and DVR (techniques_<storage>.cu).
+cudaError_t launch_technique_f32(const RenderArgs& a, const TechArgs& t, int sampler, int integ, bool grad,
+                                 cudaStream_t s);
+cudaError_t launch_technique_f16(const RenderArgs& a, const TechArgs& t, int sampler, int integ, bool grad,
+                                 cudaStream_t s);
+cudaError_t launch_technique_bf16(const RenderArgs& a, const TechArgs& t, int sampler, int integ, bool grad,
+                                  cudaStream_t s);
+cudaError_t launch_technique_u8(const RenderArgs& a, const TechArgs& t, int sampler, int integ, bool grad,
+                                cudaStream_t s);
 
 // Work distribution of one render launch: `order` == nullptr selects the static raster grid;
 // otherwise persistent CTAs pull `ntiles` 8x4 tiles in `order` through the counter `next`.
