@@ -226,6 +226,15 @@ const char* vvlic_last_error(const vvlic_ctx* ctx);
 vvlic_status vvlic_upload_field(vvlic_ctx* ctx, const void* xyz, int32_t dtype,
                                 int32_t nx, int32_t ny, int32_t nz, const float* slice_dist,
                                 int32_t storage, int32_t* vol_id);
+/* Time-dependent field: the encoding of the linear interpolation between two timesteps at
+ * t = interp_index / interp_size, as VectorDataSet::fillTexDataFloatInterp /
+ * fillTexDataCharInterp compute it (dataset.cpp:533-635, 724-823) for the idle-loop animation
+ * (3DLIC.cpp:129-171, checkInterpolateStage dataset.cpp:202-210).  Unlike the reference, which
+ * shifts its UCHAR3 buffers by -128 in place on every call, each call starts from the raw data. */
+vvlic_status vvlic_upload_field_interp(vvlic_ctx* ctx, const void* xyz0, const void* xyz1, int32_t dtype,
+                                       int32_t nx, int32_t ny, int32_t nz, const float* slice_dist,
+                                       int32_t storage, int32_t interp_index, int32_t interp_size,
+                                       int32_t* vol_id);
 /* Same from a device pointer (float32 xyz only), asynchronous on `stream`. */
 vvlic_status vvlic_upload_field_device(vvlic_ctx* ctx, const float* d_xyz,
                                        int32_t nx, int32_t ny, int32_t nz, const float* slice_dist,

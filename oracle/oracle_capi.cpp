@@ -38,6 +38,12 @@ void vvo_encode_field(const void* xyz, int32_t dtype, const int32_t n[3], float*
   vvo::encode_field(xyz, dtype, nn, out_rgba);
 }
 
+void vvo_encode_field_interp(const void* xyz0, const void* xyz1, int32_t dtype, const int32_t n[3], int32_t index,
+                             int32_t size, float* out_rgba) {
+  int nn[3] = {n[0], n[1], n[2]};
+  vvo::encode_field_interp(xyz0, xyz1, (float)index / (float)size, dtype, nn, out_rgba);
+}
+
 void vvo_round_storage(float* v, uint64_t count, int32_t storage) { vvo::round_storage(v, (size_t)count, storage); }
 
 void vvo_noise_gradients(const uint8_t* noise, const int32_t m[3], int32_t mode, const float* slice_dist,

@@ -59,6 +59,7 @@ def lib() -> C.CDLL:
         l = C.CDLL(LIB)
         P, I = C.c_void_p, C.c_int32
         l.vvo_encode_field.argtypes = [P, I, P, P]
+        l.vvo_encode_field_interp.argtypes = [P, P, I, P, I, I, P]
         l.vvo_round_storage.argtypes = [P, C.c_uint64, I]
         l.vvo_noise_gradients.argtypes = [P, P, I, P, P]
         l.vvo_noise_filter_weights.argtypes = [P]
@@ -90,6 +91,18 @@ def encode_field(xyz: np.ndarray) -> np.ndarray:
         a = a.astype(np.float32, copy=False)
     out = np.empty(a.shape[:3] + (4,), np.float32)
     lib().vvo_encode_field(a.ctypes.data, dtype, _dims(a).ctypes.data, out.ctypes.data)
+    return out
+
+
+def encode_field_interp(xyz0: np.ndarray, xyz1: np.ndarray, index: int, size: int) -> np.ndarray:
+    """Encoding of the time interpolation of two timesteps at t = index / size."""
+    a0, a1 = np.ascontiguousarray(xyz0), np.ascontiguousarray(xyz1)
+    dtype = capi.DTYPE_UINT8 if a0.dtype == np.uint8 else capi.DTYPE_FLOAT32
+    if dtype == capi.DTYPE_FLOAT32:
+        a0, a1 = a0.astype(np.float32, copy=False), a1.astype(np.float32, copy=False)
+    out = np.empty(a0.shape[:3] + (4,), np.float32)
+    lib().vvo_encode_field_interp(a0.ctypes.data, a1.ctypes.data, dtype, _dims(a0).ctypes.data, index, size,
+                                  out.ctypes.data)
     return out
 
 

@@ -98,11 +98,15 @@ static inline Geometry geometry(const int n[3], const float sd_in[3]) {
 }
 
 /* ------------------------------------------------------------------------------------- */
-/* field encoding: fillTexDataFloatInterp (dataset.cpp:533-635) with interpIndex = 0        */
+/* field encoding: fillTexDataFloatInterp (dataset.cpp:533-635).  `next` == NULL is          */
+/* interpIndex = 0 (the static upload); otherwise each component is the lerp                */
+/* data + t * (next - data), t = (float)interpIndex / InterpSize, evaluated in float as     */
+/* dataset.cpp:570 / :593 do, the UCHAR3 lerp truncated back to unsigned char.              */
 /* float arithmetic exactly as the reference performs it; compile with -ffp-contract=off.  */
 /* An all-zero field (maxLen = 0) gets magnitude 0 where the reference would divide 0/0.   */
 /* ------------------------------------------------------------------------------------- */
-static inline void encode_field(const void* xyz, int dtype, const int n[3], float* out_rgba) {
+static inline void encode_field_interp(const void* xyz, const void* next, float t, int dtype, const int n[3],
+                                       float* out_rgba) {
   const size_t count = (size_t)n[0] * n[1] * n[2];
   float max_len = -1.0f;
   for (size_t a = 0; a < count; ++a) {
@@ -111,17 +115,28 @@ static inline void encode_field(const void* xyz, int dtype, const int n[3], floa
     if (dtype == VVLIC_DTYPE_UINT8) {
       /* dataU -= 128 on unsigned char wraps modulo 256 (dataset.cpp:565-569) */
       const uint8_t* u = (const uint8_t*)xyz + 3 * a;
-      unsigned char t[3];
-      for (int c = 0; c < 3; ++c) t[c] = (unsigned char)(u[c] - 128);
-      len = std::sqrt((float)((int)t[0] * t[0]) + (float)((int)t[1] * t[1]) + (float)((int)t[2] * t[2]));
+      const uint8_t* w = next ? (const uint8_t*)next + 3 * a : nullptr;
+      unsigned char v[3];
+      for (int c = 0; c < 3; ++c) {
+        const unsigned char d = (unsigned char)(u[c] - 128);
+        if (!w) {
+          v[c] = d;
+        } else {
+          const unsigned char e = (unsigned char)(w[c] - 128);
+          v[c] = (unsigned char)((float)d + t * (float)((int)e - (int)d));
+        }
+      }
+      len = std::sqrt((float)((int)v[0] * v[0]) + (float)((int)v[1] * v[1]) + (float)((int)v[2] * v[2]));
       if (len < 1e-5f) {
         len = 0.0f;
         o[0] = o[1] = o[2] = 0.5f;
       } else {
-        for (int c = 0; c < 3; ++c) o[c] = 0.5f * (float)t[c] / len + 0.5f;
+        for (int c = 0; c < 3; ++c) o[c] = 0.5f * (float)v[c] / len + 0.5f;
       }
     } else {
-      const float* f = (const float*)xyz + 3 * a;
+      const float* f0 = (const float*)xyz + 3 * a;
+      float f[3];
+      for (int c = 0; c < 3; ++c) f[c] = next ? f0[c] + t * (((const float*)next)[3 * a + c] - f0[c]) : f0[c];
       len = std::sqrt(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]);
       if (len < 1e-5f) {
         len = 0.0f;
@@ -138,6 +153,9 @@ static inline void encode_field(const void* xyz, int dtype, const int n[3], floa
     float len = max_len > 0.0f ? o[3] / max_len : 0.0f;
     o[3] = (len > 1.0f) ? 1.0f : ((len < 0.0f) ? 0.0f : len);
   }
+}
+static inline void encode_field(const void* xyz, int dtype, const int n[3], float* out_rgba) {
+  encode_field_interp(xyz, nullptr, 0.0f, dtype, n, out_rgba);
 }
 
 /* Round-to-nearest-even to FP16 / BF16 and back, the storage emulation used to compare with

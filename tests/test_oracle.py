@@ -84,6 +84,30 @@ def test_encode_uint8_wraps_like_reference(oracle):
     assert abs(rgba[0, 0, 1, 3] - 127.0 / 128.0) < 1e-7
 
 
+def test_encode_interp_lerp_closed_form(oracle):
+    # t = index/size, each component data + t*(next - data) in float32 (dataset.cpp:593)
+    rng = np.random.default_rng(5)
+    a0 = rng.standard_normal((3, 4, 5, 3)).astype(np.float32)
+    a1 = rng.standard_normal((3, 4, 5, 3)).astype(np.float32)
+    for index, size in ((0, 1), (1, 3), (7, 8)):
+        t = np.float32(index) / np.float32(size)
+        lerp = a0 + t * (a1 - a0)
+        np.testing.assert_array_equal(oracle.encode_field_interp(a0, a1, index, size), oracle.encode_field(lerp))
+    np.testing.assert_array_equal(oracle.encode_field_interp(a0, a1, 0, 4), oracle.encode_field(a0))
+
+
+def test_encode_interp_uint8_truncates(oracle):
+    # bytes 130 and 135 are 2 and 7 after the -128 wrap; at t = 1/2: 2 + 0.5*5 = 4.5 -> 4 (byte 132)
+    a0 = np.full((1, 1, 2, 3), 128, np.uint8)
+    a1 = a0.copy()
+    a0[0, 0, 0, 0], a1[0, 0, 0, 0] = 130, 135
+    a0[0, 0, 1, 1], a1[0, 0, 1, 1] = 0, 255   # 128 and 127 (the wrap): 128 - 0.5 = 127.5 -> 127
+    want = a0.copy()
+    want[0, 0, 0, 0] = 132
+    want[0, 0, 1, 1] = 255
+    np.testing.assert_array_equal(oracle.encode_field_interp(a0, a1, 1, 2), oracle.encode_field(want))
+
+
 def test_storage_rounding_matches_numpy(oracle):
     x = np.concatenate([np.linspace(0, 1, 10001, dtype=np.float32), np.float32([1e-5, 6.1e-5, 3.3e-7, 0.999999])])
     np.testing.assert_array_equal(oracle.round_storage(x, "f16"), x.astype(np.float16).astype(np.float32))

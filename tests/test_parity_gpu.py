@@ -76,6 +76,36 @@ def test_field_encoding_uint8_bit_exact(ctx, oracle):
     np.testing.assert_array_equal(ctx.download_field(vid, (6, 5, 4), "f32"), oracle.encode_field(field))
 
 
+@pytest.mark.parametrize("storage", ["f32", "f16"])
+def test_field_interp_bit_exact(ctx, oracle, storage):
+    a0 = wl.vortex_field((24, 17, 9), seed=3)
+    a1 = wl.abc_field((24, 17, 9))
+    for index, size in ((0, 5), (3, 5), (47, 48)):
+        vid = ctx.upload_field_interp(a0, a1, index, size, storage=storage)
+        got = ctx.download_field(vid, (24, 17, 9), storage)
+        want = oracle.round_storage(oracle.encode_field_interp(a0, a1, index, size), storage)
+        np.testing.assert_array_equal(got, want)
+        ctx.free_volume(vid)
+
+
+def test_field_interp_uint8_bit_exact(ctx, oracle):
+    rng = wl.SplitMix64(78)
+    a0 = (rng.uniform(7 * 6 * 5 * 3) * 256).astype(np.uint8).reshape(5, 6, 7, 3)
+    a1 = (rng.uniform(7 * 6 * 5 * 3) * 256).astype(np.uint8).reshape(5, 6, 7, 3)
+    for index, size in ((1, 2), (2, 7)):
+        vid = ctx.upload_field_interp(a0, a1, index, size)
+        np.testing.assert_array_equal(ctx.download_field(vid, (7, 6, 5), "f32"),
+                                      oracle.encode_field_interp(a0, a1, index, size))
+        ctx.free_volume(vid)
+
+
+def test_field_interp_rejects_bad_index(ctx):
+    a0 = wl.abc_field((8, 8, 8))
+    for index, size in ((2, 2), (-1, 4), (0, 0)):
+        with pytest.raises(capi.VVLICError):
+            ctx.upload_field_interp(a0, a0, index, size)
+
+
 def test_field_encoding_zero_field(ctx, oracle):
     field = np.zeros((3, 4, 5, 3), np.float32)
     vid = ctx.upload_field(field)

@@ -128,6 +128,7 @@ _SIGS = {
     "vvlic_last_error": (C.c_char_p, [_P]),
     "vvlic_upload_field": (_I, [_P, _P, _I, _I, _I, _I, _P, _I, C.POINTER(_I)]),
     "vvlic_upload_field_device": (_I, [_P, _P, _I, _I, _I, _P, _I, _P, C.POINTER(_I)]),
+    "vvlic_upload_field_interp": (_I, [_P, _P, _P, _I, _I, _I, _I, _P, _I, _I, _I, C.POINTER(_I)]),
     "vvlic_free_volume": (_I, [_P, _I]),
     "vvlic_volume_bytes": (_I, [_P, _I, C.POINTER(C.c_uint64)]),
     "vvlic_upload_noise": (_I, [_P, _P, _I, _I, _I, _I]),
@@ -278,6 +279,23 @@ class Context:
             self._lib.vvlic_upload_field(self.h, a.ctypes.data, dtype, nx, ny, nz, _ptr(sd), STORAGE[storage], C.byref(vid)),
             "upload_field",
         )
+        return vid.value
+
+    def upload_field_interp(self, xyz0: np.ndarray, xyz1: np.ndarray, index: int, size: int, slice_dist=None,
+                            storage: str = "f32") -> int:
+        """Encode the time interpolation of two timesteps at index/size."""
+        a0, a1 = np.ascontiguousarray(xyz0), np.ascontiguousarray(xyz1)
+        if a0.shape != a1.shape or a0.dtype != a1.dtype or a0.ndim != 4:
+            raise ValueError("timesteps must have the same (nz, ny, nx, 3) shape and dtype")
+        dtype = DTYPE_UINT8 if a0.dtype == np.uint8 else DTYPE_FLOAT32
+        if dtype == DTYPE_FLOAT32:
+            a0, a1 = a0.astype(np.float32, copy=False), a1.astype(np.float32, copy=False)
+        nz, ny, nx = a0.shape[:3]
+        sd = None if slice_dist is None else np.asarray(slice_dist, np.float32)
+        vid = _I(0)
+        self._check(self._lib.vvlic_upload_field_interp(self.h, a0.ctypes.data, a1.ctypes.data, dtype, nx, ny, nz,
+                                                         _ptr(sd), STORAGE[storage], index, size, C.byref(vid)),
+                    "upload_field_interp")
         return vid.value
 
     def upload_field_device(self, d_xyz: int, dims, slice_dist=None, storage: str = "f32", stream: int = 0) -> int:

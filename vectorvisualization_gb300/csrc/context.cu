@@ -464,6 +464,41 @@ extern "C" vvlic_status vvlic_upload_field(vvlic_ctx* c, const void* xyz, int32_
   return VVLIC_OK;
 }
 
+extern "C" vvlic_status vvlic_upload_field_interp(vvlic_ctx* c, const void* xyz0, const void* xyz1, int32_t dtype,
+                                                 int32_t nx, int32_t ny, int32_t nz, const float* slice_dist,
+                                                 int32_t storage, int32_t interp_index, int32_t interp_size,
+                                                 int32_t* vol_id) {
+  if (!c) return VVLIC_ERR_BAD_HANDLE;
+  const int n[3] = {nx, ny, nz};
+  if (!xyz0 || !xyz1 || !vol_id || !valid_dims(n) || interp_size < 1 || interp_index < 0 ||
+      interp_index >= interp_size)
+    return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "upload_field_interp: bad arguments");
+  if (slice_dist)
+    for (int i = 0; i < 3; ++i)
+      if (!(slice_dist[i] > 0.0f)) return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "upload_field_interp: slice distance");
+  if (dtype != VVLIC_DTYPE_FLOAT32 && dtype != VVLIC_DTYPE_UINT8)
+    return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "upload_field_interp: dtype %d", dtype);
+  if (storage < VVLIC_STORAGE_F32 || storage > VVLIC_STORAGE_UNORM8)
+    return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "upload_field_interp: storage %d", storage);
+  DeviceGuard g(c->device);
+  const size_t bytes = (size_t)nx * ny * nz * 3 * (dtype == VVLIC_DTYPE_FLOAT32 ? 4 : 1);
+  const size_t slot = (bytes + 255) & ~(size_t)255;
+  vvlic_status st = grow(c, &c->d_upload, &c->upload_cap, 3 * slot);
+  if (st) return st;
+  char* base = (char*)c->d_upload;
+  cudaError_t e = cudaMemcpyAsync(base, xyz0, bytes, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(base + slot, xyz1, bytes, cudaMemcpyHostToDevice, c->stream);
+  // (float)interpIndex / InterpSize, as the reference computes it
+  const float t = (float)interp_index / (float)interp_size;
+  if (e == cudaSuccess) e = launch_interp_field(base, base + slot, dtype, n, t, base + 2 * slot, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "upload_field_interp");
+  st = encode_into_volume(c, base + 2 * slot, dtype, n, slice_dist, storage, c->stream, vol_id);
+  if (st) return st;
+  e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "upload_field_interp");
+  return VVLIC_OK;
+}
+
 extern "C" vvlic_status vvlic_upload_field_device(vvlic_ctx* c, const float* d_xyz, int32_t nx, int32_t ny, int32_t nz,
                                                  const float* slice_dist, int32_t storage, void* stream,
                                                  int32_t* vol_id) {

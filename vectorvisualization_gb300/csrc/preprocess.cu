@@ -245,6 +245,32 @@ inline int grid_for(size_t count) {
 
 }  // namespace
 
+namespace {
+// Time interpolation of fillTexData*Interp (dataset.cpp:555-585): t = interpIndex / InterpSize,
+// FLOAT3: data + t * (next - data); UCHAR3: the same on the 128-shifted bytes, stored back
+// un-shifted so the encoding's own shift recovers the interpolated value.
+__global__ void field_interp_kernel(const void* a0, const void* a1, int dtype, size_t count3, float t, void* out) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count3; i += (size_t)gridDim.x * blockDim.x) {
+    if (dtype == VVLIC_DTYPE_UINT8) {
+      const unsigned char d = (unsigned char)(reinterpret_cast<const uint8_t*>(a0)[i] - 128);
+      const unsigned char nx = (unsigned char)(reinterpret_cast<const uint8_t*>(a1)[i] - 128);
+      const unsigned char v = (unsigned char)((float)d + t * (float)((int)nx - (int)d));
+      reinterpret_cast<uint8_t*>(out)[i] = (uint8_t)(v + 128);
+    } else {
+      const float d = reinterpret_cast<const float*>(a0)[i], nx = reinterpret_cast<const float*>(a1)[i];
+      reinterpret_cast<float*>(out)[i] = d + t * (nx - d);
+    }
+  }
+}
+}  // namespace
+
+cudaError_t launch_interp_field(const void* d_a0, const void* d_a1, int dtype, const int n[3], float t, void* d_out,
+                                cudaStream_t s) {
+  const size_t count3 = (size_t)n[0] * n[1] * n[2] * 3;
+  field_interp_kernel<<<grid_for(count3), kThreads, 0, s>>>(d_a0, d_a1, dtype, count3, t, d_out);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_encode_field(const void* d_xyz, int dtype, const int n[3], int storage, void* d_texels,
                                 unsigned* d_maxbits, cudaStream_t s) {
   const size_t count = (size_t)n[0] * n[1] * n[2];
