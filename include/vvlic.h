@@ -104,13 +104,19 @@ enum { VVLIC_PERSPECTIVE = 0, VVLIC_ORTHOGRAPHIC = 1 };
  *                      position.
  *   GRAD_NOISE_NO_FREQ the gradient-noise fetch freqSamplingGrad ignores freqScale
  *                      (inc_lic.glsl:124-131).
+ *   ZOECKLER_LUMINANCE the Zoeckler table is a LUMINANCE_ALPHA texture (illumination.cpp:113,
+ *                      172), so illumZoeckler's `.rg` reads (L, L): the specular term adds
+ *                      0.9 * diffuse-table value and the stored specular alpha is never read
+ *                      (inc_illum.glsl:133-143).  Off: `.g` reads the stored specular.
  * VVLIC_QUIRKS_REFERENCE is what the reference actually computes. */
 enum {
   VVLIC_QUIRK_LUMINANCE_NOISE = 1u << 0,
   VVLIC_QUIRK_UNIFORM_SCALE_BUG = 1u << 1,
-  VVLIC_QUIRK_GRAD_NOISE_NO_FREQ = 1u << 2
+  VVLIC_QUIRK_GRAD_NOISE_NO_FREQ = 1u << 2,
+  VVLIC_QUIRK_ZOECKLER_LUMINANCE = 1u << 3
 };
-#define VVLIC_QUIRKS_REFERENCE (VVLIC_QUIRK_UNIFORM_SCALE_BUG | VVLIC_QUIRK_GRAD_NOISE_NO_FREQ)
+#define VVLIC_QUIRKS_REFERENCE \
+  (VVLIC_QUIRK_UNIFORM_SCALE_BUG | VVLIC_QUIRK_GRAD_NOISE_NO_FREQ | VVLIC_QUIRK_ZOECKLER_LUMINANCE)
 
 /* Render parameters.  The first block is the reference's LICParams (types.h:91-109, defaults in
  * its constructor); the rest are the shader #define variants and GL state the reference sets
@@ -280,6 +286,32 @@ vvlic_status vvlic_set_filter_taps(vvlic_ctx* ctx, const float* taps, int32_t st
 /* The taps the next render would use (count L_b+L_f+1) and the inverse filter area. */
 vvlic_status vvlic_get_filter_taps(const vvlic_ctx* ctx, float* taps, int32_t capacity,
                                    float* inv_filter_area);
+
+/* Illuminated-streamline material: LineMat (illumination.h:38-62) and the table size of
+ * Illumination (illumination.cpp:43, setTextureWidth/Height round up to a power of two).  Only
+ * channel 0 of light_color / ambient / diffuse / specular enters the Zoeckler table
+ * (illumination.cpp:155-160); the Mallo tables use all four. */
+typedef struct vvlic_line_material {
+  float light_color[4]; /* (1,1,1,1) */
+  float ambient[4];     /* (0.1, ...) */
+  float diffuse[4];     /* (0.5, ...) */
+  float specular[4];    /* (0.8, ...) */
+  float spec_exp;       /* 40 */
+  float diff_exp;       /* 2 */
+  int32_t width;        /* table width (256) */
+  int32_t height;       /* table height (256) */
+} vvlic_line_material;
+void vvlic_line_material_default(vvlic_line_material* mat);
+/* Rebuilds the Zoeckler and Mallo tables of Illumination::createIllumTextures
+ * (illumination.cpp:58-90, 96-200, 205-290, 355-391).  The reference passes floatTex to neither
+ * builder, so all three are 8-bit textures: each float is stored as round(255 * value).  The
+ * initial material is the default; tables are built on first use. */
+vvlic_status vvlic_set_line_material(vvlic_ctx* ctx, const vvlic_line_material* mat);
+/* The three tables as the shaders sample them, RGBA8 rows of `width` texels, x fastest:
+ * Zoeckler as LUMINANCE_ALPHA reads (L, L, L, A) with L = diffuse and A = 0.9 * specular;
+ * Mallo diffuse and specular RGBA.  Any pointer may be NULL; width/height are always written. */
+vvlic_status vvlic_get_illum_luts(vvlic_ctx* ctx, uint8_t* zoeckler, uint8_t* mallo_diffuse,
+                                  uint8_t* mallo_specular, int32_t* width, int32_t* height);
 
 /* LICParams + shader variant: Renderer::setLICParams + setRenderVolParams (renderer.cpp:925-996)
  * + the define injection of GLSLShader::loadShader (GLSLShader.cpp:120-136). */

@@ -131,6 +131,13 @@ class Renderer {
     std::memcpy(params_.light_pos, pos, sizeof(float) * 3);
     check(vvlic_set_params(ctx_, &params_), "setLight");
   }
+  /* Illumination::setMaterial + createIllumTextures, and the spot exponent the reference copies
+   * into GL_LIGHT0 (3DLIC.cpp:735-736); the renderer's setIllum*Tex bindings are implicit. */
+  void setLineMaterial(const vvlic_line_material& m) {
+    check(vvlic_set_line_material(ctx_, &m), "setLineMaterial");
+    params_.spec_exp = m.spec_exp;
+    check(vvlic_set_params(ctx_, &params_), "setLineMaterial");
+  }
   void setLowRes(bool lowRes) {
     params_.low_res = lowRes ? 1 : 0;
     check(vvlic_set_params(ctx_, &params_), "setLowRes");

@@ -29,6 +29,8 @@ typedef struct vvo_inputs {
   double inv_filter_area;      /* used with explicit taps */
   const float* licvol;         /* LIC volume for the LICVOLUME technique, or NULL */
   int32_t ln[3];
+  const uint8_t* luts;         /* line-illumination tables (vvo_illum_luts) or NULL */
+  int32_t lut_w, lut_h;
 } vvo_inputs;
 
 int32_t vvo_abi(void) { return 1; }
@@ -42,6 +44,11 @@ void vvo_encode_field_interp(const void* xyz0, const void* xyz1, int32_t dtype, 
                              int32_t size, float* out_rgba) {
   int nn[3] = {n[0], n[1], n[2]};
   vvo::encode_field_interp(xyz0, xyz1, (float)index / (float)size, dtype, nn, out_rgba);
+}
+
+/* The Zoeckler and Mallo tables for `mat` at w x h: 3 * w * h * 4 bytes. */
+void vvo_illum_luts(const vvlic_line_material* mat, int32_t w, int32_t h, uint8_t* out) {
+  vvo::illum_luts(*mat, w, h, out);
 }
 
 void vvo_round_storage(float* v, uint64_t count, int32_t storage) { vvo::round_storage(v, (size_t)count, storage); }
@@ -125,7 +132,11 @@ int32_t vvo_render(const vvo_inputs* vi, const vvlic_params* p, const double* ra
   in.inv_filter_area = inv_area;
   in.licvol = vi->licvol;
   for (int i = 0; i < 3; ++i) in.ln[i] = vi->ln[i];
+  in.luts = vi->luts;
+  in.lut_w = vi->lut_w;
+  in.lut_h = vi->lut_h;
   if (p->technique == VVLIC_TECHNIQUE_LICVOLUME && !in.licvol) return -3;
+  if ((p->illum == VVLIC_ILLUM_ZOECKLER || p->illum == VVLIC_ILLUM_MALLO) && !in.luts) return -5;
   double slicing[5] = {0, 0, 0, 0, 0};
   if (p->technique == VVLIC_TECHNIQUE_SLICING) {
     if (!view) return -4;

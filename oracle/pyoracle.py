@@ -39,6 +39,9 @@ class Inputs(C.Structure):
         ("inv_filter_area", C.c_double),
         ("licvol", C.c_void_p),
         ("ln", C.c_int32 * 3),
+        ("luts", C.c_void_p),
+        ("lut_w", C.c_int32),
+        ("lut_h", C.c_int32),
     ]
 
 
@@ -61,6 +64,7 @@ def lib() -> C.CDLL:
         l.vvo_encode_field.argtypes = [P, I, P, P]
         l.vvo_encode_field_interp.argtypes = [P, P, I, P, I, I, P]
         l.vvo_round_storage.argtypes = [P, C.c_uint64, I]
+        l.vvo_illum_luts.argtypes = [P, I, I, P]
         l.vvo_noise_gradients.argtypes = [P, P, I, P, P]
         l.vvo_noise_filter_weights.argtypes = [P]
         l.vvo_filter_inv_area.argtypes = [P, I, I]
@@ -103,6 +107,15 @@ def encode_field_interp(xyz0: np.ndarray, xyz1: np.ndarray, index: int, size: in
     out = np.empty(a0.shape[:3] + (4,), np.float32)
     lib().vvo_encode_field_interp(a0.ctypes.data, a1.ctypes.data, dtype, _dims(a0).ctypes.data, index, size,
                                   out.ctypes.data)
+    return out
+
+
+def illum_luts(material: "capi.LineMaterial | None" = None) -> np.ndarray:
+    """Zoeckler, Mallo diffuse and Mallo specular tables, (3, h, w, 4) uint8."""
+    m = material if material is not None else capi.line_material_default()
+    w, h = capi.lut_size(m.width), capi.lut_size(m.height)
+    out = np.empty((3, h, w, 4), np.uint8)
+    lib().vvo_illum_luts(C.byref(m), w, h, out.ctypes.data)
     return out
 
 
@@ -204,6 +217,8 @@ class Scene:
     def render(self, params: capi.Params, view: capi.View, w: int, h: int, rows=None, precision: int = 64,
                threads: int = 0):
         """Returns (image (nrows, w, 4) float32, samples (nrows, w) uint32)."""
+        if params.illum in (capi.ILLUM_ZOECKLER, capi.ILLUM_MALLO) and not self.inputs.luts:
+            self.attach_line_material()
         rc = view_rays(view, self.dims, w, h, list(self.inputs.slice_dist))
         r = None if rows is None else np.ascontiguousarray(rows, dtype=np.int32)
         nr = h if r is None else r.size
@@ -224,6 +239,13 @@ class Scene:
         if st != 0:
             raise RuntimeError(f"oracle LIC volume failed ({st})")
         return out
+
+    def attach_line_material(self, material: "capi.LineMaterial | None" = None):
+        """Line-illumination tables for ZOECKLER / MALLO renders (default material if None)."""
+        self._luts = illum_luts(material)
+        self.inputs.luts = self._luts.ctypes.data
+        self.inputs.lut_w = self._luts.shape[2]
+        self.inputs.lut_h = self._luts.shape[1]
 
     def attach_lic_volume(self, licvol: np.ndarray):
         self._licvol = np.ascontiguousarray(licvol, dtype=np.float32)

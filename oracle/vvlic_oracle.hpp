@@ -374,7 +374,103 @@ struct Inputs {
   double inv_filter_area;
   const float* licvol = nullptr; /* LIC volume (LICVOLUME technique), ln[0]*ln[1]*ln[2] */
   int ln[3] = {0, 0, 0};
+  /* line-illumination tables (ZOECKLER / MALLO): Zoeckler, Mallo diffuse, Mallo specular,
+   * lut_w*lut_h RGBA8 each, from illum_luts() */
+  const uint8_t* luts = nullptr;
+  int lut_w = 0, lut_h = 0;
 };
+
+/* ------------------------------------------------------------------------------------- */
+/* line-illumination tables: Illumination::createIllumTexZoeckler (illumination.cpp:96-200)  */
+/* and createIllumTexMallo (:205-330, Simpson rule :355-391), in double in the reference's  */
+/* order, stored as the 8-bit textures the reference uploads (createIllumTextures passes   */
+/* floatTex to neither builder): round(clamp(v) * 255).                                     */
+/* ------------------------------------------------------------------------------------- */
+static inline uint8_t gl_unorm8(float v) {
+  double c = v;
+  if (!(c > 0.0)) c = 0.0;
+  if (c > 1.0) c = 1.0;
+  return (uint8_t)std::floor(c * 255.0 + 0.5);
+}
+
+static inline double mallo_f(double beta, double n, double theta) {
+  double y = std::cos(theta - beta);
+  if (y < 0.0) y = 0.0;
+  return std::pow(y, n) * (std::cos(theta) / 2.0);
+}
+
+static inline double mallo_simpson(double alpha, double beta, double n) {
+  const double pi = 3.14159265358979323846;
+  double a = alpha - pi / 2.0, b = pi / 2.0;
+  int m = 10;
+  double h = (b - a) / (2.0 * m), sum = 0.0;
+  for (int i = 0; i < 2 * m; i += 2) {
+    sum += 2.0 * mallo_f(beta, n, a + i * h);
+    sum += 4.0 * mallo_f(beta, n, a + (i + 1) * h);
+  }
+  sum += mallo_f(beta, n, b);
+  sum -= mallo_f(beta, n, a); /* f(a) entered twice above */
+  return sum * (h / 3.0);
+}
+
+/* out: 3 tables of w*h RGBA8 (Zoeckler as LUMINANCE_ALPHA samples it: L, L, L, A). */
+static inline void illum_luts(const vvlic_line_material& m, int w, int h, uint8_t* out) {
+  const double pi = 3.14159265358979323846;
+  double ix = 1.0 / (double)(w - 1), iy = 1.0 / (double)(h - 1);
+  for (int y = 0; y < h; ++y)
+    for (int x = 0; x < w; ++x) {
+      double lt = 2.0 * ((double)x * ix) - 1.0, vt = 2.0 * ((double)y * iy) - 1.0;
+      double diffuse = std::pow(std::sqrt(1.0 - lt * lt), (double)m.diff_exp);
+      double dp = lt * vt - std::sqrt(1.0 - lt * lt) * std::sqrt(1.0 - vt * vt);
+      if (dp < -1.0) dp = -1.0;
+      if (dp > 1.0) dp = 1.0;
+      double td = m.ambient[0] * m.light_color[0] + diffuse * m.diffuse[0] * m.light_color[0];
+      double ts = std::pow(std::fabs(dp), (double)m.spec_exp) * m.specular[0] * m.light_color[0];
+      td *= 0.5;
+      td = td < 0.0 ? 0.0 : (td > 1.0 ? 1.0 : td);
+      ts *= 0.5;
+      ts = ts < 0.0 ? 0.0 : (ts > 1.0 ? 1.0 : ts);
+      uint8_t* o = out + 4 * ((size_t)y * w + x);
+      o[0] = o[1] = o[2] = gl_unorm8((float)td);
+      o[3] = gl_unorm8((float)ts * 0.9f);
+    }
+  uint8_t* dt = out + (size_t)4 * w * h;
+  uint8_t* st = out + (size_t)8 * w * h;
+  for (int y = 0; y < h; ++y)
+    for (int x = 0; x < w; ++x) {
+      double s = ((double)x + 0.5) / w, t = ((double)y + 0.5) / h;
+      double alpha = std::acos(2.0 * s - 1.0), beta = std::acos(2.0 * t - 1.0), lt = 2.0 * t - 1.0;
+      double diffuse = std::sqrt(1.0 - lt * lt) * (std::sin(alpha) + (pi - alpha) * std::cos(alpha)) * 0.25;
+      double specular = 3.5 * mallo_simpson(alpha, beta, m.spec_exp);
+      for (int i = 0; i < 4; ++i) {
+        size_t o = 4 * ((size_t)y * w + x) + i;
+        double c = diffuse * m.diffuse[i] * m.light_color[i];
+        dt[o] = gl_unorm8((float)(c < 0.0 ? 0.0 : (c > 1.0 ? 1.0 : c)));
+        c = specular * m.specular[i] * m.light_color[i];
+        st[o] = gl_unorm8((float)(c < 0.0 ? 0.0 : (c > 1.0 ? 1.0 : c)));
+      }
+    }
+}
+
+/* texture2D(table, (s, r)) with LINEAR + CLAMP_TO_EDGE on an RGBA8 table; a NaN coordinate
+ * (degenerate tangent) is taken as 0. */
+template <class R> static inline V4<R> tex2d_lut(const uint8_t* t, int w, int h, R s, R r) {
+  s = std::fmin(std::fmax(s, R(0)), R(1));
+  r = std::fmin(std::fmax(r, R(0)), R(1));
+  R u = s * R(w) - R(0.5), v = r * R(h) - R(0.5);
+  R fu = std::floor(u), fv = std::floor(v);
+  R au = u - fu, av = v - fv;
+  int x0 = std::max((int)fu, 0), x1 = std::min((int)fu + 1, w - 1);
+  int y0 = std::max((int)fv, 0), y1 = std::min((int)fv + 1, h - 1);
+  R c[4];
+  for (int k = 0; k < 4; ++k) {
+    R t00 = R(t[4 * ((size_t)y0 * w + x0) + k]), t10 = R(t[4 * ((size_t)y0 * w + x1) + k]);
+    R t01 = R(t[4 * ((size_t)y1 * w + x0) + k]), t11 = R(t[4 * ((size_t)y1 * w + x1) + k]);
+    c[k] = ((R(1) - au) * (R(1) - av) * t00 + au * (R(1) - av) * t10 + (R(1) - au) * av * t01 + au * av * t11) /
+           R(255);
+  }
+  return V4<R>{c[0], c[1], c[2], c[3]};
+}
 
 /* LINEAR + CLAMP_TO_EDGE trilinear at texture coordinate s (GL 2.1 eq. 3.23/3.27). */
 template <class R> static inline V4<R> tex3d_field(const Inputs& in, V3<R> s) {
@@ -676,12 +772,50 @@ template <class R> static inline R alpha_correct(R a, R corr) {
   return R(1) - std::pow(base, corr);
 }
 
-template <class R> static inline V4<R> shade(const LicCtx<R>& c, V4<R> illum, V4<R> tf, V3<R> pos, V3<R> dir) {
+template <class R> static inline V3<R> cross(V3<R> a, V3<R> b) {
+  return V3<R>{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+/* clamp to [0, 1] with NaN -> 0 */
+template <class R> static inline R sat_nan0(R v) { return std::fmin(std::fmax(v, R(0)), R(1)); }
+
+/* f = vectorData at pos; its encoded rgb is the tangent of illumZoeckler / illumMallo. */
+template <class R>
+static inline V4<R> shade(const LicCtx<R>& c, V4<R> illum, V4<R> tf, V3<R> pos, V3<R> dir, V4<R> f) {
   const Uniforms<R>& u = *c.u;
   const vvlic_params& p = *c.p;
   V4<R> col;
   R I = illum.w;
-  if (p.illum == VVLIC_ILLUM_GRADIENT) {
+  if (p.illum == VVLIC_ILLUM_ZOECKLER || p.illum == VVLIC_ILLUM_MALLO) {
+    const Inputs& in = *c.in;
+    V3<R> lp{R(p.light_pos[0]), R(p.light_pos[1]), R(p.light_pos[2])};
+    V3<R> sv{u.scale_vol_inv[0], u.scale_vol_inv[1], u.scale_vol_inv[2]};
+    V3<R> L = normalize(lp - mul(pos, sv));
+    V3<R> T = normalize(V3<R>{R(2) * f.x - R(1), R(2) * f.y - R(1), R(2) * f.z - R(1)});
+    if (p.illum == VVLIC_ILLUM_ZOECKLER) { /* inc_illum.glsl:117-154 */
+      V3<R> V = normalize(dir);
+      V4<R> sh = tex2d_lut<R>(in.luts, in.lut_w, in.lut_h, R(0.5) * dot(L, T) + R(0.5), R(0.5) * dot(V, T) + R(0.5));
+      R d = sh.x * u.illum_scale;
+      R g = (p.quirks & VVLIC_QUIRK_ZOECKLER_LUMINANCE) ? sh.y : sh.w;
+      col.x = tf.x * I * d + R(0.9) * g;
+      col.y = tf.y * I * d + R(0.9) * g;
+      col.z = tf.z * I * d + R(0.9) * g;
+    } else { /* inc_illum.glsl:46-112 */
+      V3<R> V = normalize(dir * R(-1));
+      V3<R> B = normalize(cross(T, V));
+      V3<R> N = cross(B, T);
+      V3<R> H = normalize(V + L);
+      R lx = dot(L, N), ly = dot(L, T), lz = dot(H, N), lw = dot(H, T);
+      R tx = R(1) / std::sqrt(R(1) - ly * ly), ty = R(1) / std::sqrt(R(1) - lw * lw);
+      R cz = R(0.5) * (lx * tx) + R(0.5), cy = R(0.5) * ly + R(0.5), cw = R(0.5) * (lz * ty) + R(0.5);
+      size_t one = (size_t)4 * in.lut_w * in.lut_h;
+      V4<R> df = tex2d_lut<R>(in.luts + one, in.lut_w, in.lut_h, cz, cy);
+      V4<R> sp = tex2d_lut<R>(in.luts + 2 * one, in.lut_w, in.lut_h, cz, cw);
+      R att = std::pow(ty, -R(p.spec_exp));
+      col.x = tf.x * I * (df.x * u.illum_scale) + sat_nan0(sp.x * att);
+      col.y = tf.y * I * (df.y * u.illum_scale) + sat_nan0(sp.y * att);
+      col.z = tf.z * I * (df.z * u.illum_scale) + sat_nan0(sp.z * att);
+    }
+  } else if (p.illum == VVLIC_ILLUM_GRADIENT) {
     V3<R> lp{R(p.light_pos[0]), R(p.light_pos[1]), R(p.light_pos[2])};
     V3<R> sv{u.scale_vol_inv[0], u.scale_vol_inv[1], u.scale_vol_inv[2]};
     V3<R> L = normalize(lp - mul(pos, sv));
@@ -812,7 +946,7 @@ template <class R> static inline uint32_t slice_pixel(const Inputs& in, const vv
     V4<R> il = compute_lic<R>(c, pos, f);
     ++samples;
     il.w *= u.intensity_scale;
-    V4<R> src = shade<R>(c, il, tf, pos, dir);
+    V4<R> src = shade<R>(c, il, tf, pos, dir, f);
     src.x *= src.w;
     src.y *= src.w;
     src.z *= src.w;
@@ -867,7 +1001,7 @@ template <class R> static inline uint32_t render_pixel(const Inputs& in, const v
           V4<R> tf{tex1d<R>(in.tf_rgba, 4, 0, idx), tex1d<R>(in.tf_rgba, 4, 1, idx), tex1d<R>(in.tf_rgba, 4, 2, idx),
                    tex1d<R>(in.tf_rgba, 4, 3, idx)};
           V4<R> il{R(0), R(0), R(0), tex3d_licvol<R>(in, pos)};
-          src = shade<R>(cq, il, tf, pos, dir);
+          src = shade<R>(cq, il, tf, pos, dir, f);
         } else {
           src = V4<R>{f.x, f.y, f.z, tex1d<R>(in.tf_rgba, 4, 3, f.w)};
         }
@@ -899,7 +1033,7 @@ template <class R> static inline uint32_t render_pixel(const Inputs& in, const v
       V4<R> il = compute_lic<R>(c, pos, f);
       ++samples;
       il.w *= u.intensity_scale;
-      src = shade<R>(c, il, tf, pos, dir);
+      src = shade<R>(c, il, tf, pos, dir, f);
       src.x *= src.w;
       src.y *= src.w;
       src.z *= src.w;

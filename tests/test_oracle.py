@@ -108,6 +108,64 @@ def test_encode_interp_uint8_truncates(oracle):
     np.testing.assert_array_equal(oracle.encode_field_interp(a0, a1, 1, 2), oracle.encode_field(want))
 
 
+def _unorm8(v):
+    return np.floor(np.clip(np.asarray(v, np.float32).astype(np.float64), 0, 1) * 255 + 0.5).astype(np.int64)
+
+
+def test_zoeckler_table_matches_numpy_restatement(oracle):
+    # illumination.cpp:96-172 with the default LineMat, vectorised in numpy (float64 throughout,
+    # ambient*lightColor and the 0.9 factor in float32 as in the reference)
+    luts = oracle.illum_luts()
+    assert luts.shape == (3, 256, 256, 4)
+    x = np.arange(256)
+    lt = 2.0 * (x * (1.0 / 255)) - 1.0
+    LT, VT = np.meshgrid(lt, lt)
+    diff = np.sqrt(1 - LT * LT) ** 2.0
+    dp = np.clip(LT * VT - np.sqrt(1 - LT * LT) * np.sqrt(1 - VT * VT), -1, 1)
+    td = np.clip((float(np.float32(0.1)) + diff * float(np.float32(0.5))) * 0.5, 0, 1)
+    ts = np.clip(np.abs(dp) ** 40.0 * float(np.float32(0.8)) * 0.5, 0, 1)
+    z = luts[0].astype(np.int64)
+    assert np.abs(z[..., 0] - _unorm8(td)).max() <= 1
+    assert np.abs(z[..., 3] - _unorm8(ts.astype(np.float32) * np.float32(0.9))).max() <= 1
+    np.testing.assert_array_equal(z[..., 0], z[..., 1])  # LUMINANCE_ALPHA reads (L, L, L, A)
+    # lt = +-1: no diffuse term, only ambient 0.1 halved -> round(12.75) = 13
+    assert (z[:, 0, 0] == 13).all() and (z[:, 255, 0] == 13).all()
+
+
+def test_mallo_tables_match_numpy_restatement(oracle):
+    luts = oracle.illum_luts()
+    s = (np.arange(256) + 0.5) / 256
+    alpha = np.arccos(2 * s - 1)[None, :]
+    beta = np.arccos(2 * s - 1)[:, None]
+    lt = (2 * s - 1)[:, None]
+    fd = np.sqrt(1 - lt * lt) * (np.sin(alpha) + (np.pi - alpha) * np.cos(alpha)) * 0.25
+    # Simpson, 20 intervals over [alpha - pi/2, pi/2] of max(0, cos(th - beta))^40 cos(th) / 2
+    a = alpha - np.pi / 2
+    hstep = (np.pi / 2 - a) / 20
+    f = lambda th: np.maximum(np.cos(th - beta), 0) ** 40.0 * (np.cos(th) / 2)
+    acc = sum((2.0 if i % 2 == 0 else 4.0) * f(a + i * hstep) for i in range(20)) + f(a + 20 * hstep) - f(a)
+    fs = 3.5 * acc * (hstep / 3)
+    md, ms = luts[1].astype(np.int64), luts[2].astype(np.int64)
+    for c in range(4):
+        assert np.abs(md[..., c] - _unorm8(np.clip(fd * float(np.float32(0.5)), 0, 1))).max() <= 1
+        assert np.abs(ms[..., c] - _unorm8(np.clip(fs * float(np.float32(0.8)), 0, 1))).max() <= 1
+    # the Simpson sum approximates the exact integral (a smooth check on the specular table)
+    from scipy.integrate import quad
+
+    for i, j in [(40, 200), (128, 128), (220, 60)]:
+        al, be = float(alpha[0, i]), float(beta[j, 0])
+        exact, _ = quad(lambda th: max(np.cos(th - be), 0) ** 40 * np.cos(th) / 2, al - np.pi / 2, np.pi / 2)
+        assert abs(fs[j, i] / 3.5 - exact) <= 0.02 * max(exact, 1e-3) + 1e-4
+
+
+def test_line_material_size_rounds_to_power_of_two(oracle):
+    from vectorvisualization_gb300 import capi
+
+    m = capi.line_material_default()
+    m.width, m.height = 100, 60
+    assert oracle.illum_luts(m).shape == (3, 64, 128, 4)
+
+
 def test_storage_rounding_matches_numpy(oracle):
     x = np.concatenate([np.linspace(0, 1, 10001, dtype=np.float32), np.float32([1e-5, 6.1e-5, 3.3e-7, 0.999999])])
     np.testing.assert_array_equal(oracle.round_storage(x, "f16"), x.astype(np.float16).astype(np.float32))

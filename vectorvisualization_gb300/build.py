@@ -27,7 +27,7 @@ BUILD_DIR = os.path.join(ROOT, "_build", "vvlic")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
 # Files whose float arithmetic must round like the reference's CPU code.
-NO_FMA = {"preprocess.cu", "noalloc.cu"}
+NO_FMA = {"preprocess.cu", "noalloc.cu", "illum.cu"}
 
 
 def _nvcc() -> str:
@@ -71,7 +71,7 @@ def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -
         obj = os.path.join(BUILD_DIR, src.replace(".cu", ".o"))
         cmd = [nvcc, *ARCH, *COMMON, *extra, "-I", INCLUDE, "-c", os.path.join(CSRC, src), "-o", obj]
         if src in NO_FMA:
-            cmd.insert(1, "-fmad=false")
+            cmd[1:1] = ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]
         if verbose:
             print(" ".join(cmd), flush=True)
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -31,8 +31,8 @@ TF_INDEX_DIR_Z, TF_INDEX_MAGNITUDE = 0, 1
 KERNEL_CLAMP_BORDER, KERNEL_CLAMP_EDGE = 0, 1
 FILTER = {"box": 0, "triangle": 1, "cos2": 2, "gaussian": 3}
 PERSPECTIVE, ORTHOGRAPHIC = 0, 1
-QUIRK_LUMINANCE_NOISE, QUIRK_UNIFORM_SCALE_BUG, QUIRK_GRAD_NOISE_NO_FREQ = 1, 2, 4
-QUIRKS_REFERENCE = QUIRK_UNIFORM_SCALE_BUG | QUIRK_GRAD_NOISE_NO_FREQ
+QUIRK_LUMINANCE_NOISE, QUIRK_UNIFORM_SCALE_BUG, QUIRK_GRAD_NOISE_NO_FREQ, QUIRK_ZOECKLER_LUMINANCE = 1, 2, 4, 8
+QUIRKS_REFERENCE = QUIRK_UNIFORM_SCALE_BUG | QUIRK_GRAD_NOISE_NO_FREQ | QUIRK_ZOECKLER_LUMINANCE
 
 _f3 = C.c_float * 3
 
@@ -106,6 +106,19 @@ class Job(C.Structure):
     ]
 
 
+class LineMaterial(C.Structure):
+    _fields_ = [
+        ("light_color", C.c_float * 4),
+        ("ambient", C.c_float * 4),
+        ("diffuse", C.c_float * 4),
+        ("specular", C.c_float * 4),
+        ("spec_exp", C.c_float),
+        ("diff_exp", C.c_float),
+        ("width", C.c_int32),
+        ("height", C.c_int32),
+    ]
+
+
 class Stats(C.Structure):
     _fields_ = [
         ("samples", C.c_uint64),
@@ -123,6 +136,9 @@ _SIGS = {
     "vvlic_status_string": (C.c_char_p, [_I]),
     "vvlic_abi_version": (_I, []),
     "vvlic_make_filter_table": (_I, [_I, _I, _P, C.POINTER(_I)]),
+    "vvlic_line_material_default": (None, [C.POINTER(LineMaterial)]),
+    "vvlic_set_line_material": (_I, [_P, C.POINTER(LineMaterial)]),
+    "vvlic_get_illum_luts": (_I, [_P, _P, _P, _P, C.POINTER(_I), C.POINTER(_I)]),
     "vvlic_create": (_I, [C.POINTER(_P), _I]),
     "vvlic_destroy": (_I, [_P]),
     "vvlic_last_error": (C.c_char_p, [_P]),
@@ -196,6 +212,20 @@ def view_default() -> View:
     v = View()
     load().vvlic_view_default(C.byref(v))
     return v
+
+
+def line_material_default() -> LineMaterial:
+    m = LineMaterial()
+    load().vvlic_line_material_default(C.byref(m))
+    return m
+
+
+def lut_size(v: int) -> int:
+    """Table size the library uses for a requested width/height (next power of two)."""
+    p = 1
+    while p < v:
+        p <<= 1
+    return p
 
 
 def make_filter_table(kind: str | int, width: int = 256) -> np.ndarray:
@@ -355,6 +385,18 @@ class Context:
         r = None if rgba is None else np.ascontiguousarray(rgba, dtype=np.float32).reshape(TF_ENTRIES * 4)
         o = None if opacity is None else np.ascontiguousarray(opacity, dtype=np.float32).reshape(TF_ENTRIES)
         self._check(self._lib.vvlic_set_tf(self.h, _ptr(r), _ptr(o)), "set_tf")
+
+    def set_line_material(self, material: LineMaterial):
+        self._check(self._lib.vvlic_set_line_material(self.h, C.byref(material)), "set_line_material")
+
+    def illum_luts(self) -> np.ndarray:
+        """Zoeckler, Mallo diffuse and Mallo specular tables as sampled, (3, h, w, 4) uint8."""
+        w, h = _I(0), _I(0)
+        self._check(self._lib.vvlic_get_illum_luts(self.h, None, None, None, C.byref(w), C.byref(h)), "illum_luts")
+        out = np.empty((3, h.value, w.value, 4), np.uint8)
+        self._check(self._lib.vvlic_get_illum_luts(self.h, out[0].ctypes.data, out[1].ctypes.data,
+                                                    out[2].ctypes.data, None, None), "illum_luts")
+        return out
 
     def set_filter_table(self, table: np.ndarray, clamp: int = KERNEL_CLAMP_BORDER):
         t = np.ascontiguousarray(table, dtype=np.uint8)

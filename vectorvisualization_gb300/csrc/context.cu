@@ -333,6 +333,7 @@ extern "C" vvlic_status vvlic_create(vvlic_ctx** out, int32_t device) {
   c->device = device;
   vvlic_params_default(&c->params);
   vvlic_view_default(&c->view);
+  vvlic_line_material_default(&c->line_mat);
   default_tables(c);
   DeviceGuard g(device);
   if ((e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess ||
@@ -374,6 +375,7 @@ extern "C" vvlic_status vvlic_destroy(vvlic_ctx* c) {
   free_noise(c->noise);
   if (c->d_scalar) cudaFree(c->d_scalar);
   if (c->d_tf) cudaFree(c->d_tf);
+  if (c->d_luts) cudaFree(c->d_luts);
   if (c->d_counters) cudaFree(c->d_counters);
   if (c->d_scratch_word) cudaFree(c->d_scratch_word);
   if (c->d_image) cudaFree(c->d_image);
@@ -684,8 +686,6 @@ static vvlic_status check_params(vvlic_ctx* c, const vvlic_params& p) {
     return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "params: integrator %d", p.integrator);
   if (p.illum < VVLIC_ILLUM_NONE || p.illum > VVLIC_ILLUM_MALLO)
     return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "params: illum %d", p.illum);
-  if (p.illum == VVLIC_ILLUM_ZOECKLER || p.illum == VVLIC_ILLUM_MALLO)
-    return fail(c, VVLIC_ERR_UNSUPPORTED, "params: illumination model %d not built", p.illum);
   if (p.tf_index != VVLIC_TF_INDEX_DIR_Z && p.tf_index != VVLIC_TF_INDEX_MAGNITUDE)
     return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "params: tf_index %d", p.tf_index);
   if (p.sampler < VVLIC_SAMPLER_GATHER || p.sampler > VVLIC_SAMPLER_HYBRID)

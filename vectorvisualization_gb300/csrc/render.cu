@@ -207,6 +207,12 @@ vvlic_status build_render_args_ex(vvlic_ctx* c, Volume& v, int W, int H, cudaStr
     a.light_spec[i] = p.light_specular[i];
     a.light_amb[i] = p.light_ambient[i];
   }
+  if (p.illum == VVLIC_ILLUM_ZOECKLER || p.illum == VVLIC_ILLUM_MALLO) {
+    if ((st = ensure_illum_luts(c)) != VVLIC_OK) return st;
+    a.luts = (const uchar4*)c->d_luts;
+    a.lut_w = c->lut_w;
+    a.lut_h = c->lut_h;
+  }
   a.counters = c->d_counters;
   return VVLIC_OK;
 }

@@ -61,7 +61,7 @@ __device__ __forceinline__ float4 slice_pixel(const RenderArgs& a, const TechArg
     float4 il = compute_lic<ST, FL, NL, INTEG, GRAD>(a, pos, f);
     ++samples;
     il.w *= a.intensity_scale;
-    const float4 src = shade(a, s_tf, il, tfv, pos, dir);
+    const float4 src = shade<GRAD>(a, s_tf, il, tfv, pos, dir, f);
     dest = blend(dest, src);
   }
   return dest;
@@ -84,7 +84,7 @@ __device__ __forceinline__ float4 volume_pixel(const RenderArgs& a, const TechAr
       if (t.technique == VVLIC_TECHNIQUE_LICVOLUME) {
         const float I = sample_licvol(t, pos);
         const float4 tfv = tf_rgba(s_tf, a.tf_index == VVLIC_TF_INDEX_MAGNITUDE ? f.w : f.z);
-        src = shade(a, s_tf, make_float4(0.f, 0.f, 0.f, I), tfv, pos, dir);  // illumLIC
+        src = shade<false>(a, s_tf, make_float4(0.f, 0.f, 0.f, I), tfv, pos, dir, f);  // illumLIC
       } else {
         src = make_float4(f.x, f.y, f.z, tf_rgba(s_tf, f.w).w);
       }

@@ -42,6 +42,10 @@ struct RenderArgs {
   float gate_lo, gate_hi;
   int num_iter, lb, lf, illum, tf_index, sof, gate, quirks;
   float light_pos[3], spec_exp, light_diff[3], light_spec[3], light_amb[3];
+  // line-illumination tables (ZOECKLER / MALLO): Zoeckler, Mallo diffuse, Mallo specular,
+  // lut_w x lut_h RGBA8 each, x fastest
+  const uchar4* luts;
+  int lut_w, lut_h;
   // adjoint tape (recording forward / adjoint only): per ray `tape_stride` samples of
   // (intensity, TF coordinate), `tape_nck` checkpoints of (position, dest before the sample)
   // every kSegment samples, and the sample count
@@ -477,13 +481,76 @@ __device__ __forceinline__ float alpha_correct(float al, float corr) {
   return 1.0f - powf(base, corr);
 }
 
+__device__ __forceinline__ float3 cross3(float3 a, float3 b) {
+  return f3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+
+// texture2D on an RGBA8 table with LINEAR + CLAMP_TO_EDGE (illumination.cpp:335-346): texel
+// centres at (i + 0.5) / w.  Clamping the coordinate to [0, 1] first is the same for finite
+// coordinates and sends a NaN one (a degenerate tangent) to the edge texel.
+__device__ __forceinline__ float4 lut2d(const uchar4* t, int w, int h, float s, float r) {
+  s = fminf(fmaxf(s, 0.0f), 1.0f);
+  r = fminf(fmaxf(r, 0.0f), 1.0f);
+  const float u = s * (float)w - 0.5f, v = r * (float)h - 0.5f;
+  const float fu = floorf(u), fv = floorf(v);
+  const float au = u - fu, av = v - fv;
+  const int x0 = max((int)fu, 0), x1 = min((int)fu + 1, w - 1);
+  const int y0 = max((int)fv, 0), y1 = min((int)fv + 1, h - 1);
+  const uchar4 c00 = __ldg(t + y0 * w + x0), c10 = __ldg(t + y0 * w + x1);
+  const uchar4 c01 = __ldg(t + y1 * w + x0), c11 = __ldg(t + y1 * w + x1);
+  const float k = 1.0f / 255.0f;
+  const float w00 = (1.0f - au) * (1.0f - av) * k, w10 = au * (1.0f - av) * k;
+  const float w01 = (1.0f - au) * av * k, w11 = au * av * k;
+  return make_float4(w00 * c00.x + w10 * c10.x + w01 * c01.x + w11 * c11.x,
+                     w00 * c00.y + w10 * c10.y + w01 * c01.y + w11 * c11.y,
+                     w00 * c00.z + w10 * c10.z + w01 * c01.z + w11 * c11.z,
+                     w00 * c00.w + w10 * c10.w + w01 * c01.w + w11 * c11.w);
+}
+
+// Light direction of every illumination model: normalize(light - pos * scaleVolInv).
+__device__ __forceinline__ float3 light_dir(const RenderArgs& a, float3 pos) {
+  return norm3(sub3(f3(a.light_pos[0], a.light_pos[1], a.light_pos[2]),
+                    mul3(pos, f3(a.scale_vol_inv[0], a.scale_vol_inv[1], a.scale_vol_inv[2]))));
+}
+
+// `f` is the field sample at `pos` (vectorData): its encoded direction is the streamline
+// tangent of illumZoeckler / illumMallo.  GRAD kernels (noise gradients fetched) only ever
+// shade with illumGradient; the others with illumLIC, illumZoeckler or illumMallo.
+template <bool GRAD>
 __device__ __forceinline__ float4 shade(const RenderArgs& a, const float* s_tf, float4 il, float4 tf, float3 pos,
-                                        float3 dir) {
+                                        float3 dir, float4 f) {
   const float I = il.w;
   float4 col;
-  if (a.illum == VVLIC_ILLUM_GRADIENT) {
-    float3 L = norm3(sub3(f3(a.light_pos[0], a.light_pos[1], a.light_pos[2]),
-                          mul3(pos, f3(a.scale_vol_inv[0], a.scale_vol_inv[1], a.scale_vol_inv[2]))));
+  if (!GRAD && a.illum == VVLIC_ILLUM_ZOECKLER) {  // inc_illum.glsl:117-154
+    const float3 L = light_dir(a, pos);
+    const float3 V = norm3(dir);
+    const float3 T = norm3(f3(2.0f * f.x - 1.0f, 2.0f * f.y - 1.0f, 2.0f * f.z - 1.0f));
+    const float4 sh = lut2d(a.luts, a.lut_w, a.lut_h, 0.5f * dot3(L, T) + 0.5f, 0.5f * dot3(V, T) + 0.5f);
+    const float d = sh.x * a.illum_scale;
+    const float sp = 0.9f * ((a.quirks & VVLIC_QUIRK_ZOECKLER_LUMINANCE) ? sh.y : sh.w);
+    col.x = tf.x * I * d + sp;
+    col.y = tf.y * I * d + sp;
+    col.z = tf.z * I * d + sp;
+  } else if (!GRAD && a.illum == VVLIC_ILLUM_MALLO) {  // inc_illum.glsl:46-112
+    const float3 L = light_dir(a, pos);
+    const float3 V = norm3(scl3(dir, -1.0f));
+    const float3 T = norm3(f3(2.0f * f.x - 1.0f, 2.0f * f.y - 1.0f, 2.0f * f.z - 1.0f));
+    const float3 B = norm3(cross3(T, V));
+    const float3 N = cross3(B, T);
+    const float3 Hv = norm3(add3(V, L));
+    const float ln = dot3(L, N), lt = dot3(L, T), hn = dot3(Hv, N), ht = dot3(Hv, T);
+    const float rl = 1.0f / sqrtf(1.0f - lt * lt), rh = 1.0f / sqrtf(1.0f - ht * ht);
+    const float cz = 0.5f * (ln * rl) + 0.5f, cy = 0.5f * lt + 0.5f, cw = 0.5f * (hn * rh) + 0.5f;
+    const size_t one = (size_t)a.lut_w * a.lut_h;
+    const float4 df = lut2d(a.luts + one, a.lut_w, a.lut_h, cz, cy);
+    const float4 sc = lut2d(a.luts + 2 * one, a.lut_w, a.lut_h, cz, cw);
+    const float att = powf(rh, -a.spec_exp);  // (1 - (H.T)^2)^(n/2)
+    const float ti = I * a.illum_scale;
+    col.x = tf.x * ti * df.x + __saturatef(sc.x * att);
+    col.y = tf.y * ti * df.y + __saturatef(sc.y * att);
+    col.z = tf.z * ti * df.z + __saturatef(sc.z * att);
+  } else if (GRAD) {
+    float3 L = light_dir(a, pos);
     float3 V = norm3(scl3(dir, -1.0f));
     float3 N = norm3(f3(-il.x, -il.y, -il.z));
     float3 R = norm3(sub3(scl3(N, 2.0f * dot3(L, N)), L));
@@ -587,7 +654,7 @@ __device__ __forceinline__ float4 trace_pixel(const RenderArgs& a, const float* 
         if (samples < (uint32_t)a.tape_stride) a.tape_is[ray * a.tape_stride + samples] = make_float2(il.w, tfc);
       }
       ++samples;
-      src = shade(a, s_tf, il, tf, pos, dir);
+      src = shade<GRAD>(a, s_tf, il, tf, pos, dir, f);
       dest = blend(dest, src);
       pos = add3(pos, scl3(dir, a.step_size));
       outside = outside_box(a, pos) || src.w > a.alpha_thr;

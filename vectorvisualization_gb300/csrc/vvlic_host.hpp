@@ -96,6 +96,12 @@ struct vvlic_ctx {
   float taps_inv_area = 0.5f;
   vvlic_params params;
   vvlic_view view;
+  // line-illumination tables: Zoeckler, Mallo diffuse, Mallo specular, lut_w x lut_h RGBA8 each
+  vvlic_line_material line_mat;
+  void* d_luts = nullptr;
+  size_t lut_bytes = 0;
+  int lut_w = 0, lut_h = 0;
+  bool luts_valid = false;
   unsigned long long* d_counters = nullptr;
   unsigned* d_scratch_word = nullptr;
   void* d_image = nullptr;
@@ -135,6 +141,8 @@ struct vvlic_ctx {
 
 namespace vvlic {
 vvlic_status fail(vvlic_ctx* c, vvlic_status s, const char* fmt, ...);
+// Builds (first use, or after a material change) and uploads the line-illumination tables.
+vvlic_status ensure_illum_luts(vvlic_ctx* c);
 vvlic_status cuda_fail(vvlic_ctx* c, cudaError_t e, const char* what);
 Geometry make_geometry(const int n[3], const float* slice_dist);
 vvlic_status derive_taps(const vvlic_ctx* c, int lb, int lf, float* taps, float* inv_area);
