@@ -53,6 +53,10 @@ def parse():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--c3", action="store_true", help="also time the 64-volume batch")
     ap.add_argument("--c3-volumes", type=int, default=64)
+    ap.add_argument("--c5", action="store_true", help="also time the 512^3 RK4 lit orbit")
+    ap.add_argument("--c5-frames", type=int, default=8)
+    ap.add_argument("--c5-size", type=int, default=512)
+    ap.add_argument("--c5-image", type=int, default=2048)
     return ap.parse_args()
 
 
@@ -387,6 +391,69 @@ def bench_batch(ctx, torch, stream, flush, args):
     }
 
 
+def bench_orbit(ctx, torch, stream, flush, args):
+    """C5: 512^3 FP16 solenoidal spectral field, dense gradient noise, RK4 L=60, step 1/512,
+    2048^2, gradient lighting; the first `--c5-frames` frames of the 64-frame orbit, one launch
+    each, L2 flushed between frames (the 1.5 GiB field + noise working set exceeds L2 anyway)."""
+    from vectorvisualization_gb300 import capi, workloads as wl
+
+    t0 = time.perf_counter()
+    w = wl.c5(size=args.c5_size, image=args.c5_image, frames=64, device="cuda")
+    gen_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    vid = wl.setup_context(ctx, w)
+    p = w.params
+    p.sampler = capi.SAMPLER[args.sampler]
+    p.schedule = capi.SCHEDULE[args.schedule]
+    ctx.set_params(p)
+    setup_s = time.perf_counter() - t0
+    W, H = w.width, w.height
+    out = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+    sh = stream.cuda_stream
+    frames = max(1, min(args.c5_frames, 64))
+    with torch.cuda.stream(stream):
+        ctx.render_device(vid, out.data_ptr(), W, H, None, sh)  # warm-up (cell layouts, tables)
+    stream.synchronize()
+    ms, steps, samples = [], 0, 0
+    clocks = Clocks(torch.cuda.current_device())
+    clocks.start()
+    for f in range(frames):
+        ctx.set_view(w.views[f])
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            e0.record(stream)
+            ctx.render_device(vid, out.data_ptr(), W, H, None, sh)
+            e1.record(stream)
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+        st = ctx.stats()
+        steps += int(st.sample_steps)
+        samples += int(st.samples)
+    clk = clocks.stop()
+    total_ms = sum(ms)
+    peak, peak_kind = load_peaks()
+
+    class _S:
+        pass
+
+    agg = _S()
+    agg.sample_steps, agg.samples = steps, samples
+    alg = algorithmic_bytes(agg, p, w.storage, True, W * H * frames)
+    achieved = alg / (total_ms / 1e3) / 1e9
+    key = f"c5/{w.storage}/{args.sampler}/{args.c5_size}/{args.c5_image}"
+    traffic = load_traffic(key)
+    return {
+        "workload": w.name, "frames": frames, "ms_per_frame": total_ms / frames,
+        "frames_per_s": frames / (total_ms / 1e3), "gss": steps / (total_ms / 1e3) / 1e9,
+        "sample_steps_per_frame": steps / frames, "samples_per_frame": samples / frames,
+        "sampler": args.sampler, "storage": w.storage,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "peak_kind": peak_kind, "algorithmic_bytes_per_frame": alg / frames},
+        "clocks": clk, "generation_s": gen_s, "setup_s": setup_s,
+    }
+
+
 def run_ours(args, dist: Dist):
     import torch
 
@@ -513,6 +580,9 @@ def run_ours(args, dist: Dist):
     if args.c3 and dist.rank == 0:
         with capi.Context(dev) as bctx:
             line["batch"] = bench_batch(bctx, torch, stream, flush, args)
+    if args.c5 and dist.rank == 0:
+        with capi.Context(dev) as octx:
+            line["orbit"] = bench_orbit(octx, torch, stream, flush, args)
 
     # end to end through the C ABI with host buffers
     if not args.no_e2e:
