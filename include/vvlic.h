@@ -396,6 +396,61 @@ vvlic_status vvlic_get_stats(vvlic_ctx* ctx, vvlic_stats* stats);
  * background_fragment.glsl:7-20 (dest = clamp((1-dest.a)*white + dest, 0, 1)).  Host memory. */
 vvlic_status vvlic_composite_background(float* rgba, int32_t w, int32_t h, const float* bg_rgba);
 
+/* ---- on-disk formats and the image dump (host only; no context, no device) ---------- */
+
+/* Data types of a .dat description (reader.h DataType). */
+enum { VVLIC_DAT_NONE = 0, VVLIC_DAT_UCHAR = 1, VVLIC_DAT_USHORT = 2, VVLIC_DAT_FLOAT = 3 };
+
+/* A parsed .dat volume description: DatFile::parseDatFile (reader.cpp:80-262).  Lines starting
+ * with '#' are skipped; the keys ObjectFileName, Resolution, SliceThickness, Format and
+ * TimeDependent are found anywhere in a line, in that order of precedence, with the value
+ * after the first ':'; other lines are ignored.  Format takes UCHAR / USHORT / FLOAT and the
+ * first number after it as the component count (1 if none).  raw_file is the raw-file pattern
+ * (printf-style, formatted with the timestep) as written, or, when the file it names does not
+ * exist, the same pattern relative to the .dat file's directory. */
+typedef struct vvlic_dat_info {
+  char raw_file[1024];
+  int32_t resolution[3];     /* (0, 0, 0) */
+  float slice_thickness[3];  /* (1, 1, 1) */
+  int32_t format;            /* VVLIC_DAT_* */
+  int32_t components;        /* data dimension */
+  int32_t timestep_begin;    /* TimeDependent: first and last timestep (0, 0) */
+  int32_t timestep_end;
+} vvlic_dat_info;
+/* VVLIC_ERR_IO if the .dat or a raw file of any timestep cannot be opened; VVLIC_ERR_FORMAT for
+ * a key without ':' or with too few values, an unknown Format, illegal TimeDependent bounds, or
+ * no ObjectFileName.  vvlic_io_error() then holds the message. */
+vvlic_status vvlic_dat_parse(const char* dat_path, vvlic_dat_info* info);
+/* Bytes of one timestep: type size * components * resolution product. */
+uint64_t vvlic_dat_bytes(const vvlic_dat_info* info);
+/* DatFile::readRawData (reader.cpp:265-303): one timestep's raw data, x fastest.  Unlike the
+ * reference, which returns a partly filled buffer, a short file is VVLIC_ERR_IO. */
+vvlic_status vvlic_dat_read(const vvlic_dat_info* info, int32_t timestep, void* out, uint64_t capacity);
+/* VectorDataSet::loadData + createTextureIterp (dataset.cpp:96-176, 290-366): parse, check that
+ * the set is a 3-component UCHAR or FLOAT field (else VVLIC_ERR_FORMAT), read `timestep` and
+ * upload it with the .dat's slice thickness.  timestep < 0 takes timestep_begin. */
+vvlic_status vvlic_upload_dat(vvlic_ctx* ctx, const char* dat_path, int32_t timestep, int32_t storage,
+                              int32_t* vol_id);
+
+/* Noise volume file of NoiseDataSet::loadRawData (dataset.cpp:1347-1389): a 12-byte header of
+ * three native int32 sizes (x, y, z) followed by x*y*z bytes, x fastest.  With out == NULL only
+ * dims is written. */
+vvlic_status vvlic_noise_read(const char* path, uint8_t* out, uint64_t capacity, int32_t dims[3]);
+vvlic_status vvlic_noise_write(const char* path, const uint8_t* noise, const int32_t dims[3]);
+
+/* Image dump of Renderer::saveTexture + pngWrite (renderer.cpp:340-420, imageUtils.cpp:117-139):
+ * each float channel to (int)(255 * v) clamped to [0, 255], rows written top first (the image's
+ * row 0 is the bottom, as GL reads it back).  VVLIC_IMAGE_PPM writes binary P6 RGB (alpha
+ * dropped), VVLIC_IMAGE_PNG an 8-bit RGBA PNG.  With composite != 0 the image is first put over
+ * white as background_fragment.glsl does (the window image; 0 dumps the render buffer as the
+ * reference's screenshot does). */
+enum { VVLIC_IMAGE_PPM = 0, VVLIC_IMAGE_PNG = 1 };
+vvlic_status vvlic_image_write(const char* path, const float* rgba, int32_t w, int32_t h, int32_t kind,
+                               int32_t composite);
+
+/* Message of the last failing call of this section on the calling thread. */
+const char* vvlic_io_error(void);
+
 /* ---- preprocessing on caller-owned device buffers ----------------------------------- */
 
 /* computeGradients/filterGradients/quantizeGradients + RGBA pack (gradient.cpp:190-531,

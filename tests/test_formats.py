@@ -1,0 +1,227 @@
+"""On-disk formats (vectorvisualization_gb300.formats over formats.cpp): the .dat/.raw reader
+against the reference's own DatFile (golden results generated by tests/golden/make_dat_golden.py
+from reader.cpp compiled unmodified, and live when oracle/_ref is built), the noise file, and the
+PNG / PPM image dump."""
+import ctypes as C
+import json
+import os
+import struct
+import sys
+import zlib
+
+import numpy as np
+import pytest
+
+from vectorvisualization_gb300 import capi, formats
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "golden"))
+from dat_cases import CASES, make_case  # noqa: E402
+
+REF = os.path.join(HERE, "..", "oracle", "_ref", "libvvref_sobel.so")
+
+
+def ours(path):
+    try:
+        i = formats.parse_dat(path)
+    except capi.VVLICError:
+        return {"ok": False}
+    return {"ok": True, "raw_file": i.raw_file, "resolution": list(i.resolution),
+            "slice_thickness": [float(v) for v in i.slice_thickness], "format": i.format,
+            "components": i.components, "timestep_begin": i.timestep_begin, "timestep_end": i.timestep_end}
+
+
+@pytest.fixture
+def empty_cwd(tmp_path, monkeypatch):
+    d = tmp_path / "_cwd"
+    d.mkdir()
+    monkeypatch.chdir(d)
+    return tmp_path
+
+
+def test_dat_parse_matches_reference_golden(empty_cwd):
+    with open(os.path.join(HERE, "golden", "dat_golden.json")) as fh:
+        golden = json.load(fh)
+    assert set(golden) == {c[0] for c in CASES}
+    for name, text, raws in CASES:
+        p = make_case(str(empty_cwd), name, text, raws)
+        got = ours(p)
+        want = dict(golden[name])
+        if got["ok"]:
+            got["raw_file"] = got["raw_file"].replace(os.path.join(str(empty_cwd), name), "<DIR>")
+        assert got == want, name
+
+
+def _ref_lib():
+    if not os.path.exists(REF):
+        pytest.skip("oracle/_ref not built (the reference sources are not present)")
+    return C.CDLL(os.path.abspath(REF))
+
+
+def _ref_parse(lib, path):
+    raw = C.create_string_buffer(1024)
+    sizes, dists = (C.c_int * 3)(), (C.c_float * 3)()
+    t, dim, b, e = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+    if lib.vvref_dat_parse(path.encode(), raw, 1024, sizes, dists, C.byref(t), C.byref(dim), C.byref(b), C.byref(e)):
+        return {"ok": False}
+    return {"ok": True, "raw_file": raw.value.decode(), "resolution": list(sizes),
+            "slice_thickness": [float(v) for v in dists], "format": t.value, "components": dim.value,
+            "timestep_begin": b.value, "timestep_end": e.value}
+
+
+def test_dat_parse_fuzz_against_reference(empty_cwd):
+    """Random key orders, spacing, comments, number spellings and bad lines, parsed by both."""
+    lib = _ref_lib()
+    rng = np.random.default_rng(7)
+    ints = lambda v: rng.choice([str(v), f"0x{v:x}", f"0{v:o}", f"+{v}", f" {v} "])  # noqa: E731
+    fmts = ["UCHAR3", "FLOAT3", "USHORT", "FLOAT", "UCHAR 3", "FLOAT x3 data", "uchar3", "INT3"]
+    for k in range(150):
+        nx, ny, nz = (int(v) for v in rng.integers(1, 9, 3))
+        lines = [
+            f"ObjectFileName{rng.choice([':', ' :', ':  '])}r{k}.raw{rng.choice(['', '  # c', ' extra'])}",
+            f"Resolution:{ints(nx)} {ints(ny)} {ints(nz)}",
+            f"SliceThickness: {rng.choice(['1 1 1', '0.5 2 1e0', '2.5e-1 1 3', '1 2'])}",
+            f"Format: {rng.choice(fmts)}",
+        ]
+        if rng.random() < 0.3:
+            lines.append(f"TimeDependent: {rng.choice(['0 0', '1 0', '-1 2', '0'])}")
+        if rng.random() < 0.3:
+            lines.insert(int(rng.integers(0, len(lines))), rng.choice(["# comment", "Unknown: 3", "", "   "]))
+        rng.shuffle(lines)
+        text = rng.choice(["\n", "\r\n"]).join(lines) + "\n"
+        p = make_case(str(empty_cwd), f"f{k}", text, {f"r{k}.raw": 8 * 3 * 512})
+        want = _ref_parse(lib, p)
+        got = ours(p)
+        if want["ok"] and want["format"] == 0:  # no Format line parsed: the reference leaves
+            want.pop("components"), got.pop("components", None)  # the component count unset
+        assert got == want, text
+
+
+def test_dat_read_matches_reference_and_numpy(empty_cwd):
+    rng = np.random.default_rng(3)
+    field = rng.standard_normal((3, 4, 5, 3)).astype(np.float32)
+    p = str(empty_cwd / "v.dat")
+    formats.write_dat(p, field, slice_thickness=(1.0, 0.5, 2.0))
+    info = formats.parse_dat(p)
+    assert info.resolution == (5, 4, 3) and info.components == 3 and info.format == capi.DAT_FLOAT
+    np.testing.assert_array_equal(formats.read_dat(info), field)
+    got, sd = formats.load_vector_dataset(p)
+    np.testing.assert_array_equal(got, field)
+    assert sd == (1.0, 0.5, 2.0)
+    if os.path.exists(REF):
+        lib = _ref_lib()
+        buf = np.empty_like(field)
+        assert lib.vvref_dat_read(p.encode(), 0, buf.ctypes.data, C.c_long(buf.nbytes)) == 0
+        np.testing.assert_array_equal(buf, field)
+
+
+def test_dat_timesteps_and_errors(empty_cwd):
+    steps = [np.full((2, 3, 4, 3), t, np.uint8) for t in range(3)]
+    p = str(empty_cwd / "t.dat")
+    formats.write_dat(p, None, timesteps=steps)
+    info = formats.parse_dat(p)
+    assert (info.timestep_begin, info.timestep_end) == (0, 2)
+    for t in range(3):
+        np.testing.assert_array_equal(formats.read_dat(info, t), steps[t])
+    with pytest.raises(capi.VVLICError):
+        formats.read_dat(info, 3)
+    # a truncated raw file is an error (the reference returns a partly filled buffer)
+    with open(str(empty_cwd / "t_1.raw"), "r+b") as fh:
+        fh.truncate(10)
+    with pytest.raises(capi.VVLICError, match="holds 10 of 72 bytes"):
+        formats.read_dat(info, 1)
+    with pytest.raises(capi.VVLICError, match="cannot open"):
+        formats.parse_dat(str(empty_cwd / "nope.dat"))
+    # a raw-file pattern with a non-integer conversion is rejected, not formatted
+    bad = str(empty_cwd / "bad.dat")
+    with open(bad, "w") as fh:
+        fh.write("ObjectFileName: x%s.raw\nResolution: 1 1 1\nFormat: UCHAR3\n")
+    with pytest.raises(capi.VVLICError):
+        formats.parse_dat(bad)
+    # a scalar set is not a vector data set
+    s = str(empty_cwd / "s.dat")
+    formats.write_dat(s, np.zeros((2, 2, 2), np.uint8))
+    with pytest.raises(capi.VVLICError):
+        formats.load_vector_dataset(s)
+
+
+def test_noise_file_layout_and_roundtrip(tmp_path):
+    rng = np.random.default_rng(1)
+    noise = rng.integers(0, 256, (3, 5, 7), dtype=np.uint8)
+    p = str(tmp_path / "noise_7_5_3")
+    formats.write_noise(p, noise)
+    raw = open(p, "rb").read()
+    assert struct.unpack("<3i", raw[:12]) == (7, 5, 3)  # x, y, z sizes, x fastest
+    assert raw[12:] == noise.tobytes()
+    np.testing.assert_array_equal(formats.read_noise(p), noise)
+    with open(p, "r+b") as fh:
+        fh.truncate(12 + 50)
+    with pytest.raises(capi.VVLICError):
+        formats.read_noise(p)
+    with open(p, "wb") as fh:
+        fh.write(struct.pack("<3i", -1, 5, 3))
+    with pytest.raises(capi.VVLICError):
+        formats.read_noise(p)
+
+
+def _decode_png(data: bytes):
+    assert data[:8] == b"\x89PNG\r\n\x1a\n"
+    pos, chunks = 8, {}
+    while pos < len(data):
+        n = struct.unpack(">I", data[pos:pos + 4])[0]
+        typ = data[pos + 4:pos + 8]
+        body = data[pos + 8:pos + 8 + n]
+        crc = struct.unpack(">I", data[pos + 8 + n:pos + 12 + n])[0]
+        assert zlib.crc32(typ + body) & 0xFFFFFFFF == crc
+        chunks.setdefault(typ, b"")
+        chunks[typ] += body
+        pos += 12 + n
+    w, h, depth, ctype = struct.unpack(">IIBB", chunks[b"IHDR"][:10])
+    assert (depth, ctype) == (8, 6)
+    raw = zlib.decompress(chunks[b"IDAT"])
+    rows = np.frombuffer(raw, np.uint8).reshape(h, 4 * w + 1)
+    assert (rows[:, 0] == 0).all()
+    return rows[:, 1:].reshape(h, w, 4)
+
+
+def test_png_dump_is_the_saved_texture(tmp_path):
+    rng = np.random.default_rng(2)
+    img = rng.uniform(-0.2, 1.2, (37, 300, 4)).astype(np.float32)  # > 64 KiB of rows: several blocks
+    p = str(tmp_path / "a.png")
+    formats.write_image(p, img)
+    got = _decode_png(open(p, "rb").read())
+    want = np.clip((np.float32(255.0) * img).astype(np.int64), 0, 255).astype(np.uint8)[::-1]  # (int)(255 v)
+    np.testing.assert_array_equal(got, want)
+    # over white: clamp((1 - a) * 1 + c, 0, 1)
+    formats.present(p, img)
+    comp = np.clip((1.0 - img[..., 3:4]) + img, 0, 1).astype(np.float32)
+    want = np.clip((np.float32(255.0) * comp).astype(np.int64), 0, 255).astype(np.uint8)[::-1]
+    np.testing.assert_array_equal(_decode_png(open(p, "rb").read()), want)
+
+
+def test_ppm_dump(tmp_path):
+    img = np.zeros((2, 3, 4), np.float32)
+    img[0, 0] = (1.0, 0.5, 0.25, 1.0)  # bottom-left pixel
+    p = str(tmp_path / "a.ppm")
+    formats.write_image(p, img)
+    data = open(p, "rb").read()
+    head = b"P6\n3 2\n255\n"
+    assert data.startswith(head)
+    px = np.frombuffer(data[len(head):], np.uint8).reshape(2, 3, 3)
+    assert tuple(px[1, 0]) == (255, 127, 63) and px[0].max() == 0
+
+
+@pytest.mark.gpu
+def test_upload_dat_matches_upload_field(ctx, oracle, tmp_path):
+    from vectorvisualization_gb300 import workloads as wl
+
+    field = wl.vortex_field((12, 10, 8), seed=4)
+    p = str(tmp_path / "v.dat")
+    formats.write_dat(p, field, slice_thickness=(1.0, 1.0, 2.0))
+    vid = ctx.upload_dat(p, storage="f32")
+    np.testing.assert_array_equal(ctx.download_field(vid, (12, 10, 8), "f32"), oracle.encode_field(field))
+    steps = [wl.abc_field((6, 6, 6)), wl.vortex_field((6, 6, 6), seed=2)]
+    p2 = str(tmp_path / "t.dat")
+    formats.write_dat(p2, None, timesteps=steps)
+    vid = ctx.upload_dat(p2, timestep=1)
+    np.testing.assert_array_equal(ctx.download_field(vid, (6, 6, 6), "f32"), oracle.encode_field(steps[1]))

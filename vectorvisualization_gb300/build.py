@@ -38,7 +38,14 @@ def _nvcc() -> str:
 
 
 def _sources() -> list[str]:
-    return sorted(f for f in os.listdir(CSRC) if f.endswith(".cu"))
+    return sorted(f for f in os.listdir(CSRC) if f.endswith((".cu", ".cpp")))
+
+
+def _cxx() -> str:
+    for cand in (os.environ.get("CXX"), shutil.which("g++"), shutil.which("c++")):
+        if cand:
+            return cand
+    raise RuntimeError("no C++ compiler found")
 
 
 def _digest(extra: str) -> str:
@@ -68,8 +75,12 @@ def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -
                 return LIB
 
     def compile_one(src: str) -> str:
-        obj = os.path.join(BUILD_DIR, src.replace(".cu", ".o"))
-        cmd = [nvcc, *ARCH, *COMMON, *extra, "-I", INCLUDE, "-c", os.path.join(CSRC, src), "-o", obj]
+        obj = os.path.join(BUILD_DIR, os.path.splitext(src)[0] + ".o")
+        if src.endswith(".cpp"):  # host-only C++ (file formats): the plain C++ compiler
+            cmd = [_cxx(), "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-I", INCLUDE, "-c",
+                   os.path.join(CSRC, src), "-o", obj]
+        else:
+            cmd = [nvcc, *ARCH, *COMMON, *extra, "-I", INCLUDE, "-c", os.path.join(CSRC, src), "-o", obj]
         if src in NO_FMA:
             cmd[1:1] = ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]
         if verbose:

@@ -119,6 +119,22 @@ class LineMaterial(C.Structure):
     ]
 
 
+class DatInfo(C.Structure):
+    _fields_ = [
+        ("raw_file", C.c_char * 1024),
+        ("resolution", C.c_int32 * 3),
+        ("slice_thickness", C.c_float * 3),
+        ("format", C.c_int32),
+        ("components", C.c_int32),
+        ("timestep_begin", C.c_int32),
+        ("timestep_end", C.c_int32),
+    ]
+
+
+DAT_NONE, DAT_UCHAR, DAT_USHORT, DAT_FLOAT = 0, 1, 2, 3
+IMAGE_PPM, IMAGE_PNG = 0, 1
+
+
 class Stats(C.Structure):
     _fields_ = [
         ("samples", C.c_uint64),
@@ -139,6 +155,14 @@ _SIGS = {
     "vvlic_line_material_default": (None, [C.POINTER(LineMaterial)]),
     "vvlic_set_line_material": (_I, [_P, C.POINTER(LineMaterial)]),
     "vvlic_get_illum_luts": (_I, [_P, _P, _P, _P, C.POINTER(_I), C.POINTER(_I)]),
+    "vvlic_dat_parse": (_I, [C.c_char_p, C.POINTER(DatInfo)]),
+    "vvlic_dat_bytes": (C.c_uint64, [C.POINTER(DatInfo)]),
+    "vvlic_dat_read": (_I, [C.POINTER(DatInfo), _I, _P, C.c_uint64]),
+    "vvlic_upload_dat": (_I, [_P, C.c_char_p, _I, _I, C.POINTER(_I)]),
+    "vvlic_noise_read": (_I, [C.c_char_p, _P, C.c_uint64, _P]),
+    "vvlic_noise_write": (_I, [C.c_char_p, _P, _P]),
+    "vvlic_image_write": (_I, [C.c_char_p, _P, _I, _I, _I, _I]),
+    "vvlic_io_error": (C.c_char_p, []),
     "vvlic_create": (_I, [C.POINTER(_P), _I]),
     "vvlic_destroy": (_I, [_P]),
     "vvlic_last_error": (C.c_char_p, [_P]),
@@ -385,6 +409,15 @@ class Context:
         r = None if rgba is None else np.ascontiguousarray(rgba, dtype=np.float32).reshape(TF_ENTRIES * 4)
         o = None if opacity is None else np.ascontiguousarray(opacity, dtype=np.float32).reshape(TF_ENTRIES)
         self._check(self._lib.vvlic_set_tf(self.h, _ptr(r), _ptr(o)), "set_tf")
+
+    def upload_dat(self, dat_path: str, timestep: int = -1, storage: str = "f32") -> int:
+        """Load a .dat/.raw vector data set (VectorDataSet::loadData) into a volume."""
+        vid = _I(0)
+        st = self._lib.vvlic_upload_dat(self.h, os.fsencode(dat_path), timestep, STORAGE[storage], C.byref(vid))
+        if st:
+            msg = self._lib.vvlic_io_error().decode() or self._lib.vvlic_last_error(self.h).decode()
+            raise VVLICError(st, f"upload_dat: {msg}")
+        return vid.value
 
     def set_line_material(self, material: LineMaterial):
         self._check(self._lib.vvlic_set_line_material(self.h, C.byref(material)), "set_line_material")
