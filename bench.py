@@ -63,45 +63,10 @@ def parse():
 # ---------------------------------------------------------------------------------------------
 # distributed plumbing (one process per GPU; replicas of the same workload, no data exchange)
 # ---------------------------------------------------------------------------------------------
-class Dist:
-    def __init__(self, init: bool = True):
-        self.world = int(os.environ.get("WORLD_SIZE", "1"))
-        self.rank = int(os.environ.get("RANK", "0"))
-        self.local = int(os.environ.get("LOCAL_RANK", "0"))
-        self.pg = None
-        if self.world > 1 and init:
-            import torch
-            import torch.distributed as dist
+def Dist(init: bool = True):
+    from vectorvisualization_gb300.replicas import Replicas
 
-            torch.cuda.set_device(self.local)
-            dist.init_process_group("nccl")
-            self.pg = dist
-
-    def barrier(self):
-        if self.pg:
-            self.pg.barrier()
-
-    def max(self, x: float) -> float:
-        if not self.pg:
-            return x
-        import torch
-
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
-        return float(t.item())
-
-    def sum(self, x: float) -> float:
-        if not self.pg:
-            return x
-        import torch
-
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        self.pg.all_reduce(t, op=self.pg.ReduceOp.SUM)
-        return float(t.item())
-
-    def close(self):
-        if self.pg:
-            self.pg.destroy_process_group()
+    return Replicas(backend="nccl", init=init)
 
 
 # ---------------------------------------------------------------------------------------------
@@ -220,7 +185,7 @@ def cpu_sample(w, seconds: float, threads: int = 0, rows_offset: int = 0):
             "threads": pyoracle.max_threads() if threads <= 0 else threads}
 
 
-def run_reference(args, dist: Dist):
+def run_reference(args, dist):
     """CPU restatement of the reference path, all host threads, bounded sample per step."""
     if dist.rank != 0:
         return 0
@@ -391,10 +356,11 @@ def bench_batch(ctx, torch, stream, flush, args):
     }
 
 
-def bench_orbit(ctx, torch, stream, flush, args):
+def bench_orbit(ctx, torch, stream, flush, args, dist):
     """C5: 512^3 FP16 solenoidal spectral field, dense gradient noise, RK4 L=60, step 1/512,
-    2048^2, gradient lighting; the first `--c5-frames` frames of the 64-frame orbit, one launch
-    each, L2 flushed between frames (the 1.5 GiB field + noise working set exceeds L2 anyway)."""
+    2048^2, gradient lighting; `--c5-frames` frames of the 64-frame orbit per GPU (frames dealt
+    round-robin over the ranks, each holding its own copy of the inputs), one launch each, L2
+    flushed between frames (the 1.5 GiB field + noise working set exceeds L2 anyway)."""
     from vectorvisualization_gb300 import capi, workloads as wl
 
     t0 = time.perf_counter()
@@ -410,14 +376,17 @@ def bench_orbit(ctx, torch, stream, flush, args):
     W, H = w.width, w.height
     out = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
     sh = stream.cuda_stream
-    frames = max(1, min(args.c5_frames, 64))
+    per_rank = max(1, min(args.c5_frames, 64 // dist.world))
+    mine = dist.shard(per_rank * dist.world)
+    frames = len(mine)
     with torch.cuda.stream(stream):
         ctx.render_device(vid, out.data_ptr(), W, H, None, sh)  # warm-up (cell layouts, tables)
     stream.synchronize()
     ms, steps, samples = [], 0, 0
     clocks = Clocks(torch.cuda.current_device())
     clocks.start()
-    for f in range(frames):
+    dist.barrier()
+    for f in mine:
         ctx.set_view(w.views[f])
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         with torch.cuda.stream(stream):
@@ -431,7 +400,9 @@ def bench_orbit(ctx, torch, stream, flush, args):
         steps += int(st.sample_steps)
         samples += int(st.samples)
     clk = clocks.stop()
-    total_ms = sum(ms)
+    total_ms = dist.max(sum(ms))
+    steps, samples = dist.sum(float(steps)), dist.sum(float(samples))
+    frames = per_rank * dist.world
     peak, peak_kind = load_peaks()
 
     class _S:
@@ -440,7 +411,7 @@ def bench_orbit(ctx, torch, stream, flush, args):
     agg = _S()
     agg.sample_steps, agg.samples = steps, samples
     alg = algorithmic_bytes(agg, p, w.storage, True, W * H * frames)
-    achieved = alg / (total_ms / 1e3) / 1e9
+    achieved = alg / (total_ms / 1e3) / 1e9 / dist.world  # per GPU, against one GPU's peak
     key = f"c5/{w.storage}/{args.sampler}/{args.c5_size}/{args.c5_image}"
     traffic = load_traffic(key)
     return {
@@ -454,7 +425,7 @@ def bench_orbit(ctx, torch, stream, flush, args):
     }
 
 
-def run_ours(args, dist: Dist):
+def run_ours(args, dist):
     import torch
 
     from vectorvisualization_gb300 import build, capi, workloads as wl
@@ -580,9 +551,11 @@ def run_ours(args, dist: Dist):
     if args.c3 and dist.rank == 0:
         with capi.Context(dev) as bctx:
             line["batch"] = bench_batch(bctx, torch, stream, flush, args)
-    if args.c5 and dist.rank == 0:
+    if args.c5:
         with capi.Context(dev) as octx:
-            line["orbit"] = bench_orbit(octx, torch, stream, flush, args)
+            orbit = bench_orbit(octx, torch, stream, flush, args, dist)
+        if dist.rank == 0:
+            line["orbit"] = orbit
 
     # end to end through the C ABI with host buffers
     if not args.no_e2e:
