@@ -400,6 +400,9 @@ def bench_orbit(ctx, torch, stream, flush, args, dist):
         steps += int(st.sample_steps)
         samples += int(st.samples)
     clk = clocks.stop()
+    adjoint = None
+    if not args.no_adjoint:
+        adjoint = orbit_adjoint(ctx, torch, stream, flush, w, vid, out, mine[0])
     total_ms = dist.max(sum(ms))
     steps, samples = dist.sum(float(steps)), dist.sum(float(samples))
     frames = per_rank * dist.world
@@ -422,7 +425,58 @@ def bench_orbit(ctx, torch, stream, flush, args, dist):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_kind": peak_kind, "algorithmic_bytes_per_frame": alg / frames},
         "clocks": clk, "generation_s": gen_s, "setup_s": setup_s,
+        "fwd_adjoint": adjoint,
     }
+
+
+def orbit_adjoint(ctx, torch, stream, flush, w, vid, out, frame):
+    """Forward (recording) + adjoint of one lit C5 frame: L2 loss to the same frame rendered with
+    another transfer function; gradients for the TF, opacity and 121 taps."""
+    from vectorvisualization_gb300 import workloads as wl
+
+    W, H = w.width, w.height
+    sh = stream.cuda_stream
+    p = w.params
+    ctx.set_view(w.views[frame])
+    target = torch.empty_like(out)
+    ctx.set_tf(*wl.random_tf(seed=505))
+    ctx.render_device(vid, target.data_ptr(), W, H, None, sh)
+    ctx.set_tf(w.tf_rgba, w.tf_opac)
+    stream.synchronize()
+    ntaps = p.steps_forward + p.steps_backward + 1
+    d_tf = torch.empty((256, 4), dtype=torch.float32, device="cuda")
+    d_op = torch.empty(256, dtype=torch.float32, device="cuda")
+    d_taps = torch.empty(ntaps, dtype=torch.float32, device="cuda")
+    g = torch.empty_like(out)
+
+    def timed(fn):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
+    p.record_tape = 0
+    ctx.set_params(p)
+    fwd_ms = timed(lambda: ctx.render_device(vid, out.data_ptr(), W, H, None, sh))
+    steps = ctx.stats().sample_steps
+    p.record_tape = 1
+    ctx.set_params(p)
+    rec_ms = timed(lambda: ctx.render_device(vid, out.data_ptr(), W, H, None, sh))
+    with torch.cuda.stream(stream):
+        torch.mul(out - target, 2.0, out=g)
+    adj_ms = timed(lambda: ctx.render_adjoint(vid, g.data_ptr(), W, H, d_tf.data_ptr(), d_op.data_ptr(),
+                                              d_taps.data_ptr(), sh))
+    p.record_tape = 0
+    ctx.set_params(p)
+    return {"frame": frame, "fwd_ms": fwd_ms, "fwd_recording_ms": rec_ms, "adjoint_ms": adj_ms,
+            "fwd_plus_adjoint_over_fwd": (rec_ms + adj_ms) / fwd_ms,
+            "gss_fwd": steps / (fwd_ms / 1e3) / 1e9, "gss_fwd_adjoint": steps / ((rec_ms + adj_ms) / 1e3) / 1e9,
+            "finite": bool(torch.isfinite(d_tf).all() and torch.isfinite(d_taps).all()),
+            "grad_norms": {"tf": float(d_tf.norm()), "opacity": float(d_op.norm()), "taps": float(d_taps.norm())}}
 
 
 def run_ours(args, dist):

@@ -191,7 +191,7 @@ int32_t vvo_lic_volume(const vvo_inputs* vi, const vvlic_params* p, const int32_
  * dL/dtaps (L_b+L_f+1) for the image cotangent g_img (h*w*4). */
 int32_t vvo_adjoint(const vvo_inputs* vi, const vvlic_params* p, const double* ray_coeffs, int32_t w, int32_t h,
                     const float* g_img, double* d_tf, double* d_opac, double* d_taps, int32_t threads) {
-  if (p->illum != VVLIC_ILLUM_NONE) return -2;
+  if (p->illum != VVLIC_ILLUM_NONE && p->illum != VVLIC_ILLUM_GRADIENT) return -2;
   int lb, lf;
   int ntaps = effective_steps(p, &lb, &lf);
   std::vector<double> taps(ntaps);

@@ -1056,7 +1056,7 @@ template <class R> static inline uint32_t render_pixel(const Inputs& in, const v
 }
 
 /* ------------------------------------------------------------------------------------- */
-/* adjoint: reverse mode through the unlit ray (illumLIC + blend) with respect to the TF    */
+/* adjoint: reverse mode through the ray (illumLIC or illumGradient + blend) w.r.t. the TF  */
 /* RGBA table, the opacity table and the filter taps.  Conventions shared with the kernel: */
 /* d clamp(u)/du = 1 on [0, 1] and 0 outside; the alpha-correction derivative is 0 where   */
 /* its base 1 - a is <= 0; a 1D lookup's derivative in its coordinate is 0 where the       */
@@ -1089,11 +1089,11 @@ struct AdjointOut {
   double* taps;  /* L_b + L_f + 1 */
 };
 
-/* noise values n_j of every tap of the LIC at `pos` (order: index j + L_b) */
-template <class R> static inline void lic_noise_taps(const LicCtx<R>& c, V3<R> pos, V4<R> f0, std::vector<R>& n) {
+/* noise taps (gradient xyz, value) of every tap of the LIC at `pos` (order: index j + L_b) */
+template <class R> static inline void lic_noise_taps(const LicCtx<R>& c, V3<R> pos, V4<R> f0, std::vector<V4<R>>& n) {
   const int lb = c.u->lb, lf = c.u->lf;
-  n.assign(lb + lf + 1, R(0));
-  n[lb] = noise_tap<R>(c, pos).w;
+  n.assign(lb + lf + 1, V4<R>{R(0), R(0), R(0), R(0)});
+  n[lb] = noise_tap<R>(c, pos);
   for (int half = 0; half < 2; ++half) {
     R dirs = half == 0 ? R(-1) : R(1);
     int L = half == 0 ? lb : lf;
@@ -1101,9 +1101,73 @@ template <class R> static inline void lic_noise_taps(const LicCtx<R>& c, V3<R> p
     V4<R> step = f0;
     for (int i = 1; i <= L; ++i) {
       p = lic_step<R>(c, p, step, dirs);
-      n[half == 0 ? lb - i : lb + i] = noise_tap<R>(c, p).w;
+      n[half == 0 ? lb - i : lb + i] = noise_tap<R>(c, p);
     }
   }
+}
+
+/* illumGradient's colour (inc_illum.glsl:1-41) and its reverse mode.  Forward: N = n(-G),
+ * R = n(2 (L.N) N - L), col_c = (tf_c I (ld_c df + 0.3 + la_c) + ls_c I sat(R.V)^e) is with
+ * df = sat(L.N) is.  lit_vjp returns dL/dtf_c, dL/dI (colour part) and dL/dG for a colour
+ * cotangent dcol.  sat() has derivative 1 strictly inside (0, 1). */
+template <class R> struct Lit {
+  V3<R> L, V, m, N, r, Rv;
+  R mlen, rlen, ln, rv, df, spf, I;
+  bool ln_in, rv_in;
+};
+template <class R>
+static inline Lit<R> lit_setup(const LicCtx<R>& c, V3<R> G, R I, V3<R> pos, V3<R> dir) {
+  const Uniforms<R>& u = *c.u;
+  const vvlic_params& p = *c.p;
+  Lit<R> t;
+  V3<R> lp{R(p.light_pos[0]), R(p.light_pos[1]), R(p.light_pos[2])};
+  V3<R> sv{u.scale_vol_inv[0], u.scale_vol_inv[1], u.scale_vol_inv[2]};
+  t.L = normalize(lp - mul(pos, sv));
+  t.V = normalize(dir * R(-1));
+  t.m = V3<R>{-G.x, -G.y, -G.z};
+  t.mlen = std::sqrt(dot(t.m, t.m));
+  t.N = normalize(t.m);
+  t.ln = dot(t.L, t.N);
+  t.r = t.N * (R(2) * t.ln) - t.L;
+  t.rlen = std::sqrt(dot(t.r, t.r));
+  t.Rv = normalize(t.r);
+  t.rv = dot(t.Rv, t.V);
+  t.rv_in = t.rv > R(0) && t.rv < R(1);
+  t.ln_in = t.ln > R(0) && t.ln < R(1);
+  t.spf = std::pow(clamp01(t.rv), R(p.spec_exp));
+  t.df = clamp01(t.ln) * u.illum_scale;
+  t.I = I;
+  return t;
+}
+template <class R>
+static inline void lit_vjp(const LicCtx<R>& c, const Lit<R>& t, V4<R> tf, const R dcol[3], R dtf[3], R* dI, V3<R>* dG) {
+  const Uniforms<R>& u = *c.u;
+  const vvlic_params& p = *c.p;
+  const R is = u.illum_scale;
+  R cdf = R(0), cspf = R(0);
+  *dI = R(0);
+  for (int ch = 0; ch < 3; ++ch) {
+    R ld = R(p.light_diffuse[ch]), la = R(p.light_ambient[ch]), ls = R(p.light_specular[ch]);
+    R tfc = (&tf.x)[ch];
+    dtf[ch] = dcol[ch] * t.I * (ld * t.df + R(0.3) + la) * is;
+    *dI += dcol[ch] * (tfc * (ld * t.df + R(0.3) + la) + ls * t.spf) * is;
+    cdf += dcol[ch] * tfc * t.I * ld * is;
+    cspf += dcol[ch] * ls * t.I * is;
+  }
+  V3<R> gN{R(0), R(0), R(0)};
+  if (t.ln_in) gN = gN + t.L * (cdf * is);
+  if (t.rv_in && t.rlen > R(0) && cspf != R(0)) {
+    R e = R(p.spec_exp);
+    R dspf = cspf * e * std::pow(t.rv, e - R(1));
+    V3<R> gR = t.V * dspf;
+    /* R = r / |r| */
+    V3<R> gr = (gR - t.Rv * dot(t.Rv, gR)) * (R(1) / t.rlen);
+    /* r = 2 (L.N) N - L */
+    gN = gN + t.L * (R(2) * dot(t.N, gr)) + gr * (R(2) * t.ln);
+  }
+  V3<R> gm{R(0), R(0), R(0)};
+  if (t.mlen > R(0)) gm = (gN - t.N * dot(t.N, gN)) * (R(1) / t.mlen);
+  *dG = gm * R(-1);
 }
 
 /* One pixel: forward (storing every sample), then the reverse pass with cotangent g_out. */
@@ -1121,11 +1185,13 @@ template <class R> static inline void adjoint_pixel(const Inputs& in, const vvli
   V3<R> sv{u.scale_vol[0], u.scale_vol[1], u.scale_vol[2]};
   V3<R> pos = mul(V3<R>{o[0] + te * d[0], o[1] + te * d[1], o[2] + te * d[2]}, sv);
   V3<R> dir = mul(normalize(V3<R>{d[0], d[1], d[2]}), sv);
-  LicCtx<R> c{&in, &p, &u, false};
+  const bool lit = p.illum == VVLIC_ILLUM_GRADIENT;
+  LicCtx<R> c{&in, &p, &u, lit};
   struct Sample {
     V3<R> pos;
     V4<R> f;
     R I, idx;
+    V3<R> G;
   };
   std::vector<Sample> smp;
   V4<R> src{R(0), R(0), R(0), R(0)};
@@ -1137,7 +1203,7 @@ template <class R> static inline void adjoint_pixel(const Inputs& in, const vvli
       R idx = p.tf_index == VVLIC_TF_INDEX_MAGNITUDE ? f.w : f.z;
       V4<R> il = compute_lic<R>(c, pos, f);
       R I = il.w * u.intensity_scale;
-      smp.push_back(Sample{pos, f, I, idx});
+      smp.push_back(Sample{pos, f, I, idx, V3<R>{il.x, il.y, il.z}});
       /* shade to evaluate the termination test */
       Lookup<R> lt = lookup1d<R>(idx), lo = lookup1d<R>(I * R(1.3));
       R tfa = (R(1) - lt.t) * R(in.tf_rgba[4 * lt.i0 + 3]) + lt.t * R(in.tf_rgba[4 * lt.i1 + 3]);
@@ -1158,6 +1224,7 @@ template <class R> static inline void adjoint_pixel(const Inputs& in, const vvli
     V4<R> tf;
     R op, a0, base, alpha;
     V3<R> col;
+    Lit<R> lt3;
   };
   std::vector<Sh> sh(S);
   for (size_t k = 0; k < S; ++k) {
@@ -1170,8 +1237,17 @@ template <class R> static inline void adjoint_pixel(const Inputs& in, const vvli
     h.a0 = h.op * h.tf.w;
     h.base = R(1) - h.a0;
     h.alpha = R(1) - std::pow(h.base > R(0) ? h.base : R(0), u.alpha_correction);
-    h.col = V3<R>{smp[k].I * h.tf.x * u.illum_scale, smp[k].I * h.tf.y * u.illum_scale,
-                  smp[k].I * h.tf.z * u.illum_scale};
+    if (lit) {
+      h.lt3 = lit_setup<R>(c, smp[k].G, smp[k].I, smp[k].pos, dir);
+      R cc[3];
+      for (int ch = 0; ch < 3; ++ch)
+        cc[ch] = ((&h.tf.x)[ch] * smp[k].I * (R(p.light_diffuse[ch]) * h.lt3.df + R(0.3) + R(p.light_ambient[ch])) +
+                  R(p.light_specular[ch]) * h.lt3.spf * smp[k].I) * u.illum_scale;
+      h.col = V3<R>{cc[0], cc[1], cc[2]};
+    } else {
+      h.col = V3<R>{smp[k].I * h.tf.x * u.illum_scale, smp[k].I * h.tf.y * u.illum_scale,
+                    smp[k].I * h.tf.z * u.illum_scale};
+    }
     V4<R> s{h.col.x * h.alpha, h.col.y * h.alpha, h.col.z * h.alpha, h.alpha};
     R om = R(1) - D[k].w;
     D[k + 1] = V4<R>{clamp01(om * s.x + D[k].x), clamp01(om * s.y + D[k].y), clamp01(om * s.z + D[k].z),
@@ -1179,7 +1255,7 @@ template <class R> static inline void adjoint_pixel(const Inputs& in, const vvli
   }
   /* reverse */
   V4<R> g{R(g_out[0]), R(g_out[1]), R(g_out[2]), R(g_out[3])};
-  std::vector<R> n;
+  std::vector<V4<R>> n;
   for (size_t kk = S; kk-- > 0;) {
     const Sh& h = sh[kk];
     const V4<R>& Dp = D[kk];
@@ -1203,19 +1279,27 @@ template <class R> static inline void adjoint_pixel(const Inputs& in, const vvli
     out.opac[h.lo.i0] += double(dop * (R(1) - h.lo.t));
     out.opac[h.lo.i1] += double(dop * h.lo.t);
     R dI = dop * (R(in.tf_opac[h.lo.i1]) - R(in.tf_opac[h.lo.i0])) * h.lo.dvds_scale * R(1.3);
-    /* col = I * tf.rgb * illumScale */
-    R dtf[4] = {dcol[0] * smp[kk].I * u.illum_scale, dcol[1] * smp[kk].I * u.illum_scale,
-                dcol[2] * smp[kk].I * u.illum_scale, dtfa};
-    dI += (dcol[0] * h.tf.x + dcol[1] * h.tf.y + dcol[2] * h.tf.z) * u.illum_scale;
+    R dtf[4] = {R(0), R(0), R(0), dtfa};
+    V3<R> dG{R(0), R(0), R(0)};
+    if (lit) {
+      R dI_col;
+      lit_vjp<R>(c, h.lt3, h.tf, dcol, dtf, &dI_col, &dG);
+      dI += dI_col;
+    } else {
+      /* col = I * tf.rgb * illumScale */
+      for (int ch = 0; ch < 3; ++ch) dtf[ch] = dcol[ch] * smp[kk].I * u.illum_scale;
+      dI += (dcol[0] * h.tf.x + dcol[1] * h.tf.y + dcol[2] * h.tf.z) * u.illum_scale;
+    }
     for (int ch = 0; ch < 4; ++ch) {
       out.tf[4 * h.lt.i0 + ch] += double(dtf[ch] * (R(1) - h.lt.t));
       out.tf[4 * h.lt.i1 + ch] += double(dtf[ch] * h.lt.t);
     }
-    /* I = intensity_scale * sum_j w_j n_j */
+    /* I = intensity_scale * sum_j w_j n_j, G = sum_j w_j g_j */
     R dIraw = dI * u.intensity_scale;
-    if (dIraw != R(0)) {
+    if (dIraw != R(0) || dG.x != R(0) || dG.y != R(0) || dG.z != R(0)) {
       lic_noise_taps<R>(c, smp[kk].pos, smp[kk].f, n);
-      for (size_t j = 0; j < n.size(); ++j) out.taps[j] += double(dIraw * n[j]);
+      for (size_t j = 0; j < n.size(); ++j)
+        out.taps[j] += double(dIraw * n[j].w + dG.x * n[j].x + dG.y * n[j].y + dG.z * n[j].z);
     }
     g = gp;
   }

@@ -14,15 +14,23 @@ from vectorvisualization_gb300 import capi, workloads as wl
 pytestmark = pytest.mark.gpu
 
 
-def case(size=24, image=32, L=6, sampler="cell", storage="f32"):
+def case(size=24, image=32, L=6, sampler="cell", storage="f32", lit=False):
     w = wl.c4(size=size, image=image, views=1)
     w.params.steps_forward = w.params.steps_backward = L
     w.params.step_size_vol = 1.0 / 48.0
     w.params.gradient_scale = 8.0
     w.params.sampler = capi.SAMPLER[sampler]
+    if lit:  # illumGradient on central-difference noise gradients
+        w.params.illum = capi.ILLUM_GRADIENT
+        w.params.light_pos[:] = (0.2, 1.4, 1.1)
+        w.noise_mode = capi.NOISE_GRAD_CENTRAL
     w.storage = storage
     taps = np.linspace(0.5, 1.0, 2 * L + 1).astype(np.float64)
     return w, taps
+
+
+def scene_noise(oracle, w):
+    return w.noise if w.noise_mode == capi.NOISE_SCALAR else oracle.noise_gradients(w.noise, w.noise_mode)
 
 
 def gpu_forward_adjoint(ctx, w, taps, target, inv_area=0.7):
@@ -51,19 +59,21 @@ def target_image(oracle, w, taps, storage="f32"):
     if storage != "f32":
         enc = oracle.round_storage(enc, storage)
     rgba_t, op_t = wl.random_tf(seed=909)
-    sc = oracle.Scene(enc, w.noise, rgba_t, op_t, taps=taps[::-1].copy(), inv_filter_area=0.7)
+    sc = oracle.Scene(enc, scene_noise(oracle, w), rgba_t, op_t, taps=taps[::-1].copy(), inv_filter_area=0.7)
     return sc.render(w.params, w.views[0], w.width, w.height)[0]
 
 
-@pytest.mark.parametrize("sampler,storage", [("cell", "f32"), ("hybrid", "f16"), ("gather", "f32")])
-def test_adjoint_matches_fp64_oracle(ctx, oracle, sampler, storage):
-    w, taps = case(sampler=sampler, storage=storage)
+@pytest.mark.parametrize("sampler,storage,lit", [("cell", "f32", False), ("hybrid", "f16", False),
+                                                 ("gather", "f32", False), ("cell", "f32", True),
+                                                 ("hybrid", "f16", True)])
+def test_adjoint_matches_fp64_oracle(ctx, oracle, sampler, storage, lit):
+    w, taps = case(sampler=sampler, storage=storage, lit=lit)
     target = target_image(oracle, w, taps, storage)
     vid, img, d_tf, d_op, d_taps = gpu_forward_adjoint(ctx, w, taps, target)
     enc = oracle.encode_field(w.field)
     if storage != "f32":
         enc = oracle.round_storage(enc, storage)
-    sc = oracle.Scene(enc, w.noise, w.tf_rgba, w.tf_opac, taps=taps, inv_filter_area=0.7)
+    sc = oracle.Scene(enc, scene_noise(oracle, w), w.tf_rgba, w.tf_opac, taps=taps, inv_filter_area=0.7)
     ref_img, _ = sc.render(w.params, w.views[0], w.width, w.height)
     # the texture unit filters the field with 8-bit weights: its images (and so the gradients)
     # carry that error; the exact samplers are held to the tight bound
@@ -76,9 +86,11 @@ def test_adjoint_matches_fp64_oracle(ctx, oracle, sampler, storage):
         scale = max(float(np.abs(ref).max()), 1e-6)
         err = float(np.abs(got - ref).max())
         rel_l2 = float(np.linalg.norm(got - ref) / max(np.linalg.norm(ref), 1e-12))
-        print(f"adjoint {sampler}/{storage} {name}: max err {err:.3e} of scale {scale:.3e}, relative L2 {rel_l2:.3e}")
+        print(f"adjoint {sampler}/{storage}/{'lit' if lit else 'unlit'} {name}: max err {err:.3e} of scale "
+              f"{scale:.3e}, relative L2 {rel_l2:.3e}")
         if not hw:
-            assert err <= 2e-3 * scale, (name, err, scale)
+            # lit tapes hold the LIC gradient sum in FP16: the replayed normals carry its rounding
+            assert err <= (1e-2 if lit else 2e-3) * scale, (name, err, scale)
         else:
             # hardware filtering moves each sample's TF coordinate by a few hundredths of an
             # entry, which shifts gradient between neighbouring entries: compare the gradient
@@ -100,10 +112,11 @@ def test_adjoint_is_deterministic(ctx, oracle):
         np.testing.assert_array_equal(x, y)
 
 
-def test_adjoint_matches_gpu_finite_differences(ctx, oracle):
+@pytest.mark.parametrize("lit", [False, True])
+def test_adjoint_matches_gpu_finite_differences(ctx, oracle, lit):
     import torch
 
-    w, taps = case(size=32, image=40, L=8)
+    w, taps = case(size=32, image=40, L=8, lit=lit)
     target = target_image(oracle, w, taps)
     vid, img, d_tf, d_op, d_taps = gpu_forward_adjoint(ctx, w, taps, target)
     p = w.params

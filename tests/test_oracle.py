@@ -307,10 +307,14 @@ def test_row_subset_matches_full(oracle):
 # ---------------------------------------------------------------------------------------------
 # the FP64 adjoint against central finite differences of the FP64 forward
 # ---------------------------------------------------------------------------------------------
-def _adjoint_case(oracle):
+def _adjoint_case(oracle, lit=False):
     w = wl.c1(size=12, image=14)
     w.field = wl.vortex_field((12, 12, 12), seed=6)
     w.noise = wl.dense_noise(12, seed=61)
+    if lit:  # illumGradient on central-difference noise gradients
+        w.noise = oracle.noise_gradients(w.noise, capi.NOISE_GRAD_CENTRAL)
+        w.params.illum = capi.ILLUM_GRADIENT
+        w.params.light_pos[:] = (0.2, 1.4, 1.1)
     w.params.integrator = capi.HEUN
     w.params.steps_forward = w.params.steps_backward = 4
     w.params.gradient_scale = 6.0
@@ -328,8 +332,9 @@ def _adjoint_case(oracle):
     return w, view, enc, rgba, op, taps, target, render
 
 
-def test_oracle_adjoint_matches_finite_differences(oracle):
-    w, view, enc, rgba, op, taps, target, render = _adjoint_case(oracle)
+@pytest.mark.parametrize("lit", [False, True])
+def test_oracle_adjoint_matches_finite_differences(oracle, lit):
+    w, view, enc, rgba, op, taps, target, render = _adjoint_case(oracle, lit)
     img, sc = render(rgba, op, taps)
     g = (2.0 * (img - target)).astype(np.float32)
     d_tf, d_op, d_taps = oracle.adjoint(sc, w.params, view, w.width, w.height, g)

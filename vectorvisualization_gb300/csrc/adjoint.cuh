@@ -1,13 +1,14 @@
-// Adjoint of the unlit LIC ray-cast (illumLIC + front-to-back blend) with respect to the
-// transfer-function table (256 RGBA), the opacity table (256) and the filter taps.
+// Adjoint of the LIC ray-cast (illumLIC or illumGradient + front-to-back blend) with respect
+// to the transfer-function table (256 RGBA), the opacity table (256) and the filter taps.
 //
-// The forward render records a tape: per sample (intensity I, TF coordinate) and every
-// kSegment samples a checkpoint (position, dest before the sample).  Per ray this kernel walks
-// the segments last to first: it recomputes the segment's compositing states from its
-// checkpoint into a local array (cheap: no streamline work), then backpropagates sample by
-// sample through clamp, blend, alpha correction, the opacity lookup and the TF lookup.  The
-// intensity's cotangent is pushed onto the filter taps by walking the sample's streamlines once
-// more (dL/dw_j = S * sum_k dL/dI_k * n_kj).
+// The forward render records a tape: per sample (intensity I, TF coordinate), with gradient
+// lighting also the LIC gradient sum G (4 halves), and every kSegment samples a checkpoint
+// (position, dest before the sample).  Per ray this kernel walks the segments last to first: it
+// recomputes the segment's compositing states from its checkpoint into a local array (cheap:
+// no streamline work), then backpropagates sample by sample through clamp, blend, alpha
+// correction, the opacity lookup, the shading and the TF lookup.  The cotangents of I and G are
+// pushed onto the filter taps by walking the sample's streamlines once more
+// (dL/dw_j = sum_k S dL/dI_k n_kj + dL/dG_k . g_kj).
 //
 // Reductions are deterministic: per-tap sums are formed by a fixed-order warp butterfly, and
 // every contribution enters 64-bit fixed-point accumulators (scale 2^30) by integer atomics,
@@ -83,19 +84,84 @@ __device__ __forceinline__ float4 unlit_source_rgba(const RenderArgs& a, const f
   return make_float4(s.col.x, s.col.y, s.col.z, s.alpha);
 }
 
-// Walk the streamlines of the LIC at `pos` once more and add gI * n_j to the tap accumulators.
-// Every lane of the warp takes part in each reduction; lanes with gI == 0 skip the fetches.
-template <int ST, int FL, int NL, int INTEG>
-__device__ __forceinline__ void tap_gradients(const RenderArgs& a, float3 pos, float gI, long long* s_taps) {
-  const bool act = gI != 0.0f;
+// illumGradient (inc_illum.glsl:1-41) intermediates: N = n(-G), R = n(2 (L.N) N - L),
+// df = sat(L.N) * illumScale, spf = sat(R.V)^e.
+struct LitT {
+  float3 L, V, N, Rv;
+  float mlen, rlen, ln, rv, df, spf;
+};
+__device__ __forceinline__ LitT lit_setup(const RenderArgs& a, float3 G, float3 pos, float3 dir) {
+  LitT t;
+  t.L = light_dir(a, pos);
+  t.V = norm3(scl3(dir, -1.0f));
+  const float3 m = f3(-G.x, -G.y, -G.z);
+  t.mlen = sqrtf(dot3(m, m));
+  t.N = norm3(m);
+  t.ln = dot3(t.L, t.N);
+  const float3 r = sub3(scl3(t.N, 2.0f * t.ln), t.L);
+  t.rlen = sqrtf(dot3(r, r));
+  t.Rv = norm3(r);
+  t.rv = dot3(t.Rv, t.V);
+  t.spf = powf(__saturatef(t.rv), a.spec_exp);
+  t.df = __saturatef(t.ln) * a.illum_scale;
+  return t;
+}
+__device__ __forceinline__ float3 lit_color(const RenderArgs& a, const LitT& t, float4 tf, float I) {
+  return f3((tf.x * I * (a.light_diff[0] * t.df + 0.3f + a.light_amb[0]) + a.light_spec[0] * t.spf * I) * a.illum_scale,
+            (tf.y * I * (a.light_diff[1] * t.df + 0.3f + a.light_amb[1]) + a.light_spec[1] * t.spf * I) * a.illum_scale,
+            (tf.z * I * (a.light_diff[2] * t.df + 0.3f + a.light_amb[2]) + a.light_spec[2] * t.spf * I) * a.illum_scale);
+}
+// Reverse mode of lit_color for a colour cotangent dcol: dL/dtf.rgb, dL/dI, dL/dG.  sat() has
+// derivative 1 strictly inside (0, 1).
+__device__ __forceinline__ void lit_vjp(const RenderArgs& a, const LitT& t, float4 tf, float I, float3 dcol,
+                                        float dtf[3], float* dI, float3* dG) {
+  const float is = a.illum_scale;
+  const float d[3] = {dcol.x, dcol.y, dcol.z}, tfc[3] = {tf.x, tf.y, tf.z};
+  float cdf = 0.0f, cspf = 0.0f, di = 0.0f;
+#pragma unroll
+  for (int ch = 0; ch < 3; ++ch) {
+    const float k = a.light_diff[ch] * t.df + 0.3f + a.light_amb[ch];
+    dtf[ch] = d[ch] * I * k * is;
+    di += d[ch] * (tfc[ch] * k + a.light_spec[ch] * t.spf) * is;
+    cdf += d[ch] * tfc[ch] * I * a.light_diff[ch] * is;
+    cspf += d[ch] * a.light_spec[ch] * I * is;
+  }
+  *dI = di;
+  float3 gN = f3(0.f, 0.f, 0.f);
+  if (t.ln > 0.0f && t.ln < 1.0f) gN = scl3(t.L, cdf * is);
+  if (t.rv > 0.0f && t.rv < 1.0f && t.rlen > 0.0f && cspf != 0.0f) {
+    const float dspf = cspf * a.spec_exp * powf(t.rv, a.spec_exp - 1.0f);
+    const float3 gR = scl3(t.V, dspf);
+    const float3 gr = scl3(sub3(gR, scl3(t.Rv, dot3(t.Rv, gR))), 1.0f / t.rlen);
+    gN = add3(gN, add3(scl3(t.L, 2.0f * dot3(t.N, gr)), scl3(gr, 2.0f * t.ln)));
+  }
+  *dG = t.mlen > 0.0f ? scl3(sub3(gN, scl3(t.N, dot3(t.N, gN))), -1.0f / t.mlen) : f3(0.f, 0.f, 0.f);
+}
+__device__ __forceinline__ float3 tape_gradient(const RenderArgs& a, size_t idx) {
+  const uint2 v = a.tape_g[idx];
+  const float2 xy = __half22float2(*reinterpret_cast<const __half2*>(&v.x));
+  const float2 z0 = __half22float2(*reinterpret_cast<const __half2*>(&v.y));
+  return f3(xy.x, xy.y, z0.x);
+}
+
+// Walk the streamlines of the LIC at `pos` once more and add gI * n_j (+ gG . g_j with noise
+// gradients) to the tap accumulators.  Every lane of the warp takes part in each reduction;
+// lanes with zero cotangents skip the fetches.
+template <int ST, int FL, int NL, int INTEG, bool GRAD>
+__device__ __forceinline__ float tap_dot(float4 n, float gI, float3 gG) {
+  return GRAD ? fmaf(gI, n.w, gG.x * n.x + gG.y * n.y + gG.z * n.z) : gI * n.w;
+}
+template <int ST, int FL, int NL, int INTEG, bool GRAD>
+__device__ __forceinline__ void tap_gradients(const RenderArgs& a, float3 pos, float gI, float3 gG, long long* s_taps) {
+  const bool act = gI != 0.0f || (GRAD && (gG.x != 0.0f || gG.y != 0.0f || gG.z != 0.0f));
   const int lb = a.lb, lf = a.lf, L = max(lb, lf);
   float4 f0 = make_float4(0.f, 0.f, 0.f, 0.f);
-  float n0 = 0.0f;
+  float v0 = 0.0f;
   if (act) {
     f0 = Field<ST, FL>::sample(a, pos);
-    n0 = noise_tap<NL, false>(a, pos).w;
+    v0 = tap_dot<ST, FL, NL, INTEG, GRAD>(noise_tap<NL, GRAD>(a, pos), gI, gG);
   }
-  warp_fixed_add(s_taps + lb, gI * n0);
+  warp_fixed_add(s_taps + lb, v0);
   float3 pb = pos, pf = pos;
   float4 sb = f0, sf = f0;
   for (int i = 1; i <= L; ++i) {
@@ -103,11 +169,11 @@ __device__ __forceinline__ void tap_gradients(const RenderArgs& a, float3 pos, f
     if (act) {
       if (i <= lb) {
         pb = lic_step<ST, FL, INTEG>(a, pb, sb, -1.0f);
-        vb = gI * noise_tap<NL, false>(a, pb).w;
+        vb = tap_dot<ST, FL, NL, INTEG, GRAD>(noise_tap<NL, GRAD>(a, pb), gI, gG);
       }
       if (i <= lf) {
         pf = lic_step<ST, FL, INTEG>(a, pf, sf, 1.0f);
-        vf = gI * noise_tap<NL, false>(a, pf).w;
+        vf = tap_dot<ST, FL, NL, INTEG, GRAD>(noise_tap<NL, GRAD>(a, pf), gI, gG);
       }
     }
     if (i <= lb) warp_fixed_add(s_taps + lb - i, vb);
@@ -115,7 +181,7 @@ __device__ __forceinline__ void tap_gradients(const RenderArgs& a, float3 pos, f
   }
 }
 
-template <int ST, int FL, int NL, int INTEG>
+template <int ST, int FL, int NL, int INTEG, bool GRAD>
 __global__ void __launch_bounds__(kThreads) adjoint_kernel(const __grid_constant__ RenderArgs a,
                                                            const float4* __restrict__ g_img, long long* acc,
                                                            const uint32_t* __restrict__ order, int ntiles,
@@ -159,18 +225,34 @@ __global__ void __launch_bounds__(kThreads) adjoint_kernel(const __grid_constant
         for (int kk = 0; kk < cnt; ++kk) {
           Ploc[kk] = p;
           Dloc[kk] = D;
-          const float2 rec = a.tape_is[ray * a.tape_stride + seg * kSegment + kk];
-          D = blend(D, unlit_source_rgba(a, s_tf, rec.x, rec.y));
+          const size_t idx = ray * a.tape_stride + seg * kSegment + kk;
+          const float2 rec = a.tape_is[idx];
+          float4 src;
+          if (GRAD) {
+            const Src us = unlit_source(a, s_tf, rec.x, rec.y);
+            const float3 col = lit_color(a, lit_setup(a, tape_gradient(a, idx), p, dir), us.tf, rec.x);
+            src = make_float4(col.x, col.y, col.z, us.alpha);
+          } else {
+            src = unlit_source_rgba(a, s_tf, rec.x, rec.y);
+          }
+          D = blend(D, src);
           p = add3(p, scl3(dir, a.step_size));
         }
       }
       for (int kk = kSegment - 1; kk >= 0; --kk) {
         float gIraw = 0.0f;
+        float3 gG = f3(0.f, 0.f, 0.f);
         float3 pk = f3(0.f, 0.f, 0.f);
         if (kk < cnt) {
-          const float2 rec = a.tape_is[ray * a.tape_stride + seg * kSegment + kk];
+          const size_t idx = ray * a.tape_stride + seg * kSegment + kk;
+          const float2 rec = a.tape_is[idx];
           const float I = rec.x;
-          const Src s = unlit_source(a, s_tf, I, rec.y);
+          Src s = unlit_source(a, s_tf, I, rec.y);
+          LitT lt;
+          if (GRAD) {
+            lt = lit_setup(a, tape_gradient(a, idx), Ploc[kk], dir);
+            s.col = lit_color(a, lt, s.tf, I);
+          }
           const float4 sv = premultiplied(s);
           const float4 Dp = Dloc[kk];
           pk = Ploc[kk];
@@ -194,10 +276,19 @@ __global__ void __launch_bounds__(kThreads) adjoint_kernel(const __grid_constant
           fixed_add(s_acc + kAccOpac + s.lo.i1, dop * s.lo.t);
           const float* op = s_tf + 4 * VVLIC_TF_ENTRIES;
           float dI = s.lo.inside ? dop * (op[s.lo.i1] - op[s.lo.i0]) * (float)VVLIC_TF_ENTRIES * 1.3f : 0.0f;
-          // col = I * tf.rgb * illumScale
-          const float ci = I * a.illum_scale;
-          const float dtf[4] = {dcx * ci, dcy * ci, dcz * ci, dtfa};
-          dI += (dcx * s.tf.x + dcy * s.tf.y + dcz * s.tf.z) * a.illum_scale;
+          float dtf[4];
+          dtf[3] = dtfa;
+          if (GRAD) {
+            float dIc;
+            lit_vjp(a, lt, s.tf, I, f3(dcx, dcy, dcz), dtf, &dIc, &gG);
+            dI += dIc;
+          } else {  // col = I * tf.rgb * illumScale
+            const float ci = I * a.illum_scale;
+            dtf[0] = dcx * ci;
+            dtf[1] = dcy * ci;
+            dtf[2] = dcz * ci;
+            dI += (dcx * s.tf.x + dcy * s.tf.y + dcz * s.tf.z) * a.illum_scale;
+          }
 #pragma unroll
           for (int ch = 0; ch < 4; ++ch) {
             fixed_add(s_acc + kAccTF + 4 * s.lt.i0 + ch, dtf[ch] * (1.0f - s.lt.t));
@@ -206,7 +297,8 @@ __global__ void __launch_bounds__(kThreads) adjoint_kernel(const __grid_constant
           gIraw = dI * a.intensity_scale;
           g = gp;
         }
-        if (__any_sync(0xffffffffu, gIraw != 0.0f)) tap_gradients<ST, FL, NL, INTEG>(a, pk, gIraw, s_acc + kAccTaps);
+        const bool need = gIraw != 0.0f || (GRAD && (gG.x != 0.0f || gG.y != 0.0f || gG.z != 0.0f));
+        if (__any_sync(0xffffffffu, need)) tap_gradients<ST, FL, NL, INTEG, GRAD>(a, pk, gIraw, gG, s_acc + kAccTaps);
       }
     }
   }
@@ -215,10 +307,10 @@ __global__ void __launch_bounds__(kThreads) adjoint_kernel(const __grid_constant
     if (s_acc[i] != 0) atomicAdd(reinterpret_cast<unsigned long long*>(acc + i), (unsigned long long)s_acc[i]);
 }
 
-template <int ST, int FL, int NL, int INTEG>
+template <int ST, int FL, int NL, int INTEG, bool GRAD>
 static cudaError_t launch_adjoint_one(const RenderArgs& a, const float4* g_img, long long* acc, const Schedule& sch,
                                       cudaStream_t s) {
-  auto kern = adjoint_kernel<ST, FL, NL, INTEG>;
+  auto kern = adjoint_kernel<ST, FL, NL, INTEG, GRAD>;
   int per_sm = 0;
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, 0);
   if (e != cudaSuccess) return e;
@@ -226,26 +318,33 @@ static cudaError_t launch_adjoint_one(const RenderArgs& a, const float4* g_img, 
   return cudaGetLastError();
 }
 
+template <int ST, int FL, int NL, bool GRAD>
+static cudaError_t launch_adjoint_integ(const RenderArgs& a, int integ, const float4* g_img, long long* acc,
+                                        const Schedule& sch, cudaStream_t s) {
+  if (integ == VVLIC_EULER) return launch_adjoint_one<ST, FL, NL, VVLIC_EULER, GRAD>(a, g_img, acc, sch, s);
+  if (integ == VVLIC_HEUN) return launch_adjoint_one<ST, FL, NL, VVLIC_HEUN, GRAD>(a, g_img, acc, sch, s);
+  return launch_adjoint_one<ST, FL, NL, VVLIC_RK4, GRAD>(a, g_img, acc, sch, s);
+}
+
 template <int ST, int FL, int NL>
-static cudaError_t launch_adjoint_layout(const RenderArgs& a, int integ, const float4* g_img, long long* acc,
-                                         const Schedule& sch, cudaStream_t s) {
-  if (integ == VVLIC_EULER) return launch_adjoint_one<ST, FL, NL, VVLIC_EULER>(a, g_img, acc, sch, s);
-  if (integ == VVLIC_HEUN) return launch_adjoint_one<ST, FL, NL, VVLIC_HEUN>(a, g_img, acc, sch, s);
-  return launch_adjoint_one<ST, FL, NL, VVLIC_RK4>(a, g_img, acc, sch, s);
+static cudaError_t launch_adjoint_layout(const RenderArgs& a, int integ, bool lit, const float4* g_img,
+                                         long long* acc, const Schedule& sch, cudaStream_t s) {
+  return lit ? launch_adjoint_integ<ST, FL, NL, true>(a, integ, g_img, acc, sch, s)
+             : launch_adjoint_integ<ST, FL, NL, false>(a, integ, g_img, acc, sch, s);
 }
 
 template <int ST>
-static cudaError_t launch_adjoint_storage(const RenderArgs& a, int sampler, int integ, const float4* g_img,
-                                         long long* acc, const Schedule& sch, cudaStream_t s) {
+static cudaError_t launch_adjoint_storage(const RenderArgs& a, int sampler, int integ, bool lit, const float4* g_img,
+                                          long long* acc, const Schedule& sch, cudaStream_t s) {
   switch (sampler) {
-    case VVLIC_SAMPLER_GATHER: return launch_adjoint_layout<ST, kGather, kGather>(a, integ, g_img, acc, sch, s);
-    case VVLIC_SAMPLER_CELL: return launch_adjoint_layout<ST, kCell, kCell>(a, integ, g_img, acc, sch, s);
+    case VVLIC_SAMPLER_GATHER: return launch_adjoint_layout<ST, kGather, kGather>(a, integ, lit, g_img, acc, sch, s);
+    case VVLIC_SAMPLER_CELL: return launch_adjoint_layout<ST, kCell, kCell>(a, integ, lit, g_img, acc, sch, s);
     case VVLIC_SAMPLER_TEXTURE:
       if constexpr (ST == VVLIC_STORAGE_BF16) return cudaErrorNotSupported;
-      else return launch_adjoint_layout<ST, kTexture, kTexture>(a, integ, g_img, acc, sch, s);
+      else return launch_adjoint_layout<ST, kTexture, kTexture>(a, integ, lit, g_img, acc, sch, s);
     case VVLIC_SAMPLER_HYBRID:
       if constexpr (ST == VVLIC_STORAGE_BF16) return cudaErrorNotSupported;
-      else return launch_adjoint_layout<ST, kTexture, kCell>(a, integ, g_img, acc, sch, s);
+      else return launch_adjoint_layout<ST, kTexture, kCell>(a, integ, lit, g_img, acc, sch, s);
     default: return cudaErrorInvalidValue;
   }
 }

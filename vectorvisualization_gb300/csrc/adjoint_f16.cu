@@ -3,9 +3,9 @@
 
 namespace vvlic {
 
-cudaError_t launch_adjoint_f16(const RenderArgs& a, int sampler, int integ, const float4* g_img, long long* acc,
-                               const Schedule& sch, cudaStream_t s) {
-  return launch_adjoint_storage<VVLIC_STORAGE_F16>(a, sampler, integ, g_img, acc, sch, s);
+cudaError_t launch_adjoint_f16(const RenderArgs& a, int sampler, int integ, bool lit, const float4* g_img,
+                               long long* acc, const Schedule& sch, cudaStream_t s) {
+  return launch_adjoint_storage<VVLIC_STORAGE_F16>(a, sampler, integ, lit, g_img, acc, sch, s);
 }
 
 }  // namespace vvlic

@@ -347,9 +347,10 @@ vvlic_status prepare_tape(vvlic_ctx* c, const Geometry& gm, int w, int h, Render
   const int stride = std::max(1, (int)std::ceil(bound));
   const int nck = (stride + kSegment - 1) / kSegment;
   const size_t rays = (size_t)w * h;
+  const bool lit = a.illum == VVLIC_ILLUM_GRADIENT;
   const size_t b_is = rays * stride * sizeof(float2), b_ck = rays * nck * 2 * sizeof(float4),
-               b_n = rays * sizeof(uint32_t);
-  const size_t bytes = b_ck + b_is + b_n;
+               b_g = lit ? rays * stride * sizeof(uint2) : 0, b_n = rays * sizeof(uint32_t);
+  const size_t bytes = b_ck + b_is + b_g + b_n;
   if (c->tape_cap < bytes) {
     if (c->d_tape) cudaFree(c->d_tape);
     c->d_tape = nullptr;
@@ -365,7 +366,8 @@ vvlic_status prepare_tape(vvlic_ctx* c, const Geometry& gm, int w, int h, Render
   char* base = (char*)c->d_tape;
   a.tape_ck = (float4*)base;
   a.tape_is = (float2*)(base + b_ck);
-  a.tape_n = (uint32_t*)(base + b_ck + b_is);
+  a.tape_g = lit ? (uint2*)(base + b_ck + b_is) : nullptr;
+  a.tape_n = (uint32_t*)(base + b_ck + b_is + b_g);
   a.tape_overflow = c->d_tape_flag;
   a.tape_stride = stride;
   a.tape_nck = nck;
@@ -484,8 +486,9 @@ extern "C" vvlic_status vvlic_render_adjoint(vvlic_ctx* c, int32_t vol_id, const
     return fail(c, VVLIC_ERR_NOT_READY,
                 "render_adjoint: the last render of this context did not record a tape for volume %d at %dx%d "
                 "(set params.record_tape)", vol_id, w, h);
-  if (c->tape_illum != VVLIC_ILLUM_NONE)
-    return fail(c, VVLIC_ERR_UNSUPPORTED, "render_adjoint: only the unlit shading (illumLIC) is differentiated");
+  if (c->tape_illum != VVLIC_ILLUM_NONE && c->tape_illum != VVLIC_ILLUM_GRADIENT)
+    return fail(c, VVLIC_ERR_UNSUPPORTED,
+                "render_adjoint: only illumLIC and illumGradient shading are differentiated");
   if (c->vols.find(vol_id) == c->vols.end())
     return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "render_adjoint: unknown volume %d", vol_id);
   DeviceGuard g(c->device);
@@ -506,11 +509,14 @@ extern "C" vvlic_status vvlic_render_adjoint(vvlic_ctx* c, int32_t vol_id, const
   e = cudaEventRecord(c->ev0, s);
   const float4* gi = (const float4*)d_dl_drgba;
   if (e == cudaSuccess) {
+    const bool lit = c->tape_illum == VVLIC_ILLUM_GRADIENT;
     switch (c->tape_storage) {
-      case VVLIC_STORAGE_F32: e = launch_adjoint_f32(a, c->tape_sampler, c->tape_integ, gi, c->d_acc, sch, s); break;
-      case VVLIC_STORAGE_F16: e = launch_adjoint_f16(a, c->tape_sampler, c->tape_integ, gi, c->d_acc, sch, s); break;
-      case VVLIC_STORAGE_UNORM8: e = launch_adjoint_u8(a, c->tape_sampler, c->tape_integ, gi, c->d_acc, sch, s); break;
-      default: e = launch_adjoint_bf16(a, c->tape_sampler, c->tape_integ, gi, c->d_acc, sch, s); break;
+      case VVLIC_STORAGE_F32: e = launch_adjoint_f32(a, c->tape_sampler, c->tape_integ, lit, gi, c->d_acc, sch, s); break;
+      case VVLIC_STORAGE_F16: e = launch_adjoint_f16(a, c->tape_sampler, c->tape_integ, lit, gi, c->d_acc, sch, s); break;
+      case VVLIC_STORAGE_UNORM8:
+        e = launch_adjoint_u8(a, c->tape_sampler, c->tape_integ, lit, gi, c->d_acc, sch, s);
+        break;
+      default: e = launch_adjoint_bf16(a, c->tape_sampler, c->tape_integ, lit, gi, c->d_acc, sch, s); break;
     }
   }
   if (e == cudaSuccess) e = cudaEventRecord(c->ev1, s);

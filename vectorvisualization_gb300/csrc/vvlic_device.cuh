@@ -50,6 +50,7 @@ struct RenderArgs {
   // (intensity, TF coordinate), `tape_nck` checkpoints of (position, dest before the sample)
   // every kSegment samples, and the sample count
   float2* tape_is;
+  uint2* tape_g;  // gradient lighting only: per sample the LIC gradient sum G as 4 halves (x, y, z, 0)
   float4* tape_ck;
   uint32_t* tape_n;
   unsigned long long* tape_overflow;  // rays with more samples than tape_stride
@@ -651,7 +652,14 @@ __device__ __forceinline__ float4 trace_pixel(const RenderArgs& a, const float* 
           ck[0] = make_float4(pos.x, pos.y, pos.z, 0.f);
           ck[1] = dest;
         }
-        if (samples < (uint32_t)a.tape_stride) a.tape_is[ray * a.tape_stride + samples] = make_float2(il.w, tfc);
+        if (samples < (uint32_t)a.tape_stride) {
+          a.tape_is[ray * a.tape_stride + samples] = make_float2(il.w, tfc);
+          if (GRAD) {
+            const __half2 xy = __floats2half2_rn(il.x, il.y), z0 = __floats2half2_rn(il.z, 0.0f);
+            a.tape_g[ray * a.tape_stride + samples] =
+                make_uint2(*reinterpret_cast<const unsigned*>(&xy), *reinterpret_cast<const unsigned*>(&z0));
+          }
+        }
       }
       ++samples;
       src = shade<GRAD>(a, s_tf, il, tf, pos, dir, f);

@@ -40,16 +40,16 @@ cudaError_t launch_raycast_bf16(const RenderArgs& a, int sampler, int integ, boo
 cudaError_t launch_raycast_u8(const RenderArgs& a, int sampler, int integ, bool grad, const Schedule& sch,
                               cudaStream_t s);
 
-// Adjoint of the unlit render (adjoint_<storage>.cu): accumulates 64-bit fixed-point
-// gradients into acc (TF 1024, opacity 256, taps).
-cudaError_t launch_adjoint_f32(const RenderArgs& a, int sampler, int integ, const float4* g_img, long long* acc,
-                               const Schedule& sch, cudaStream_t s);
-cudaError_t launch_adjoint_f16(const RenderArgs& a, int sampler, int integ, const float4* g_img, long long* acc,
-                               const Schedule& sch, cudaStream_t s);
-cudaError_t launch_adjoint_bf16(const RenderArgs& a, int sampler, int integ, const float4* g_img, long long* acc,
-                                const Schedule& sch, cudaStream_t s);
-cudaError_t launch_adjoint_u8(const RenderArgs& a, int sampler, int integ, const float4* g_img, long long* acc,
-                              const Schedule& sch, cudaStream_t s);
+// Adjoint of the unlit (lit == false) or gradient-lit render (adjoint_<storage>.cu):
+// accumulates 64-bit fixed-point gradients into acc (TF 1024, opacity 256, taps).
+cudaError_t launch_adjoint_f32(const RenderArgs& a, int sampler, int integ, bool lit, const float4* g_img,
+                               long long* acc, const Schedule& sch, cudaStream_t s);
+cudaError_t launch_adjoint_f16(const RenderArgs& a, int sampler, int integ, bool lit, const float4* g_img,
+                               long long* acc, const Schedule& sch, cudaStream_t s);
+cudaError_t launch_adjoint_bf16(const RenderArgs& a, int sampler, int integ, bool lit, const float4* g_img,
+                                long long* acc, const Schedule& sch, cudaStream_t s);
+cudaError_t launch_adjoint_u8(const RenderArgs& a, int sampler, int integ, bool lit, const float4* g_img,
+                              long long* acc, const Schedule& sch, cudaStream_t s);
 
 // Batched render (batch_<storage>.cu): one persistent launch over (job, tile) items.
 struct BatchLaunch {
