@@ -300,6 +300,26 @@ def test_scalar_gate(ctx, oracle):
     assert rmse(img, ref) <= RMSE_TOL
 
 
+def test_table_updates_wait_for_renders_in_flight(ctx):
+    """set_tf right after an asynchronous render on another stream applies to later renders only."""
+    import torch
+
+    w = small()
+    w.width = w.height = 192
+    w.params.steps_forward = w.params.steps_backward = 24
+    vid = wl.setup_context(ctx, w)
+    ref = ctx.render(vid, w.width, w.height)
+    stream = torch.cuda.Stream()
+    out = torch.empty((w.height, w.width, 4), dtype=torch.float32, device="cuda")
+    other = wl.random_tf(seed=3)
+    for _ in range(3):
+        ctx.render_device(vid, out.data_ptr(), w.width, w.height, None, stream.cuda_stream)
+        ctx.set_tf(*other)  # must not reach the render above
+        stream.synchronize()
+        np.testing.assert_array_equal(out.cpu().numpy(), ref)
+        ctx.set_tf(w.tf_rgba, w.tf_opac)
+
+
 def test_views_that_miss_give_zero(ctx, oracle):
     w = small()
     vid = wl.setup_context(ctx, w)

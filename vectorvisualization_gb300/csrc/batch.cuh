@@ -44,7 +44,7 @@ __global__ void __launch_bounds__(kThreads, VVLIC_MIN_BLOCKS)
     const int py = (int)(item.y / tiles_x) * th + lane / tw;
     if (px < a.W && py < a.H) {
       uint32_t samples, hit;
-      float4 dest = trace_pixel<ST, FL, NL, INTEG, GRAD>(a, s_tf, px, py, samples, hit);
+      float4 dest = trace_ray<ST, FL, NL, INTEG, GRAD>(a, s_tf, px, py, samples, hit);
       store_pixel(a, px, py, dest, samples);
       samples_acc += samples;
       hits_acc += hit;

@@ -608,6 +608,13 @@ extern "C" vvlic_status vvlic_upload_scalar(vvlic_ctx* c, const float* scalar, i
   return VVLIC_OK;
 }
 
+namespace vvlic {
+// The device tables (TF, line-illumination tables) are read by kernels still in flight on the
+// caller's streams.  An update is ordered after the context's last launch (every launch records
+// ev1 on its stream), so it applies to later renders only, as a GL state change does.
+cudaError_t after_launches(vvlic_ctx* c) { return cudaStreamWaitEvent(c->stream, c->ev1, 0); }
+}  // namespace vvlic
+
 extern "C" vvlic_status vvlic_set_tf(vvlic_ctx* c, const float* rgba, const float* opacity) {
   if (!c) return VVLIC_ERR_BAD_HANDLE;
   if (rgba) std::memcpy(c->tf, rgba, sizeof(float) * 4 * VVLIC_TF_ENTRIES);
@@ -615,8 +622,9 @@ extern "C" vvlic_status vvlic_set_tf(vvlic_ctx* c, const float* rgba, const floa
   for (int i = 0; i < 5 * VVLIC_TF_ENTRIES; ++i)
     if (!std::isfinite(c->tf[i])) return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "set_tf: non-finite entry %d", i);
   DeviceGuard g(c->device);
-  cudaError_t e = cudaMemcpyAsync(c->d_tf, c->tf, sizeof(float) * 5 * VVLIC_TF_ENTRIES, cudaMemcpyHostToDevice,
-                                  c->stream);
+  cudaError_t e = after_launches(c);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(c->d_tf, c->tf, sizeof(float) * 5 * VVLIC_TF_ENTRIES, cudaMemcpyHostToDevice, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "set_tf");
   return VVLIC_OK;

@@ -104,17 +104,15 @@ vvlic_status ensure_illum_luts(vvlic_ctx* c) {
   std::vector<uint8_t> host(bytes);
   build_illum_luts(c->line_mat, w, h, host.data());
   if (c->lut_bytes < bytes) {
-    if (c->d_luts) {
-      cudaStreamSynchronize(c->stream);  // a render may still read the old tables
-      cudaFree(c->d_luts);
-    }
+    if (c->d_luts) cudaFree(c->d_luts);  // cudaFree waits for the kernels that read the old tables
     c->d_luts = nullptr;
     c->lut_bytes = 0;
     cudaError_t e = cudaMalloc(&c->d_luts, bytes);
     if (e != cudaSuccess) return cuda_fail(c, e, "illumination tables");
     c->lut_bytes = bytes;
   }
-  cudaError_t e = cudaMemcpyAsync(c->d_luts, host.data(), bytes, cudaMemcpyHostToDevice, c->stream);
+  cudaError_t e = after_launches(c);  // renders in flight may read the old tables
+  if (e == cudaSuccess) e = cudaMemcpyAsync(c->d_luts, host.data(), bytes, cudaMemcpyHostToDevice, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);  // `host` is pageable and local
   if (e != cudaSuccess) return cuda_fail(c, e, "illumination tables upload");
   c->lut_w = w;

@@ -55,7 +55,7 @@ __global__ void __launch_bounds__(kThreads, VVLIC_MIN_BLOCKS) raycast_kernel(con
   const int py = blockIdx.y * kTileH + (threadIdx.x / kTileW);
   uint32_t samples = 0, hit = 0;
   if (px < a.W && py < a.H) {
-    float4 dest = trace_pixel<ST, FL, NL, INTEG, GRAD>(a, s_tf, px, py, samples, hit);
+    float4 dest = trace_ray<ST, FL, NL, INTEG, GRAD>(a, s_tf, px, py, samples, hit);
     store_pixel(a, px, py, dest, samples);
   }
   flush_counters(a, samples, hit);
@@ -80,7 +80,7 @@ __global__ void __launch_bounds__(kThreads, VVLIC_MIN_BLOCKS) raycast_queue_kern
     const int py = (int)(tile / tiles_x) * kWarpTileH + (lane / kWarpTileW);
     if (px < a.W && py < a.H) {
       uint32_t samples, hit;
-      float4 dest = trace_pixel<ST, FL, NL, INTEG, GRAD>(a, s_tf, px, py, samples, hit);
+      float4 dest = trace_ray<ST, FL, NL, INTEG, GRAD>(a, s_tf, px, py, samples, hit);
       store_pixel(a, px, py, dest, samples);
       samples_acc += samples;
       hits_acc += hit;

@@ -143,6 +143,8 @@ namespace vvlic {
 vvlic_status fail(vvlic_ctx* c, vvlic_status s, const char* fmt, ...);
 // Builds (first use, or after a material change) and uploads the line-illumination tables.
 vvlic_status ensure_illum_luts(vvlic_ctx* c);
+// Orders the context stream after the context's last launch (device-table updates).
+cudaError_t after_launches(vvlic_ctx* c);
 vvlic_status cuda_fail(vvlic_ctx* c, cudaError_t e, const char* what);
 Geometry make_geometry(const int n[3], const float* slice_dist);
 vvlic_status derive_taps(const vvlic_ctx* c, int lb, int lf, float* taps, float* inv_area);
