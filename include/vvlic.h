@@ -344,10 +344,12 @@ vvlic_status vvlic_render_device(vvlic_ctx* ctx, int32_t vol_id, float* d_out_rg
  * size with params.record_tape = 1; that render recorded, per ray sample, the LIC intensity and
  * TF coordinate (with VVLIC_ILLUM_GRADIENT also the LIC gradient sum, in FP16) and, every 32
  * samples, a compositing checkpoint: 8 B (16 B lit) per sample of the longest possible ray for
- * every pixel.  Shading VVLIC_ILLUM_NONE or VVLIC_ILLUM_GRADIENT (illumGradient differentiated
- * through the normal, the diffuse and the specular term); other models return
- * VVLIC_ERR_UNSUPPORTED.  Results are deterministic (fixed-point accumulation); they are NaN if
- * the tape was too short for a ray.  Asynchronous on `stream`. */
+ * every pixel.  Every shading model is differentiated: illumGradient through the normal, the
+ * diffuse and the specular term; illumZoeckler / illumMallo through the TF colour and the
+ * intensity (their table factors do not depend on TF or taps).  The TF, line material and
+ * volume must not change between the recording render and this call.  Results are
+ * deterministic (fixed-point accumulation); they are NaN if the tape was too short for a ray.
+ * Asynchronous on `stream`. */
 vvlic_status vvlic_render_adjoint(vvlic_ctx* ctx, int32_t vol_id, const float* d_dl_drgba, int32_t w, int32_t h,
                                   float* d_dl_dtf, float* d_dl_dopacity, float* d_dl_dtaps, void* stream);
 

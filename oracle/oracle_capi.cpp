@@ -191,7 +191,6 @@ int32_t vvo_lic_volume(const vvo_inputs* vi, const vvlic_params* p, const int32_
  * dL/dtaps (L_b+L_f+1) for the image cotangent g_img (h*w*4). */
 int32_t vvo_adjoint(const vvo_inputs* vi, const vvlic_params* p, const double* ray_coeffs, int32_t w, int32_t h,
                     const float* g_img, double* d_tf, double* d_opac, double* d_taps, int32_t threads) {
-  if (p->illum != VVLIC_ILLUM_NONE && p->illum != VVLIC_ILLUM_GRADIENT) return -2;
   int lb, lf;
   int ntaps = effective_steps(p, &lb, &lf);
   std::vector<double> taps(ntaps);
@@ -219,6 +218,10 @@ int32_t vvo_adjoint(const vvo_inputs* vi, const vvlic_params* p, const double* r
   in.tf_opac = vi->tf_opac;
   in.taps = taps.data();
   in.inv_filter_area = inv_area;
+  in.luts = vi->luts;
+  in.lut_w = vi->lut_w;
+  in.lut_h = vi->lut_h;
+  if ((p->illum == VVLIC_ILLUM_ZOECKLER || p->illum == VVLIC_ILLUM_MALLO) && !in.luts) return -5;
   vvo::AdjointOut out{d_tf, d_opac, d_taps};
   vvo::adjoint<double>(in, *p, ray_coeffs, w, h, g_img, out, threads);
   return 0;

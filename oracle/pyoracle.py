@@ -256,7 +256,9 @@ class Scene:
 
 def adjoint(scene: "Scene", params: capi.Params, view: capi.View, w: int, h: int, g_img: np.ndarray,
             threads: int = 0):
-    """FP64 adjoint of the unlit render: (dL/dTF (256,4), dL/dopacity (256,), dL/dtaps)."""
+    """FP64 adjoint of the render: (dL/dTF (256,4), dL/dopacity (256,), dL/dtaps)."""
+    if params.illum in (capi.ILLUM_ZOECKLER, capi.ILLUM_MALLO) and not scene.inputs.luts:
+        scene.attach_line_material()
     rc = view_rays(view, scene.dims, w, h, list(scene.inputs.slice_dist))
     g = np.ascontiguousarray(g_img, dtype=np.float32).reshape(h, w, 4)
     lb, lf = (15, 15) if params.low_res else (params.steps_backward, params.steps_forward)

@@ -778,6 +778,44 @@ template <class R> static inline V3<R> cross(V3<R> a, V3<R> b) {
 /* clamp to [0, 1] with NaN -> 0 */
 template <class R> static inline R sat_nan0(R v) { return std::fmin(std::fmax(v, R(0)), R(1)); }
 
+/* illumZoeckler (inc_illum.glsl:117-154) / illumMallo (:46-112) as colour = tf.rgb I d + s, with
+ * d and s from the line tables; f = vectorData at pos, its encoded rgb the streamline tangent. */
+template <class R>
+static inline void line_factors(const LicCtx<R>& c, V3<R> pos, V3<R> dir, V4<R> f, R d[3], R sp[3]) {
+  const Uniforms<R>& u = *c.u;
+  const vvlic_params& p = *c.p;
+  const Inputs& in = *c.in;
+  V3<R> lp{R(p.light_pos[0]), R(p.light_pos[1]), R(p.light_pos[2])};
+  V3<R> sv{u.scale_vol_inv[0], u.scale_vol_inv[1], u.scale_vol_inv[2]};
+  V3<R> L = normalize(lp - mul(pos, sv));
+  V3<R> T = normalize(V3<R>{R(2) * f.x - R(1), R(2) * f.y - R(1), R(2) * f.z - R(1)});
+  if (p.illum == VVLIC_ILLUM_ZOECKLER) {
+    V3<R> V = normalize(dir);
+    V4<R> sh = tex2d_lut<R>(in.luts, in.lut_w, in.lut_h, R(0.5) * dot(L, T) + R(0.5), R(0.5) * dot(V, T) + R(0.5));
+    R g = (p.quirks & VVLIC_QUIRK_ZOECKLER_LUMINANCE) ? sh.y : sh.w;
+    for (int ch = 0; ch < 3; ++ch) {
+      d[ch] = sh.x * u.illum_scale;
+      sp[ch] = R(0.9) * g;
+    }
+  } else {
+    V3<R> V = normalize(dir * R(-1));
+    V3<R> B = normalize(cross(T, V));
+    V3<R> N = cross(B, T);
+    V3<R> H = normalize(V + L);
+    R lx = dot(L, N), ly = dot(L, T), lz = dot(H, N), lw = dot(H, T);
+    R tx = R(1) / std::sqrt(R(1) - ly * ly), ty = R(1) / std::sqrt(R(1) - lw * lw);
+    R cz = R(0.5) * (lx * tx) + R(0.5), cy = R(0.5) * ly + R(0.5), cw = R(0.5) * (lz * ty) + R(0.5);
+    size_t one = (size_t)4 * in.lut_w * in.lut_h;
+    V4<R> df = tex2d_lut<R>(in.luts + one, in.lut_w, in.lut_h, cz, cy);
+    V4<R> sc = tex2d_lut<R>(in.luts + 2 * one, in.lut_w, in.lut_h, cz, cw);
+    R att = std::pow(ty, -R(p.spec_exp));
+    for (int ch = 0; ch < 3; ++ch) {
+      d[ch] = (&df.x)[ch] * u.illum_scale;
+      sp[ch] = sat_nan0((&sc.x)[ch] * att);
+    }
+  }
+}
+
 /* f = vectorData at pos; its encoded rgb is the tangent of illumZoeckler / illumMallo. */
 template <class R>
 static inline V4<R> shade(const LicCtx<R>& c, V4<R> illum, V4<R> tf, V3<R> pos, V3<R> dir, V4<R> f) {
@@ -786,35 +824,11 @@ static inline V4<R> shade(const LicCtx<R>& c, V4<R> illum, V4<R> tf, V3<R> pos, 
   V4<R> col;
   R I = illum.w;
   if (p.illum == VVLIC_ILLUM_ZOECKLER || p.illum == VVLIC_ILLUM_MALLO) {
-    const Inputs& in = *c.in;
-    V3<R> lp{R(p.light_pos[0]), R(p.light_pos[1]), R(p.light_pos[2])};
-    V3<R> sv{u.scale_vol_inv[0], u.scale_vol_inv[1], u.scale_vol_inv[2]};
-    V3<R> L = normalize(lp - mul(pos, sv));
-    V3<R> T = normalize(V3<R>{R(2) * f.x - R(1), R(2) * f.y - R(1), R(2) * f.z - R(1)});
-    if (p.illum == VVLIC_ILLUM_ZOECKLER) { /* inc_illum.glsl:117-154 */
-      V3<R> V = normalize(dir);
-      V4<R> sh = tex2d_lut<R>(in.luts, in.lut_w, in.lut_h, R(0.5) * dot(L, T) + R(0.5), R(0.5) * dot(V, T) + R(0.5));
-      R d = sh.x * u.illum_scale;
-      R g = (p.quirks & VVLIC_QUIRK_ZOECKLER_LUMINANCE) ? sh.y : sh.w;
-      col.x = tf.x * I * d + R(0.9) * g;
-      col.y = tf.y * I * d + R(0.9) * g;
-      col.z = tf.z * I * d + R(0.9) * g;
-    } else { /* inc_illum.glsl:46-112 */
-      V3<R> V = normalize(dir * R(-1));
-      V3<R> B = normalize(cross(T, V));
-      V3<R> N = cross(B, T);
-      V3<R> H = normalize(V + L);
-      R lx = dot(L, N), ly = dot(L, T), lz = dot(H, N), lw = dot(H, T);
-      R tx = R(1) / std::sqrt(R(1) - ly * ly), ty = R(1) / std::sqrt(R(1) - lw * lw);
-      R cz = R(0.5) * (lx * tx) + R(0.5), cy = R(0.5) * ly + R(0.5), cw = R(0.5) * (lz * ty) + R(0.5);
-      size_t one = (size_t)4 * in.lut_w * in.lut_h;
-      V4<R> df = tex2d_lut<R>(in.luts + one, in.lut_w, in.lut_h, cz, cy);
-      V4<R> sp = tex2d_lut<R>(in.luts + 2 * one, in.lut_w, in.lut_h, cz, cw);
-      R att = std::pow(ty, -R(p.spec_exp));
-      col.x = tf.x * I * (df.x * u.illum_scale) + sat_nan0(sp.x * att);
-      col.y = tf.y * I * (df.y * u.illum_scale) + sat_nan0(sp.y * att);
-      col.z = tf.z * I * (df.z * u.illum_scale) + sat_nan0(sp.z * att);
-    }
+    R d[3], sp[3];
+    line_factors<R>(c, pos, dir, f, d, sp);
+    col.x = tf.x * I * d[0] + sp[0];
+    col.y = tf.y * I * d[1] + sp[1];
+    col.z = tf.z * I * d[2] + sp[2];
   } else if (p.illum == VVLIC_ILLUM_GRADIENT) {
     V3<R> lp{R(p.light_pos[0]), R(p.light_pos[1]), R(p.light_pos[2])};
     V3<R> sv{u.scale_vol_inv[0], u.scale_vol_inv[1], u.scale_vol_inv[2]};
@@ -1225,6 +1239,7 @@ template <class R> static inline void adjoint_pixel(const Inputs& in, const vvli
     R op, a0, base, alpha;
     V3<R> col;
     Lit<R> lt3;
+    R ld[3];
   };
   std::vector<Sh> sh(S);
   for (size_t k = 0; k < S; ++k) {
@@ -1244,6 +1259,11 @@ template <class R> static inline void adjoint_pixel(const Inputs& in, const vvli
         cc[ch] = ((&h.tf.x)[ch] * smp[k].I * (R(p.light_diffuse[ch]) * h.lt3.df + R(0.3) + R(p.light_ambient[ch])) +
                   R(p.light_specular[ch]) * h.lt3.spf * smp[k].I) * u.illum_scale;
       h.col = V3<R>{cc[0], cc[1], cc[2]};
+    } else if (p.illum == VVLIC_ILLUM_ZOECKLER || p.illum == VVLIC_ILLUM_MALLO) {
+      R sp[3];
+      line_factors<R>(c, smp[k].pos, dir, smp[k].f, h.ld, sp);
+      h.col = V3<R>{h.tf.x * smp[k].I * h.ld[0] + sp[0], h.tf.y * smp[k].I * h.ld[1] + sp[1],
+                    h.tf.z * smp[k].I * h.ld[2] + sp[2]};
     } else {
       h.col = V3<R>{smp[k].I * h.tf.x * u.illum_scale, smp[k].I * h.tf.y * u.illum_scale,
                     smp[k].I * h.tf.z * u.illum_scale};
@@ -1285,6 +1305,9 @@ template <class R> static inline void adjoint_pixel(const Inputs& in, const vvli
       R dI_col;
       lit_vjp<R>(c, h.lt3, h.tf, dcol, dtf, &dI_col, &dG);
       dI += dI_col;
+    } else if (p.illum == VVLIC_ILLUM_ZOECKLER || p.illum == VVLIC_ILLUM_MALLO) {
+      for (int ch = 0; ch < 3; ++ch) dtf[ch] = dcol[ch] * smp[kk].I * h.ld[ch];
+      dI += dcol[0] * h.tf.x * h.ld[0] + dcol[1] * h.tf.y * h.ld[1] + dcol[2] * h.tf.z * h.ld[2];
     } else {
       /* col = I * tf.rgb * illumScale */
       for (int ch = 0; ch < 3; ++ch) dtf[ch] = dcol[ch] * smp[kk].I * u.illum_scale;

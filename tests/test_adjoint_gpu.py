@@ -20,10 +20,13 @@ def case(size=24, image=32, L=6, sampler="cell", storage="f32", lit=False):
     w.params.step_size_vol = 1.0 / 48.0
     w.params.gradient_scale = 8.0
     w.params.sampler = capi.SAMPLER[sampler]
-    if lit:  # illumGradient on central-difference noise gradients
+    if lit == "gradient" or lit is True:  # illumGradient on central-difference noise gradients
         w.params.illum = capi.ILLUM_GRADIENT
         w.params.light_pos[:] = (0.2, 1.4, 1.1)
         w.noise_mode = capi.NOISE_GRAD_CENTRAL
+    elif lit:
+        w.params.illum = {"zoeckler": capi.ILLUM_ZOECKLER, "mallo": capi.ILLUM_MALLO}[lit]
+        w.params.light_pos[:] = (0.2, 1.4, 1.1)
     w.storage = storage
     taps = np.linspace(0.5, 1.0, 2 * L + 1).astype(np.float64)
     return w, taps
@@ -64,8 +67,9 @@ def target_image(oracle, w, taps, storage="f32"):
 
 
 @pytest.mark.parametrize("sampler,storage,lit", [("cell", "f32", False), ("hybrid", "f16", False),
-                                                 ("gather", "f32", False), ("cell", "f32", True),
-                                                 ("hybrid", "f16", True)])
+                                                 ("gather", "f32", False), ("cell", "f32", "gradient"),
+                                                 ("hybrid", "f16", "gradient"), ("cell", "f32", "zoeckler"),
+                                                 ("cell", "f32", "mallo")])
 def test_adjoint_matches_fp64_oracle(ctx, oracle, sampler, storage, lit):
     w, taps = case(sampler=sampler, storage=storage, lit=lit)
     target = target_image(oracle, w, taps, storage)
@@ -90,7 +94,7 @@ def test_adjoint_matches_fp64_oracle(ctx, oracle, sampler, storage, lit):
               f"{scale:.3e}, relative L2 {rel_l2:.3e}")
         if not hw:
             # lit tapes hold the LIC gradient sum in FP16: the replayed normals carry its rounding
-            assert err <= (1e-2 if lit else 2e-3) * scale, (name, err, scale)
+            assert err <= (1e-2 if lit == "gradient" else 2e-3) * scale, (name, err, scale)
         else:
             # hardware filtering moves each sample's TF coordinate by a few hundredths of an
             # entry, which shifts gradient between neighbouring entries: compare the gradient
@@ -112,7 +116,7 @@ def test_adjoint_is_deterministic(ctx, oracle):
         np.testing.assert_array_equal(x, y)
 
 
-@pytest.mark.parametrize("lit", [False, True])
+@pytest.mark.parametrize("lit", [False, "gradient", "mallo"])
 def test_adjoint_matches_gpu_finite_differences(ctx, oracle, lit):
     import torch
 

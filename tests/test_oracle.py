@@ -311,9 +311,12 @@ def _adjoint_case(oracle, lit=False):
     w = wl.c1(size=12, image=14)
     w.field = wl.vortex_field((12, 12, 12), seed=6)
     w.noise = wl.dense_noise(12, seed=61)
-    if lit:  # illumGradient on central-difference noise gradients
+    if lit == "gradient":  # illumGradient on central-difference noise gradients
         w.noise = oracle.noise_gradients(w.noise, capi.NOISE_GRAD_CENTRAL)
         w.params.illum = capi.ILLUM_GRADIENT
+        w.params.light_pos[:] = (0.2, 1.4, 1.1)
+    elif lit:
+        w.params.illum = {"zoeckler": capi.ILLUM_ZOECKLER, "mallo": capi.ILLUM_MALLO}[lit]
         w.params.light_pos[:] = (0.2, 1.4, 1.1)
     w.params.integrator = capi.HEUN
     w.params.steps_forward = w.params.steps_backward = 4
@@ -332,7 +335,7 @@ def _adjoint_case(oracle, lit=False):
     return w, view, enc, rgba, op, taps, target, render
 
 
-@pytest.mark.parametrize("lit", [False, True])
+@pytest.mark.parametrize("lit", [False, "gradient", "zoeckler", "mallo"])
 def test_oracle_adjoint_matches_finite_differences(oracle, lit):
     w, view, enc, rgba, op, taps, target, render = _adjoint_case(oracle, lit)
     img, sc = render(rgba, op, taps)

@@ -1,4 +1,4 @@
-// Adjoint of the LIC ray-cast (illumLIC or illumGradient + front-to-back blend) with respect
+// Adjoint of the LIC ray-cast (any shading model + front-to-back blend) with respect
 // to the transfer-function table (256 RGBA), the opacity table (256) and the filter taps.
 //
 // The forward render records a tape: per sample (intensity I, TF coordinate), with gradient
@@ -6,7 +6,8 @@
 // (position, dest before the sample).  Per ray this kernel walks the segments last to first: it
 // recomputes the segment's compositing states from its checkpoint into a local array (cheap:
 // no streamline work), then backpropagates sample by sample through clamp, blend, alpha
-// correction, the opacity lookup, the shading and the TF lookup.  The cotangents of I and G are
+// correction, the opacity lookup, the shading (illumZoeckler / illumMallo factors recomputed
+// from the field sample) and the TF lookup.  The cotangents of I and G are
 // pushed onto the filter taps by walking the sample's streamlines once more
 // (dL/dw_j = sum_k S dL/dI_k n_kj + dL/dG_k . g_kj).
 //
@@ -192,6 +193,7 @@ __global__ void __launch_bounds__(kThreads) adjoint_kernel(const __grid_constant
   load_tf(a, s_tf);  // includes __syncthreads
   const int lane = threadIdx.x & 31;
   const int tiles_x = (a.W + kWarpTileW - 1) / kWarpTileW;
+  const bool line = !GRAD && (a.illum == VVLIC_ILLUM_ZOECKLER || a.illum == VVLIC_ILLUM_MALLO);
   float4 Dloc[kSegment];
   float3 Ploc[kSegment];
   for (;;) {
@@ -232,6 +234,12 @@ __global__ void __launch_bounds__(kThreads) adjoint_kernel(const __grid_constant
             const Src us = unlit_source(a, s_tf, rec.x, rec.y);
             const float3 col = lit_color(a, lit_setup(a, tape_gradient(a, idx), p, dir), us.tf, rec.x);
             src = make_float4(col.x, col.y, col.z, us.alpha);
+          } else if (line) {
+            const Src us = unlit_source(a, s_tf, rec.x, rec.y);
+            float3 d, sf;
+            line_factors(a, p, dir, Field<ST, FL>::sample(a, p), d, sf);
+            src = make_float4(us.tf.x * rec.x * d.x + sf.x, us.tf.y * rec.x * d.y + sf.y, us.tf.z * rec.x * d.z + sf.z,
+                              us.alpha);
           } else {
             src = unlit_source_rgba(a, s_tf, rec.x, rec.y);
           }
@@ -249,9 +257,14 @@ __global__ void __launch_bounds__(kThreads) adjoint_kernel(const __grid_constant
           const float I = rec.x;
           Src s = unlit_source(a, s_tf, I, rec.y);
           LitT lt;
+          float3 ld = f3(0.f, 0.f, 0.f);
           if (GRAD) {
             lt = lit_setup(a, tape_gradient(a, idx), Ploc[kk], dir);
             s.col = lit_color(a, lt, s.tf, I);
+          } else if (line) {  // colour = tf.rgb * I * d + s (d, s independent of TF, taps and I)
+            float3 sf;
+            line_factors(a, Ploc[kk], dir, Field<ST, FL>::sample(a, Ploc[kk]), ld, sf);
+            s.col = f3(s.tf.x * I * ld.x + sf.x, s.tf.y * I * ld.y + sf.y, s.tf.z * I * ld.z + sf.z);
           }
           const float4 sv = premultiplied(s);
           const float4 Dp = Dloc[kk];
@@ -282,6 +295,11 @@ __global__ void __launch_bounds__(kThreads) adjoint_kernel(const __grid_constant
             float dIc;
             lit_vjp(a, lt, s.tf, I, f3(dcx, dcy, dcz), dtf, &dIc, &gG);
             dI += dIc;
+          } else if (line) {
+            dtf[0] = dcx * I * ld.x;
+            dtf[1] = dcy * I * ld.y;
+            dtf[2] = dcz * I * ld.z;
+            dI += dcx * s.tf.x * ld.x + dcy * s.tf.y * ld.y + dcz * s.tf.z * ld.z;
           } else {  // col = I * tf.rgb * illumScale
             const float ci = I * a.illum_scale;
             dtf[0] = dcx * ci;

@@ -486,9 +486,6 @@ extern "C" vvlic_status vvlic_render_adjoint(vvlic_ctx* c, int32_t vol_id, const
     return fail(c, VVLIC_ERR_NOT_READY,
                 "render_adjoint: the last render of this context did not record a tape for volume %d at %dx%d "
                 "(set params.record_tape)", vol_id, w, h);
-  if (c->tape_illum != VVLIC_ILLUM_NONE && c->tape_illum != VVLIC_ILLUM_GRADIENT)
-    return fail(c, VVLIC_ERR_UNSUPPORTED,
-                "render_adjoint: only illumLIC and illumGradient shading are differentiated");
   if (c->vols.find(vol_id) == c->vols.end())
     return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "render_adjoint: unknown volume %d", vol_id);
   DeviceGuard g(c->device);

@@ -560,28 +560,27 @@ __device__ __forceinline__ float3 light_dir(const RenderArgs& a, float3 pos) {
                     mul3(pos, f3(a.scale_vol_inv[0], a.scale_vol_inv[1], a.scale_vol_inv[2]))));
 }
 
-// `f` is the field sample at `pos` (vectorData): its encoded direction is the streamline
-// tangent of illumZoeckler / illumMallo.  GRAD kernels (noise gradients fetched) only ever
-// shade with illumGradient; the others with illumLIC, illumZoeckler or illumMallo.
-template <bool GRAD>
-__device__ __forceinline__ float4 shade(const RenderArgs& a, const float* s_tf, float4 il, float4 tf, float3 pos,
-                                        float3 dir, float4 f) {
-  const float I = il.w;
-  float4 col;
-  if (!GRAD && a.illum == VVLIC_ILLUM_ZOECKLER) {  // inc_illum.glsl:117-154
-    const float3 L = light_dir(a, pos);
+// Illuminated-streamline factors of one sample: colour = tf.rgb * I * d + s with d and s from
+// the line tables.  `f` is the field sample at `pos` (vectorData), whose encoded direction is
+// the streamline tangent.
+//   illumZoeckler (inc_illum.glsl:117-154): (L.T, V.T)/2 + 1/2 into the table, V = n(dir);
+//     d = L_d * illumScale, s = 0.9 * g (g = L_d with the luminance quirk, else the stored specular);
+//   illumMallo (inc_illum.glsl:46-112): B = n(T x V), N = B x T, H = n(V + L), V = n(-dir);
+//     d = diffuse(LN/sqrt(1-LT^2), LT) * illumScale,
+//     s = sat(specular(LN/sqrt(1-LT^2), HN/sqrt(1-HT^2)) * (1-HT^2)^(e/2)).
+__device__ __forceinline__ void line_factors(const RenderArgs& a, float3 pos, float3 dir, float4 f, float3& d,
+                                             float3& s) {
+  const float3 L = light_dir(a, pos);
+  const float3 T = norm3(f3(2.0f * f.x - 1.0f, 2.0f * f.y - 1.0f, 2.0f * f.z - 1.0f));
+  if (a.illum == VVLIC_ILLUM_ZOECKLER) {
     const float3 V = norm3(dir);
-    const float3 T = norm3(f3(2.0f * f.x - 1.0f, 2.0f * f.y - 1.0f, 2.0f * f.z - 1.0f));
     const float4 sh = lut2d(a.luts, a.lut_w, a.lut_h, 0.5f * dot3(L, T) + 0.5f, 0.5f * dot3(V, T) + 0.5f);
-    const float d = sh.x * a.illum_scale;
+    const float dd = sh.x * a.illum_scale;
     const float sp = 0.9f * ((a.quirks & VVLIC_QUIRK_ZOECKLER_LUMINANCE) ? sh.y : sh.w);
-    col.x = tf.x * I * d + sp;
-    col.y = tf.y * I * d + sp;
-    col.z = tf.z * I * d + sp;
-  } else if (!GRAD && a.illum == VVLIC_ILLUM_MALLO) {  // inc_illum.glsl:46-112
-    const float3 L = light_dir(a, pos);
+    d = f3(dd, dd, dd);
+    s = f3(sp, sp, sp);
+  } else {
     const float3 V = norm3(scl3(dir, -1.0f));
-    const float3 T = norm3(f3(2.0f * f.x - 1.0f, 2.0f * f.y - 1.0f, 2.0f * f.z - 1.0f));
     const float3 B = norm3(cross3(T, V));
     const float3 N = cross3(B, T);
     const float3 Hv = norm3(add3(V, L));
@@ -592,10 +591,24 @@ __device__ __forceinline__ float4 shade(const RenderArgs& a, const float* s_tf, 
     const float4 df = lut2d(a.luts + one, a.lut_w, a.lut_h, cz, cy);
     const float4 sc = lut2d(a.luts + 2 * one, a.lut_w, a.lut_h, cz, cw);
     const float att = powf(rh, -a.spec_exp);  // (1 - (H.T)^2)^(n/2)
-    const float ti = I * a.illum_scale;
-    col.x = tf.x * ti * df.x + __saturatef(sc.x * att);
-    col.y = tf.y * ti * df.y + __saturatef(sc.y * att);
-    col.z = tf.z * ti * df.z + __saturatef(sc.z * att);
+    d = scl3(f3(df.x, df.y, df.z), a.illum_scale);
+    s = f3(__saturatef(sc.x * att), __saturatef(sc.y * att), __saturatef(sc.z * att));
+  }
+}
+
+// GRAD kernels (noise gradients fetched) only ever shade with illumGradient; the others with
+// illumLIC, illumZoeckler or illumMallo.
+template <bool GRAD>
+__device__ __forceinline__ float4 shade(const RenderArgs& a, const float* s_tf, float4 il, float4 tf, float3 pos,
+                                        float3 dir, float4 f) {
+  const float I = il.w;
+  float4 col;
+  if (!GRAD && (a.illum == VVLIC_ILLUM_ZOECKLER || a.illum == VVLIC_ILLUM_MALLO)) {
+    float3 d, s;
+    line_factors(a, pos, dir, f, d, s);
+    col.x = tf.x * I * d.x + s.x;
+    col.y = tf.y * I * d.y + s.y;
+    col.z = tf.z * I * d.z + s.z;
   } else if (GRAD) {
     float3 L = light_dir(a, pos);
     float3 V = norm3(scl3(dir, -1.0f));
