@@ -425,6 +425,7 @@ def bench_orbit(ctx, torch, stream, flush, args, dist):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_kind": peak_kind, "algorithmic_bytes_per_frame": alg / frames},
         "clocks": clk, "generation_s": gen_s, "setup_s": setup_s,
+        "image_alpha_mean": float(out[..., 3].mean()),
         "fwd_adjoint": adjoint,
     }
 
@@ -566,6 +567,7 @@ def run_ours(args, dist):
                    "sample_steps_per_frame": int(st.sample_steps), "samples_per_frame": int(st.samples),
                    "rays": int(st.rays), "parallelism": f"replicas x{dist.world}"},
         "wall_ms_per_step": t_wall / args.steps * 1e3,
+        "image_alpha_mean": float(out[..., 3].mean()),
         "roofline": roofline,
         "gpu_launches": args.steps,
         "clocks": clk,

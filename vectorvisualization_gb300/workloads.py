@@ -102,7 +102,9 @@ def spectral_field(n: int, seed: int, kmin: float = 2.0, kmax: float = 64.0, dev
 
     Complex Gaussian modes are scaled so that the shell energy follows k^(-5/3), projected onto
     the plane orthogonal to k (solenoidal) and inverse-transformed (torch.fft on `device` when
-    given, numpy otherwise).  Returns (n, n, n, 3) float32."""
+    given, numpy otherwise), then scaled to unit RMS magnitude: the unnormalised inverse
+    transform shrinks as n^-3 (about 1e-7 at 512^3), below the 1e-5 zero-vector threshold of the
+    field encoding.  Returns (n, n, n, 3) float32."""
     rng = SplitMix64(seed)
     kx = np.fft.fftfreq(n, 1.0 / n)
     kz = np.fft.rfftfreq(n, 1.0 / n)
@@ -131,9 +133,12 @@ def spectral_field(n: int, seed: int, kmin: float = 2.0, kmax: float = 64.0, dev
             t = torch.fft.irfftn(torch.from_numpy(u).to(device), s=(n, n, n))
             r = t.float().cpu().numpy()
         else:
-            r = np.fft.irfftn(u, s=(n, n, n)).astype(np.float32)
+            r = np.fft.irfftn(u, s=(n, n, n), axes=(0, 1, 2)).astype(np.float32)
         # array axes are (x, y, z); the field layout is (z, y, x)
         out[..., d] = np.transpose(r, (2, 1, 0))
+    rms = float(np.sqrt(np.einsum("zyxc,zyxc->", out, out, dtype=np.float64) / (n ** 3)))
+    if rms > 0:
+        out *= np.float32(1.0 / rms)
     return out
 
 
