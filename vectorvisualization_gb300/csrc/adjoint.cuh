@@ -156,7 +156,6 @@ template <int ST, int FL, int NL, int INTEG, bool GRAD>
 __device__ __forceinline__ void tap_gradients(const RenderArgs& a, float3 pos, float gI, float3 gG, long long* s_taps) {
   const bool act = gI != 0.0f || (GRAD && (gG.x != 0.0f || gG.y != 0.0f || gG.z != 0.0f));
   const int lb = a.lb, lf = a.lf, L = max(lb, lf);
-  const int lane = threadIdx.x & 31;
   float4 f0 = make_float4(0.f, 0.f, 0.f, 0.f);
   float v0 = 0.0f;
   if (act) {
@@ -166,46 +165,20 @@ __device__ __forceinline__ void tap_gradients(const RenderArgs& a, float3 pos, f
   warp_fixed_add(s_taps + lb, v0);
   float3 pb = pos, pf = pos;
   float4 sb = f0, sf = f0;
-  // Four steps of both directions give eight per-lane values; one transposed warp reduction
-  // (9 shuffles instead of 8 butterflies of 5) leaves each sum on four lanes: the lane whose
-  // bits 4, 3, 2 select the slot and bits 1, 0 are zero adds it to its tap.
-  const int slot = ((lane >> 4) & 1) * 4 + ((lane >> 3) & 1) * 2 + ((lane >> 2) & 1);
-  for (int i0 = 1; i0 <= L; i0 += 4) {
-    float v[8];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int i = i0 + q;
-      float vb = 0.0f, vf = 0.0f;
-      if (act && i <= L) {
-        if (i <= lb) {
-          pb = lic_step<ST, FL, INTEG>(a, pb, sb, -1.0f);
-          vb = tap_dot<ST, FL, NL, INTEG, GRAD>(noise_tap<NL, GRAD>(a, pb), gI, gG);
-        }
-        if (i <= lf) {
-          pf = lic_step<ST, FL, INTEG>(a, pf, sf, 1.0f);
-          vf = tap_dot<ST, FL, NL, INTEG, GRAD>(noise_tap<NL, GRAD>(a, pf), gI, gG);
-        }
+  for (int i = 1; i <= L; ++i) {
+    float vb = 0.0f, vf = 0.0f;
+    if (act) {
+      if (i <= lb) {
+        pb = lic_step<ST, FL, INTEG>(a, pb, sb, -1.0f);
+        vb = tap_dot<ST, FL, NL, INTEG, GRAD>(noise_tap<NL, GRAD>(a, pb), gI, gG);
       }
-      v[2 * q] = vb;
-      v[2 * q + 1] = vf;
-    }
-    // lower lanes of each exchange keep slots [0, h), upper lanes slots [h, 2h)
-#pragma unroll
-    for (int o = 16, h = 4; h >= 1; o >>= 1, h >>= 1) {
-      const bool upper = (lane & o) != 0;
-#pragma unroll
-      for (int k = 0; k < h; ++k) {
-        const float send = upper ? v[k] : v[k + h];
-        const float keep = upper ? v[k + h] : v[k];
-        v[k] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+      if (i <= lf) {
+        pf = lic_step<ST, FL, INTEG>(a, pf, sf, 1.0f);
+        vf = tap_dot<ST, FL, NL, INTEG, GRAD>(noise_tap<NL, GRAD>(a, pf), gI, gG);
       }
     }
-    float r = v[0];
-    r += __shfl_xor_sync(0xffffffffu, r, 2);
-    r += __shfl_xor_sync(0xffffffffu, r, 1);
-    const int i = i0 + (slot >> 1);
-    const bool fwd = slot & 1;
-    if ((lane & 3) == 0 && i <= (fwd ? lf : lb)) fixed_add(s_taps + (fwd ? lb + i : lb - i), r);
+    if (i <= lb) warp_fixed_add(s_taps + lb - i, vb);
+    if (i <= lf) warp_fixed_add(s_taps + lb + i, vf);
   }
 }
 
