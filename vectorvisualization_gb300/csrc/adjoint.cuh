@@ -20,6 +20,13 @@
 
 namespace vvlic {
 
+// Minimum resident CTAs per SM requested for the adjoint kernels (register cap 65536 / (128 * n)):
+// 6 (80 registers, a few spilled bytes) measured 1786 ms against 1951 ms for 5 (93 registers)
+// on the lit 512^3 RK4 frame.
+#ifndef VVLIC_ADJ_MIN_BLOCKS
+#define VVLIC_ADJ_MIN_BLOCKS 6
+#endif
+
 constexpr float kFixedScale = 1073741824.0f;  // 2^30
 constexpr int kAccTF = 0, kAccOpac = 4 * VVLIC_TF_ENTRIES, kAccTaps = 5 * VVLIC_TF_ENTRIES;
 constexpr int kAccSize = kAccTaps + kMaxTaps;
@@ -183,7 +190,7 @@ __device__ __forceinline__ void tap_gradients(const RenderArgs& a, float3 pos, f
 }
 
 template <int ST, int FL, int NL, int INTEG, bool GRAD>
-__global__ void __launch_bounds__(kThreads) adjoint_kernel(const __grid_constant__ RenderArgs a,
+__global__ void __launch_bounds__(kThreads, VVLIC_ADJ_MIN_BLOCKS) adjoint_kernel(const __grid_constant__ RenderArgs a,
                                                            const float4* __restrict__ g_img, long long* acc,
                                                            const uint32_t* __restrict__ order, int ntiles,
                                                            unsigned* __restrict__ next) {
@@ -219,15 +226,15 @@ __global__ void __launch_bounds__(kThreads) adjoint_kernel(const __grid_constant
       const bool act_seg = seg < nseg;
       int cnt = 0;
       if (act_seg) {
-        const float4* ck = a.tape_ck + 2 * (ray * a.tape_nck + seg);
+        const float4* ck = a.tape_ck + tape_ck_entry(a, px, py, seg);
         const float4 p4 = ck[0];
         float3 p = f3(p4.x, p4.y, p4.z);
-        float4 D = ck[1];
+        float4 D = ck[32];
         cnt = min(kSegment, S - seg * kSegment);
         for (int kk = 0; kk < cnt; ++kk) {
           Ploc[kk] = p;
           Dloc[kk] = D;
-          const size_t idx = ray * a.tape_stride + seg * kSegment + kk;
+          const size_t idx = tape_entry(a, px, py, seg * kSegment + kk);
           const float2 rec = a.tape_is[idx];
           float4 src;
           if (GRAD) {
@@ -252,7 +259,7 @@ __global__ void __launch_bounds__(kThreads) adjoint_kernel(const __grid_constant
         float3 gG = f3(0.f, 0.f, 0.f);
         float3 pk = f3(0.f, 0.f, 0.f);
         if (kk < cnt) {
-          const size_t idx = ray * a.tape_stride + seg * kSegment + kk;
+          const size_t idx = tape_entry(a, px, py, seg * kSegment + kk);
           const float2 rec = a.tape_is[idx];
           const float I = rec.x;
           Src s = unlit_source(a, s_tf, I, rec.y);

@@ -347,9 +347,11 @@ vvlic_status prepare_tape(vvlic_ctx* c, const Geometry& gm, int w, int h, Render
   const int stride = std::max(1, (int)std::ceil(bound));
   const int nck = (stride + kSegment - 1) / kSegment;
   const size_t rays = (size_t)w * h;
+  // per-sample arrays in 8x4-ray tiles (tape_entry / tape_ck_entry), edge tiles padded
+  const size_t slots = (size_t)((w + 7) / 8) * (size_t)((h + 3) / 4) * 32;
   const bool lit = a.illum == VVLIC_ILLUM_GRADIENT;
-  const size_t b_is = rays * stride * sizeof(float2), b_ck = rays * nck * 2 * sizeof(float4),
-               b_g = lit ? rays * stride * sizeof(uint2) : 0, b_n = rays * sizeof(uint32_t);
+  const size_t b_is = slots * stride * sizeof(float2), b_ck = slots * nck * 2 * sizeof(float4),
+               b_g = lit ? slots * stride * sizeof(uint2) : 0, b_n = rays * sizeof(uint32_t);
   const size_t bytes = b_ck + b_is + b_g + b_n;
   if (c->tape_cap < bytes) {
     if (c->d_tape) cudaFree(c->d_tape);

@@ -685,6 +685,25 @@ __device__ __forceinline__ bool outside_box(const RenderArgs& a, float3 p) {
   return p.x < 0.0f || p.y < 0.0f || p.z < 0.0f || p.x > a.tex_max[0] || p.y > a.tex_max[1] || p.z > a.tex_max[2];
 }
 
+// Adjoint tape layout: rays grouped in 8x4-pixel tiles (the queue schedule's warp tiles) and,
+// within a tile, sample-major with the tile's 32 rays adjacent, so that a warp recording or
+// replaying sample k of its tile touches 32 consecutive entries.
+constexpr int kTapeTileW = 8, kTapeTileH = 4;
+__device__ __forceinline__ size_t tape_tile(const RenderArgs& a, int px, int py) {
+  return (size_t)(py / kTapeTileH) * (size_t)((a.W + kTapeTileW - 1) / kTapeTileW) + (size_t)(px / kTapeTileW);
+}
+__device__ __forceinline__ size_t tape_lane(int px, int py) {
+  return (size_t)((py % kTapeTileH) * kTapeTileW + px % kTapeTileW);
+}
+// tape_is / tape_g entry of sample k of the ray at (px, py)
+__device__ __forceinline__ size_t tape_entry(const RenderArgs& a, int px, int py, uint32_t k) {
+  return (tape_tile(a, px, py) * (size_t)a.tape_stride + k) * 32 + tape_lane(px, py);
+}
+// checkpoint of segment s: position at the returned index, dest 32 entries later
+__device__ __forceinline__ size_t tape_ck_entry(const RenderArgs& a, int px, int py, uint32_t s) {
+  return (tape_tile(a, px, py) * (size_t)a.tape_nck + s) * 64 + tape_lane(px, py);
+}
+
 // The whole lic3d_fragment.glsl main() for one pixel: returns dest, counts samples.
 template <int ST, int FL, int NL, int INTEG, bool GRAD>
 __device__ __forceinline__ float4 trace_pixel(const RenderArgs& a, const float* s_tf, int px, int py,
@@ -697,7 +716,6 @@ __device__ __forceinline__ float4 trace_pixel(const RenderArgs& a, const float* 
   hit = 1;
   float4 src = make_float4(0.f, 0.f, 0.f, 0.f);
   bool outside = false;
-  const size_t ray = (size_t)py * a.W + px;
   for (int j = 0; !outside && j < a.num_iter; ++j) {
     for (int i = 0; i < a.num_iter; ++i) {
       const float4 f = Field<ST, FL>::sample(a, pos);
@@ -707,16 +725,16 @@ __device__ __forceinline__ float4 trace_pixel(const RenderArgs& a, const float* 
       il.w *= a.intensity_scale;
       if (a.tape_is) {  // record for the adjoint
         if (samples % kSegment == 0 && samples / kSegment < (uint32_t)a.tape_nck) {
-          float4* ck = a.tape_ck + 2 * (ray * a.tape_nck + samples / kSegment);
+          float4* ck = a.tape_ck + tape_ck_entry(a, px, py, samples / kSegment);
           ck[0] = make_float4(pos.x, pos.y, pos.z, 0.f);
-          ck[1] = dest;
+          ck[32] = dest;
         }
         if (samples < (uint32_t)a.tape_stride) {
-          a.tape_is[ray * a.tape_stride + samples] = make_float2(il.w, tfc);
+          const size_t e = tape_entry(a, px, py, samples);
+          a.tape_is[e] = make_float2(il.w, tfc);
           if (GRAD) {
             const __half2 xy = __floats2half2_rn(il.x, il.y), z0 = __floats2half2_rn(il.z, 0.0f);
-            a.tape_g[ray * a.tape_stride + samples] =
-                make_uint2(*reinterpret_cast<const unsigned*>(&xy), *reinterpret_cast<const unsigned*>(&z0));
+            a.tape_g[e] = make_uint2(*reinterpret_cast<const unsigned*>(&xy), *reinterpret_cast<const unsigned*>(&z0));
           }
         }
       }
@@ -745,7 +763,6 @@ __device__ __forceinline__ float4 trace_pixel2(const RenderArgs& a, const float*
   if (!ray_setup(a, px, py, pos, dir)) return dest;
   hit = 1;
   const uint32_t max_samples = (uint32_t)a.num_iter * (uint32_t)a.num_iter;
-  const size_t ray = (size_t)py * a.W + px;
   const float3 dstep = scl3(dir, a.step_size);
   while (samples < max_samples) {
     const float3 pos1 = add3(pos, dstep);
@@ -763,16 +780,16 @@ __device__ __forceinline__ float4 trace_pixel2(const RenderArgs& a, const float*
       l.w *= a.intensity_scale;
       if (a.tape_is) {  // record for the adjoint
         if (samples % kSegment == 0 && samples / kSegment < (uint32_t)a.tape_nck) {
-          float4* ck = a.tape_ck + 2 * (ray * a.tape_nck + samples / kSegment);
+          float4* ck = a.tape_ck + tape_ck_entry(a, px, py, samples / kSegment);
           ck[0] = make_float4(p.x, p.y, p.z, 0.f);
-          ck[1] = dest;
+          ck[32] = dest;
         }
         if (samples < (uint32_t)a.tape_stride) {
-          a.tape_is[ray * a.tape_stride + samples] = make_float2(l.w, tfc);
+          const size_t e = tape_entry(a, px, py, samples);
+          a.tape_is[e] = make_float2(l.w, tfc);
           if (GRAD) {
             const __half2 xy = __floats2half2_rn(l.x, l.y), z0 = __floats2half2_rn(l.z, 0.0f);
-            a.tape_g[ray * a.tape_stride + samples] =
-                make_uint2(*reinterpret_cast<const unsigned*>(&xy), *reinterpret_cast<const unsigned*>(&z0));
+            a.tape_g[e] = make_uint2(*reinterpret_cast<const unsigned*>(&xy), *reinterpret_cast<const unsigned*>(&z0));
           }
         }
       }
