@@ -51,10 +51,14 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
-    ap.add_argument("--c3", action="store_true", help="also time the 64-volume batch")
+    # the batch (C3) and the large orbit (C5) run by default; --no-c3 / --no-c5 skip them
+    ap.add_argument("--c3", dest="c3", action="store_true")
+    ap.add_argument("--no-c3", dest="c3", action="store_false", help="skip the 64-volume batch")
     ap.add_argument("--c3-volumes", type=int, default=64)
-    ap.add_argument("--c5", action="store_true", help="also time the 512^3 RK4 lit orbit")
-    ap.add_argument("--c5-frames", type=int, default=8)
+    ap.add_argument("--c5", dest="c5", action="store_true")
+    ap.add_argument("--no-c5", dest="c5", action="store_false", help="skip the 512^3 RK4 lit orbit")
+    ap.add_argument("--c5-frames", type=int, default=2)
+    ap.set_defaults(c3=True, c5=True)
     ap.add_argument("--c5-size", type=int, default=512)
     ap.add_argument("--c5-image", type=int, default=2048)
     return ap.parse_args()
@@ -345,11 +349,45 @@ def bench_batch(ctx, torch, stream, flush, args):
         times.append(e0.elapsed_time(e1))
     st = ctx.stats()
     ms = min(times)
+    # cacheless model for the unlit Heun batch: 8 (2 s_F + 1) B per sample-step
+    sF = bytes_per_texel(args.storage)
+    alg = st.sample_steps * 8 * (2 * sF + 1) + st.samples * 8 * sF + len(jobs) * 512 * 512 * 16
+    peak, peak_kind = load_peaks()
+    achieved = alg / (ms / 1e3) / 1e9
+    # the plain FP32 form: the same jobs from FP32 texels with the gather sampler, one launch
+    plain_ms = None
+    with capi.Context(torch.cuda.current_device()) as pctx:
+        pctx.upload_noise(noise)
+        pctx.set_tf(*wl.default_tf())
+        pjobs = []
+        k = 0
+        for bv in vols:
+            pvid = pctx.upload_field(bv.field, storage="f32")
+            table = capi.make_filter_table(bv.filter_kind, 256)
+            for v in bv.views:
+                p = capi.Params.from_buffer_copy(base)
+                p.steps_forward = p.steps_backward = bv.L
+                p.sampler = capi.SAMPLER["gather"]
+                pjobs.append(capi.make_job(pvid, outs[k].data_ptr(), 512, 512, v, p, table))
+                k += 1
+        pctx.batch_render(pjobs, sh)
+        stream.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            e0.record(stream)
+            pctx.batch_render(pjobs, sh)
+            e1.record(stream)
+        torch.cuda.synchronize()
+        plain_ms = e0.elapsed_time(e1)
     return {
         "workload": f"C3 {len(vols)} volumes (dims 64..192 per axis), {len(jobs)} views at 512^2, L 15..60, "
                     f"mixed box/triangle/cos2, {args.storage}",
         "jobs": len(jobs), "voxels": voxels, "ms_per_batch": ms, "frames_per_s": len(jobs) / (ms / 1e3),
         "gss": st.sample_steps / (ms / 1e3) / 1e9, "sample_steps": int(st.sample_steps),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": peak_kind, "algorithmic_bytes_per_batch": alg},
+        "plain_f32_gather_ms": plain_ms, "speedup_vs_plain_f32": plain_ms / ms,
         "autotune": {"tile": f"{tw}x{32 // tw}", "sampler": [k for k, v in capi.SAMPLER.items() if v == smp][0],
                      "best_ms": tune_ms},
         "cuda_graph": True, "generation_s": gen_s,
