@@ -607,7 +607,8 @@ def run_ours(args, dist):
         "wall_ms_per_step": t_wall / args.steps * 1e3,
         "image_alpha_mean": float(out[..., 3].mean()),
         "roofline": roofline,
-        "gpu_launches": args.steps,
+        # per frame: the queue schedule's tile order (cost, bucket scan, scatter) + the ray-cast
+        "gpu_launches": args.steps * (4 if args.schedule == "queue" else 1),
         "clocks": clk,
     }
 
