@@ -32,8 +32,8 @@ struct LICParams {
   float stepSizeLIC = 0.01f;
 };
 
-/* types.h:63-72 (the techniques this library renders) */
-enum RenderTechnique { VOLIC_RAYCAST = 1 };
+/* types.h:63-72: the render techniques (VOLIC_VOLUMEANI is never rendered by the reference) */
+enum RenderTechnique { VOLIC_VOLUME = 0, VOLIC_RAYCAST = 1, VOLIC_SLICING = 2, VOLIC_LICVOLUME = 3 };
 
 class Error : public std::runtime_error {
  public:
@@ -72,6 +72,24 @@ class Renderer {
     return id;
   }
   void useVolume(int id) { vol_ = id; }
+  /* VectorDataSet::loadData(file) + createTextureIterp: a .dat/.raw vector data set (the
+   * timestep, or the first one for -1) becomes the current volume */
+  int loadData(const char* datFile, int timestep = -1, int storage = VVLIC_STORAGE_F16) {
+    int32_t id = 0;
+    vvlic_status s = vvlic_upload_dat(ctx_, datFile, timestep, storage, &id);
+    if (s != VVLIC_OK) throw Error(s, std::string("loadData: ") + vvlic_io_error());
+    vol_ = id;
+    return id;
+  }
+  /* Renderer::setTechnique (renderer.h:44); LICVOLUME renders need computeLICVolume first */
+  void setTechnique(RenderTechnique rt) {
+    params_.technique = (int32_t)rt;
+    check(vvlic_set_params(ctx_, &params_), "setTechnique");
+  }
+  /* Renderer::renderLICVolume (renderer.cpp:1311-1374): the LIC volume of the current volume */
+  void computeLICVolume(int nx = 512, int ny = 512, int nz = 512) {
+    check(vvlic_compute_lic_volume(ctx_, vol_, nx, ny, nz), "computeLICVolume");
+  }
 
   /* NoiseDataSet::createTexture + Renderer::setNoiseTex; gradients = the -g switch
    * (parseArg.cpp), gradMode = VVLIC_NOISE_GRAD_SOBEL (gradient.h SOBEL 1) or _CENTRAL. */
@@ -144,6 +162,12 @@ class Renderer {
   }
   /* Renderer::render -> raycastVolume: writes w*h RGBA floats (row 0 = bottom) to host memory */
   void render(float* rgba, int w, int h) { check(vvlic_render(ctx_, vol_, rgba, w, h), "render"); }
+  /* the screenshot of renderBackground (renderer.cpp:1480-1500): PNG of the render buffer, or
+   * of the window image composited over white */
+  static void saveImage(const char* file, const float* rgba, int w, int h, bool overWhite = false) {
+    vvlic_status s = vvlic_image_write(file, rgba, w, h, VVLIC_IMAGE_PNG, overWhite ? 1 : 0);
+    if (s != VVLIC_OK) throw Error(s, std::string("saveImage: ") + vvlic_io_error());
+  }
   /* asynchronous render into device memory on a CUDA stream */
   void renderDevice(float* d_rgba, int w, int h, void* stream = nullptr) {
     check(vvlic_render_device(ctx_, vol_, d_rgba, w, h, nullptr, stream), "renderDevice");
