@@ -4,9 +4,8 @@
 // The forward render records a tape: per sample (intensity I, TF coordinate), with gradient
 // lighting also the LIC gradient sum G (4 halves), and every kSegment samples a checkpoint
 // (position, dest before the sample).  Per ray this kernel walks the segments last to first: it
-// recomputes the segment's compositing states from its checkpoint (cheap: no streamline work;
-// every 8th state is kept, the others replayed), then backpropagates sample by sample through
-// clamp, blend, alpha
+// recomputes the segment's compositing states from its checkpoint into a local array (cheap:
+// no streamline work), then backpropagates sample by sample through clamp, blend, alpha
 // correction, the opacity lookup, the shading (illumZoeckler / illumMallo factors recomputed
 // from the field sample) and the TF lookup.  The cotangents of I and G are
 // pushed onto the filter taps by walking the sample's streamlines once more
@@ -190,32 +189,6 @@ __device__ __forceinline__ void tap_gradients(const RenderArgs& a, float3 pos, f
   }
 }
 
-// The blend source (colour not yet multiplied by alpha, alpha) of tape record `idx` at position
-// p: what shade() gave the forward render.
-template <int ST, int FL, bool GRAD>
-__device__ __forceinline__ float4 replay_source(const RenderArgs& a, const float* s_tf, bool line, size_t idx, float3 p,
-                                                float3 dir) {
-  const float2 rec = a.tape_is[idx];
-  if (GRAD) {
-    const Src us = unlit_source(a, s_tf, rec.x, rec.y);
-    const float3 col = lit_color(a, lit_setup(a, tape_gradient(a, idx), p, dir), us.tf, rec.x);
-    return make_float4(col.x, col.y, col.z, us.alpha);
-  }
-  if (line) {
-    const Src us = unlit_source(a, s_tf, rec.x, rec.y);
-    float3 d, sf;
-    line_factors(a, p, dir, Field<ST, FL>::sample(a, p), d, sf);
-    return make_float4(us.tf.x * rec.x * d.x + sf.x, us.tf.y * rec.x * d.y + sf.y, us.tf.z * rec.x * d.z + sf.z,
-                       us.alpha);
-  }
-  return unlit_source_rgba(a, s_tf, rec.x, rec.y);
-}
-
-// Compositing states within a segment are kept for every kGroup-th sample only; the reverse pass
-// replays at most kGroup - 1 blends from the group's state to reach a sample's (a few hundred
-// bytes of per-thread arrays would otherwise live in local memory and miss L1).
-constexpr int kGroup = 8, kGroups = kSegment / kGroup;
-
 template <int ST, int FL, int NL, int INTEG, bool GRAD>
 __global__ void __launch_bounds__(kThreads, VVLIC_ADJ_MIN_BLOCKS) adjoint_kernel(const __grid_constant__ RenderArgs a,
                                                            const float4* __restrict__ g_img, long long* acc,
@@ -228,8 +201,8 @@ __global__ void __launch_bounds__(kThreads, VVLIC_ADJ_MIN_BLOCKS) adjoint_kernel
   const int lane = threadIdx.x & 31;
   const int tiles_x = (a.W + kWarpTileW - 1) / kWarpTileW;
   const bool line = !GRAD && (a.illum == VVLIC_ILLUM_ZOECKLER || a.illum == VVLIC_ILLUM_MALLO);
-  float4 Dg[kGroups];
-  float3 Pg[kGroups];
+  float4 Dloc[kSegment];
+  float3 Ploc[kSegment];
   for (;;) {
     unsigned t = 0;
     if (lane == 0) t = atomicAdd(next, 1u);
@@ -259,11 +232,25 @@ __global__ void __launch_bounds__(kThreads, VVLIC_ADJ_MIN_BLOCKS) adjoint_kernel
         float4 D = ck[32];
         cnt = min(kSegment, S - seg * kSegment);
         for (int kk = 0; kk < cnt; ++kk) {
-          if (kk % kGroup == 0) {
-            Dg[kk / kGroup] = D;
-            Pg[kk / kGroup] = p;
+          Ploc[kk] = p;
+          Dloc[kk] = D;
+          const size_t idx = tape_entry(a, px, py, seg * kSegment + kk);
+          const float2 rec = a.tape_is[idx];
+          float4 src;
+          if (GRAD) {
+            const Src us = unlit_source(a, s_tf, rec.x, rec.y);
+            const float3 col = lit_color(a, lit_setup(a, tape_gradient(a, idx), p, dir), us.tf, rec.x);
+            src = make_float4(col.x, col.y, col.z, us.alpha);
+          } else if (line) {
+            const Src us = unlit_source(a, s_tf, rec.x, rec.y);
+            float3 d, sf;
+            line_factors(a, p, dir, Field<ST, FL>::sample(a, p), d, sf);
+            src = make_float4(us.tf.x * rec.x * d.x + sf.x, us.tf.y * rec.x * d.y + sf.y, us.tf.z * rec.x * d.z + sf.z,
+                              us.alpha);
+          } else {
+            src = unlit_source_rgba(a, s_tf, rec.x, rec.y);
           }
-          D = blend(D, replay_source<ST, FL, GRAD>(a, s_tf, line, tape_entry(a, px, py, seg * kSegment + kk), p, dir));
+          D = blend(D, src);
           p = add3(p, scl3(dir, a.step_size));
         }
       }
@@ -272,13 +259,6 @@ __global__ void __launch_bounds__(kThreads, VVLIC_ADJ_MIN_BLOCKS) adjoint_kernel
         float3 gG = f3(0.f, 0.f, 0.f);
         float3 pk = f3(0.f, 0.f, 0.f);
         if (kk < cnt) {
-          // dest before sample kk and its position: replayed from the group's state
-          float4 Dp = Dg[kk / kGroup];
-          pk = Pg[kk / kGroup];
-          for (int m = kk - kk % kGroup; m < kk; ++m) {
-            Dp = blend(Dp, replay_source<ST, FL, GRAD>(a, s_tf, line, tape_entry(a, px, py, seg * kSegment + m), pk, dir));
-            pk = add3(pk, scl3(dir, a.step_size));
-          }
           const size_t idx = tape_entry(a, px, py, seg * kSegment + kk);
           const float2 rec = a.tape_is[idx];
           const float I = rec.x;
@@ -286,14 +266,16 @@ __global__ void __launch_bounds__(kThreads, VVLIC_ADJ_MIN_BLOCKS) adjoint_kernel
           LitT lt;
           float3 ld = f3(0.f, 0.f, 0.f);
           if (GRAD) {
-            lt = lit_setup(a, tape_gradient(a, idx), pk, dir);
+            lt = lit_setup(a, tape_gradient(a, idx), Ploc[kk], dir);
             s.col = lit_color(a, lt, s.tf, I);
           } else if (line) {  // colour = tf.rgb * I * d + s (d, s independent of TF, taps and I)
             float3 sf;
-            line_factors(a, pk, dir, Field<ST, FL>::sample(a, pk), ld, sf);
+            line_factors(a, Ploc[kk], dir, Field<ST, FL>::sample(a, Ploc[kk]), ld, sf);
             s.col = f3(s.tf.x * I * ld.x + sf.x, s.tf.y * I * ld.y + sf.y, s.tf.z * I * ld.z + sf.z);
           }
           const float4 sv = premultiplied(s);
+          const float4 Dp = Dloc[kk];
+          pk = Ploc[kk];
           const float om = 1.0f - Dp.w;
           // clamp((1 - Dp.a) * s + Dp) per channel: derivative 1 on [0, 1]
           const float ux = fmaf(om, sv.x, Dp.x), uy = fmaf(om, sv.y, Dp.y), uz = fmaf(om, sv.z, Dp.z),
