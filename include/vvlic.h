@@ -197,7 +197,18 @@ typedef struct vvlic_stats {
   uint64_t sample_steps;  /* samples * (L_f + L_b): the throughput unit */
   uint64_t rays;          /* pixels whose ray hit the volume */
   float kernel_ms;        /* device time of the render kernel (CUDA events) */
+  uint32_t check_flags;   /* libraries built with VVLIC_BOUNDS_CHECK: VVLIC_CHECK_* bits of the
+                             out-of-range accesses the render caught (and skipped); else 0 */
 } vvlic_stats;
+
+/* Index classes of the VVLIC_BOUNDS_CHECK build. */
+enum {
+  VVLIC_CHECK_FIELD = 1u << 0,
+  VVLIC_CHECK_NOISE = 1u << 1,
+  VVLIC_CHECK_SCALAR = 1u << 2,
+  VVLIC_CHECK_TAPE = 1u << 3,
+  VVLIC_CHECK_IMAGE = 1u << 4
+};
 
 /* ---- defaults and helpers (no device work) ------------------------------------------- */
 
@@ -396,6 +407,12 @@ vvlic_status vvlic_batch_autotune(vvlic_ctx* ctx, const vvlic_job* jobs, int32_t
 
 /* Statistics of the last render (samples are counted on the device every render). */
 vvlic_status vvlic_get_stats(vvlic_ctx* ctx, vvlic_stats* stats);
+
+/* Host watchdog (no reference counterpart; the reference blocks in SwapBuffers): wait for the
+ * work queued on `stream` (and on the context's own stream) to finish, polling
+ * cudaStreamQuery, for at most timeout_ms milliseconds.  VVLIC_ERR_TIMEOUT if the deadline
+ * passes first; the work keeps running and a later call can wait again. */
+vvlic_status vvlic_synchronize(vvlic_ctx* ctx, void* stream, int32_t timeout_ms);
 
 /* Composite an RGBA image over an opaque white background in place:
  * background_fragment.glsl:7-20 (dest = clamp((1-dest.a)*white + dest, 0, 1)).  Host memory. */

@@ -60,22 +60,30 @@ def _digest(extra: str) -> str:
     return h.hexdigest()
 
 
-def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -> str:
-    """Compile libvvlic.so if its sources changed; returns the library path."""
+def build(force: bool = False, verbose: bool = False, jobs: int | None = None, extra: list[str] | None = None,
+          variant: str | None = None) -> str:
+    """Compile libvvlic.so if its sources changed; returns the library path.
+
+    `extra` nvcc flags default to $VVLIC_NVCC_EXTRA (e.g. -DVVLIC_MIN_BLOCKS=8 to trade
+    registers for occupancy).  A `variant` name builds into _lib/<variant>/ and _build/<variant>/
+    instead, leaving the default library alone (e.g. the VVLIC_BOUNDS_CHECK build)."""
     nvcc = _nvcc()
-    os.makedirs(BUILD_DIR, exist_ok=True)
-    os.makedirs(OUT_DIR, exist_ok=True)
-    stamp = os.path.join(OUT_DIR, "libvvlic.stamp")
-    # extra nvcc flags (e.g. -DVVLIC_MIN_BLOCKS=8 to trade registers for occupancy)
-    extra = os.environ.get("VVLIC_NVCC_EXTRA", "").split()
+    out_dir = OUT_DIR if not variant else os.path.join(OUT_DIR, variant)
+    build_dir = BUILD_DIR if not variant else os.path.join(os.path.dirname(BUILD_DIR), variant)
+    lib = os.path.join(out_dir, "libvvlic.so")
+    os.makedirs(build_dir, exist_ok=True)
+    os.makedirs(out_dir, exist_ok=True)
+    stamp = os.path.join(out_dir, "libvvlic.stamp")
+    if extra is None:
+        extra = os.environ.get("VVLIC_NVCC_EXTRA", "").split()
     digest = _digest(" ".join(ARCH + COMMON + extra) + os.uname().machine)
-    if not force and os.path.exists(LIB) and os.path.exists(stamp):
+    if not force and os.path.exists(lib) and os.path.exists(stamp):
         with open(stamp) as fh:
             if fh.read().strip() == digest:
-                return LIB
+                return lib
 
     def compile_one(src: str) -> str:
-        obj = os.path.join(BUILD_DIR, os.path.splitext(src)[0] + ".o")
+        obj = os.path.join(build_dir, os.path.splitext(src)[0] + ".o")
         if src.endswith(".cpp"):  # host-only C++ (file formats): the plain C++ compiler
             cmd = [_cxx(), "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-I", INCLUDE, "-c",
                    os.path.join(CSRC, src), "-o", obj]
@@ -94,15 +102,15 @@ def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -
     jobs = jobs or min(len(srcs), max(2, os.cpu_count() or 2))
     with cf.ThreadPoolExecutor(max_workers=jobs) as ex:
         objs = list(ex.map(compile_one, srcs))
-    tmp = LIB + ".tmp"
+    tmp = lib + ".tmp"
     cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB)
+    os.replace(tmp, lib)
     with open(stamp, "w") as fh:
         fh.write(digest)
-    return LIB
+    return lib
 
 
 def main(argv=None) -> int:

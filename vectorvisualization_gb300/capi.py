@@ -141,6 +141,7 @@ class Stats(C.Structure):
         ("sample_steps", C.c_uint64),
         ("rays", C.c_uint64),
         ("kernel_ms", C.c_float),
+        ("check_flags", C.c_uint32),
     ]
 
 
@@ -163,6 +164,7 @@ _SIGS = {
     "vvlic_noise_write": (_I, [C.c_char_p, _P, _P]),
     "vvlic_image_write": (_I, [C.c_char_p, _P, _I, _I, _I, _I]),
     "vvlic_io_error": (C.c_char_p, []),
+    "vvlic_synchronize": (_I, [_P, _P, _I]),
     "vvlic_create": (_I, [C.POINTER(_P), _I]),
     "vvlic_destroy": (_I, [_P]),
     "vvlic_last_error": (C.c_char_p, [_P]),
@@ -286,8 +288,8 @@ def make_job(vol_id: int, d_out: int, w: int, h: int, view: View, params: Params
 class Context:
     """One vvlic_ctx on one CUDA device."""
 
-    def __init__(self, device: int = 0):
-        self._lib = load()
+    def __init__(self, device: int = 0, lib: C.CDLL | None = None):
+        self._lib = lib or load()
         h = _P()
         st = self._lib.vvlic_create(C.byref(h), device)
         if st:
@@ -418,6 +420,14 @@ class Context:
             msg = self._lib.vvlic_io_error().decode() or self._lib.vvlic_last_error(self.h).decode()
             raise VVLICError(st, f"upload_dat: {msg}")
         return vid.value
+
+    def synchronize(self, stream: int = 0, timeout_ms: int = 60000) -> bool:
+        """Wait for the work on `stream` and the context's stream; False on VVLIC_ERR_TIMEOUT."""
+        st = self._lib.vvlic_synchronize(self.h, stream or None, timeout_ms)
+        if st == ERR_TIMEOUT:
+            return False
+        self._check(st, "synchronize")
+        return True
 
     def set_line_material(self, material: LineMaterial):
         self._check(self._lib.vvlic_set_line_material(self.h, C.byref(material)), "set_line_material")

@@ -226,7 +226,9 @@ __global__ void __launch_bounds__(kThreads, VVLIC_ADJ_MIN_BLOCKS) adjoint_kernel
       const bool act_seg = seg < nseg;
       int cnt = 0;
       if (act_seg) {
-        const float4* ck = a.tape_ck + tape_ck_entry(a, px, py, seg);
+        size_t ce = tape_ck_entry(a, px, py, seg);
+        if (!in_range(a, (long long)ce + 32, tape_ck_entries(a), VVLIC_CHECK_TAPE)) ce = 0;
+        const float4* ck = a.tape_ck + ce;
         const float4 p4 = ck[0];
         float3 p = f3(p4.x, p4.y, p4.z);
         float4 D = ck[32];
@@ -234,7 +236,7 @@ __global__ void __launch_bounds__(kThreads, VVLIC_ADJ_MIN_BLOCKS) adjoint_kernel
         for (int kk = 0; kk < cnt; ++kk) {
           Ploc[kk] = p;
           Dloc[kk] = D;
-          const size_t idx = tape_entry(a, px, py, seg * kSegment + kk);
+          const size_t idx = tape_entry_checked(a, px, py, seg * kSegment + kk);
           const float2 rec = a.tape_is[idx];
           float4 src;
           if (GRAD) {
@@ -259,7 +261,7 @@ __global__ void __launch_bounds__(kThreads, VVLIC_ADJ_MIN_BLOCKS) adjoint_kernel
         float3 gG = f3(0.f, 0.f, 0.f);
         float3 pk = f3(0.f, 0.f, 0.f);
         if (kk < cnt) {
-          const size_t idx = tape_entry(a, px, py, seg * kSegment + kk);
+          const size_t idx = tape_entry_checked(a, px, py, seg * kSegment + kk);
           const float2 rec = a.tape_is[idx];
           const float I = rec.x;
           Src s = unlit_source(a, s_tf, I, rec.y);

@@ -4,7 +4,9 @@
 
 #include <algorithm>
 #include <cmath>
+#include <chrono>
 #include <cstring>
+#include <thread>
 
 #include "../../include/vvlic.h"
 #include "vvlic_device.cuh"
@@ -568,6 +570,7 @@ extern "C" vvlic_status vvlic_get_stats(vvlic_ctx* c, vvlic_stats* out) {
     // a batch mixes LIC lengths and counts its sample-steps on the device
     c->stats.sample_steps = c->last_was_batch ? h[2] : h[0] * c->stats_steps_per_sample;
     c->stats.kernel_ms = ms;
+    c->stats.check_flags = (uint32_t)h[3];
     c->stats_pending = false;
   }
   *out = c->stats;
@@ -626,5 +629,24 @@ extern "C" vvlic_status vvlic_download_lic_volume(vvlic_ctx* c, int32_t vol_id, 
   cudaError_t e = cudaStreamSynchronize(c->stream);
   if (e == cudaSuccess) e = cudaMemcpy(out, it->second.d_licvol, bytes, cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return cuda_fail(c, e, "download_lic_volume");
+  return VVLIC_OK;
+}
+
+extern "C" vvlic_status vvlic_synchronize(vvlic_ctx* c, void* stream, int32_t timeout_ms) {
+  if (!c) return VVLIC_ERR_BAD_HANDLE;
+  if (timeout_ms < 0) return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "synchronize: negative timeout");
+  DeviceGuard g(c->device);
+  const auto deadline = std::chrono::steady_clock::now() + std::chrono::microseconds((int64_t)timeout_ms * 1000);
+  cudaStream_t streams[2] = {(cudaStream_t)stream, c->stream};
+  for (cudaStream_t st : streams) {
+    for (;;) {
+      const cudaError_t e = cudaStreamQuery(st);
+      if (e == cudaSuccess) break;
+      if (e != cudaErrorNotReady) return cuda_fail(c, e, "synchronize");
+      if (std::chrono::steady_clock::now() >= deadline)
+        return fail(c, VVLIC_ERR_TIMEOUT, "synchronize: work still running after %d ms", timeout_ms);
+      std::this_thread::sleep_for(std::chrono::microseconds(50));
+    }
+  }
   return VVLIC_OK;
 }

@@ -30,6 +30,7 @@ __device__ __forceinline__ void load_tf(const RenderArgs& a, float* s_tf) {
 
 __device__ __forceinline__ void store_pixel(const RenderArgs& a, int px, int py, float4 dest, uint32_t samples) {
   const size_t pix = (size_t)py * a.W + px;
+  if (!in_range(a, (long long)pix, (long long)a.W * a.H, VVLIC_CHECK_IMAGE)) return;
   reinterpret_cast<float4*>(a.out)[pix] = dest;
   if (a.samples) a.samples[pix] = samples;
   if (a.tape_n) {

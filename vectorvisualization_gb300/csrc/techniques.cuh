@@ -22,12 +22,17 @@ __device__ __forceinline__ float sample_licvol(const TechArgs& t, float3 s) {
   repeat_axis_fast(s.x, t.ln[0], x0, x1, ax);
   repeat_axis_fast(s.y, t.ln[1], y0, y1, ay);
   repeat_axis_fast(s.z, t.ln[2], z0, z1, az);
-  const int nx = t.ln[0], nxy = t.ln[0] * t.ln[1];
+  // up to 2048^3 entries: row offsets in 64 bits
+  const size_t nx = (size_t)t.ln[0], nxy = nx * (size_t)t.ln[1];
   const float* v = t.licvol;
-  const float c00 = lerpf(__ldg(v + z0 * nxy + y0 * nx + x0), __ldg(v + z0 * nxy + y0 * nx + x1), ax);
-  const float c10 = lerpf(__ldg(v + z0 * nxy + y1 * nx + x0), __ldg(v + z0 * nxy + y1 * nx + x1), ax);
-  const float c01 = lerpf(__ldg(v + z1 * nxy + y0 * nx + x0), __ldg(v + z1 * nxy + y0 * nx + x1), ax);
-  const float c11 = lerpf(__ldg(v + z1 * nxy + y1 * nx + x0), __ldg(v + z1 * nxy + y1 * nx + x1), ax);
+  const float* r00 = v + z0 * nxy + y0 * nx;
+  const float* r10 = v + z0 * nxy + y1 * nx;
+  const float* r01 = v + z1 * nxy + y0 * nx;
+  const float* r11 = v + z1 * nxy + y1 * nx;
+  const float c00 = lerpf(__ldg(r00 + x0), __ldg(r00 + x1), ax);
+  const float c10 = lerpf(__ldg(r10 + x0), __ldg(r10 + x1), ax);
+  const float c01 = lerpf(__ldg(r01 + x0), __ldg(r01 + x1), ax);
+  const float c11 = lerpf(__ldg(r11 + x0), __ldg(r11 + x1), ax);
   return lerpf(lerpf(c00, c10, ay), lerpf(c01, c11, ay), az);
 }
 

@@ -156,6 +156,21 @@ __device__ __forceinline__ void clamp_axis(float s, int n, int& i0, int& i1, flo
   i1 = min(max(b + 1, 0), n - 1);
 }
 
+// Bounds-checked builds (-DVVLIC_BOUNDS_CHECK=1): gather indices, tape slots and image pixels
+// are tested against their buffers; an out-of-range one sets its VVLIC_CHECK_* bit in
+// counters[3] and is replaced by entry 0 (loads) or skipped (stores).  Otherwise the tests
+// compile away.
+#ifndef VVLIC_BOUNDS_CHECK
+#define VVLIC_BOUNDS_CHECK 0
+#endif
+__device__ __forceinline__ bool in_range(const RenderArgs& a, long long i, long long n, unsigned flag) {
+  if (VVLIC_BOUNDS_CHECK && (i < 0 || i >= n)) {
+    atomicOr(a.counters + 3, (unsigned long long)flag);
+    return false;
+  }
+  return true;
+}
+
 // ------------------------------------------------------------------------------------------
 // field sampling: texture3D(volumeSampler, s), LINEAR + CLAMP_TO_EDGE (dataset.cpp:351-357)
 // ------------------------------------------------------------------------------------------
@@ -169,7 +184,12 @@ template <int ST> struct Field<ST, kGather> {
     clamp_axis(s.y, a.n[1], y0, y1, ay);
     clamp_axis(s.z, a.n[2], z0, z1, az);
     const int nx = a.n[0], nxy = a.n[0] * a.n[1];
-    const int r00 = z0 * nxy + y0 * nx, r10 = z0 * nxy + y1 * nx, r01 = z1 * nxy + y0 * nx, r11 = z1 * nxy + y1 * nx;
+    int r00 = z0 * nxy + y0 * nx, r10 = z0 * nxy + y1 * nx, r01 = z1 * nxy + y0 * nx, r11 = z1 * nxy + y1 * nx;
+    if (VVLIC_BOUNDS_CHECK) {
+      const long long n = (long long)nxy * a.n[2];
+      if (!in_range(a, (long long)r00 + x0, n, VVLIC_CHECK_FIELD) || !in_range(a, (long long)r11 + x1, n, VVLIC_CHECK_FIELD))
+        r00 = r10 = r01 = r11 = x0 = x1 = 0;
+    }
     const void* f = a.field;
     return trilerp(Texel<ST>::load(f, r00 + x0), Texel<ST>::load(f, r00 + x1), Texel<ST>::load(f, r10 + x0),
                    Texel<ST>::load(f, r10 + x1), Texel<ST>::load(f, r01 + x0), Texel<ST>::load(f, r01 + x1),
@@ -191,13 +211,17 @@ __device__ __forceinline__ int cell_index(const RenderArgs& a, float3 s, float& 
   cell_axis(s.x, a.n[0], cx, ax);
   cell_axis(s.y, a.n[1], cy, ay);
   cell_axis(s.z, a.n[2], cz, az);
-  return (cz * (a.n[1] + 1) + cy) * (a.n[0] + 1) + cx;
+  const int c = (cz * (a.n[1] + 1) + cy) * (a.n[0] + 1) + cx;
+  if (VVLIC_BOUNDS_CHECK &&
+      !in_range(a, c, (long long)(a.n[0] + 1) * (a.n[1] + 1) * (a.n[2] + 1), VVLIC_CHECK_FIELD))
+    return 0;
+  return c;
 }
 
 template <> struct Field<VVLIC_STORAGE_F32, kCell> {  // 128-byte cells, eight 16-byte loads
   static __device__ __forceinline__ float4 sample(const RenderArgs& a, float3 s) {
     float ax, ay, az;
-    const float4* c = reinterpret_cast<const float4*>(a.field) + 8 * cell_index(a, s, ax, ay, az);
+    const float4* c = reinterpret_cast<const float4*>(a.field) + 8 * (size_t)cell_index(a, s, ax, ay, az);
     return trilerp(__ldg(c + 0), __ldg(c + 1), __ldg(c + 2), __ldg(c + 3), __ldg(c + 4), __ldg(c + 5), __ldg(c + 6),
                    __ldg(c + 7), ax, ay, az);
   }
@@ -205,7 +229,7 @@ template <> struct Field<VVLIC_STORAGE_F32, kCell> {  // 128-byte cells, eight 1
 template <int ST> struct Field<ST, kCell> {  // F16 / BF16: 64-byte cells, four 16-byte loads
   static __device__ __forceinline__ float4 sample(const RenderArgs& a, float3 s) {
     float ax, ay, az;
-    const uint4* c = reinterpret_cast<const uint4*>(a.field) + 4 * cell_index(a, s, ax, ay, az);
+    const uint4* c = reinterpret_cast<const uint4*>(a.field) + 4 * (size_t)cell_index(a, s, ax, ay, az);
     uint4 q0 = __ldg(c + 0), q1 = __ldg(c + 1), q2 = __ldg(c + 2), q3 = __ldg(c + 3);
     return trilerp(Texel<ST>::decode(make_uint2(q0.x, q0.y)), Texel<ST>::decode(make_uint2(q0.z, q0.w)),
                    Texel<ST>::decode(make_uint2(q1.x, q1.y)), Texel<ST>::decode(make_uint2(q1.z, q1.w)),
@@ -216,7 +240,7 @@ template <int ST> struct Field<ST, kCell> {  // F16 / BF16: 64-byte cells, four 
 template <> struct Field<VVLIC_STORAGE_UNORM8, kCell> {  // 32-byte cells, two 16-byte loads
   static __device__ __forceinline__ float4 sample(const RenderArgs& a, float3 s) {
     float ax, ay, az;
-    const uint4* c = reinterpret_cast<const uint4*>(a.field) + 2 * cell_index(a, s, ax, ay, az);
+    const uint4* c = reinterpret_cast<const uint4*>(a.field) + 2 * (size_t)cell_index(a, s, ax, ay, az);
     uint4 q0 = __ldg(c + 0), q1 = __ldg(c + 1);
     return trilerp(unorm8x4(q0.x), unorm8x4(q0.y), unorm8x4(q0.z), unorm8x4(q0.w), unorm8x4(q1.x), unorm8x4(q1.y),
                    unorm8x4(q1.z), unorm8x4(q1.w), ax, ay, az);
@@ -257,7 +281,12 @@ template <> struct Noise<kGather> {
     repeat_axis(s.z, a.m[2], z0, z1, az);
     const float k = 1.0f / 255.0f;
     const int mx = a.m[0], mxy = a.m[0] * a.m[1];
-    const int r00 = z0 * mxy + y0 * mx, r10 = z0 * mxy + y1 * mx, r01 = z1 * mxy + y0 * mx, r11 = z1 * mxy + y1 * mx;
+    int r00 = z0 * mxy + y0 * mx, r10 = z0 * mxy + y1 * mx, r01 = z1 * mxy + y0 * mx, r11 = z1 * mxy + y1 * mx;
+    if (VVLIC_BOUNDS_CHECK) {
+      const long long n = (long long)mxy * a.m[2];
+      if (!in_range(a, (long long)r00 + x0, n, VVLIC_CHECK_NOISE) || !in_range(a, (long long)r11 + x1, n, VVLIC_CHECK_NOISE))
+        r00 = r10 = r01 = r11 = x0 = x1 = 0;
+    }
     if (RGBA) {
       const uint32_t* t = reinterpret_cast<const uint32_t*>(a.noise);
       uint32_t t000 = __ldg(t + r00 + x0), t100 = __ldg(t + r00 + x1), t010 = __ldg(t + r10 + x0),
@@ -313,9 +342,10 @@ template <> struct Noise<kCell> {
     const float bx = 1.0f - ax, by = 1.0f - ay, bz = 1.0f - az;
     const float w00 = by * bz, w10 = ay * bz, w01 = by * az, w11 = ay * az;
     const float w[8] = {bx * w00, ax * w00, bx * w10, ax * w10, bx * w01, ax * w01, bx * w11, ax * w11};
-    const int cidx = (z0 * a.m[1] + y0) * a.m[0] + x0;
+    int cidx = (z0 * a.m[1] + y0) * a.m[0] + x0;
+    if (VVLIC_BOUNDS_CHECK && !in_range(a, cidx, (long long)a.m[0] * a.m[1] * a.m[2], VVLIC_CHECK_NOISE)) cidx = 0;
     if (RGBA) {
-      const uint4* c = reinterpret_cast<const uint4*>(a.noise) + 2 * cidx;
+      const uint4* c = reinterpret_cast<const uint4*>(a.noise) + 2 * (size_t)cidx;
       const uint4 q0 = __ldg(c), q1 = __ldg(c + 1);
       const uint32_t t[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
       float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -361,6 +391,12 @@ __device__ __forceinline__ float sample_scalar(const RenderArgs& a, float3 s) {
   clamp_axis(s.z, a.sn[2], z0, z1, az);
   const int nx = a.sn[0], nxy = a.sn[0] * a.sn[1];
   const float* t = a.scalar;
+  if (VVLIC_BOUNDS_CHECK) {
+    const long long n = (long long)nxy * a.sn[2];
+    if (!in_range(a, (long long)z0 * nxy + y0 * nx + x0, n, VVLIC_CHECK_SCALAR) ||
+        !in_range(a, (long long)z1 * nxy + y1 * nx + x1, n, VVLIC_CHECK_SCALAR))
+      x0 = x1 = y0 = y1 = z0 = z1 = 0;
+  }
   float c00 = lerpf(__ldg(t + z0 * nxy + y0 * nx + x0), __ldg(t + z0 * nxy + y0 * nx + x1), ax);
   float c10 = lerpf(__ldg(t + z0 * nxy + y1 * nx + x0), __ldg(t + z0 * nxy + y1 * nx + x1), ax);
   float c01 = lerpf(__ldg(t + z1 * nxy + y0 * nx + x0), __ldg(t + z1 * nxy + y0 * nx + x1), ax);
@@ -703,6 +739,19 @@ __device__ __forceinline__ size_t tape_entry(const RenderArgs& a, int px, int py
 __device__ __forceinline__ size_t tape_ck_entry(const RenderArgs& a, int px, int py, uint32_t s) {
   return (tape_tile(a, px, py) * (size_t)a.tape_nck + s) * 64 + tape_lane(px, py);
 }
+// entries of the per-sample arrays and of the checkpoint array (VVLIC_BOUNDS_CHECK builds)
+__device__ __forceinline__ long long tape_entries(const RenderArgs& a) {
+  return (long long)((a.W + kTapeTileW - 1) / kTapeTileW) * ((a.H + kTapeTileH - 1) / kTapeTileH) * 32 *
+         a.tape_stride;
+}
+__device__ __forceinline__ long long tape_ck_entries(const RenderArgs& a) {
+  return (long long)((a.W + kTapeTileW - 1) / kTapeTileW) * ((a.H + kTapeTileH - 1) / kTapeTileH) * 64 *
+         a.tape_nck;
+}
+__device__ __forceinline__ size_t tape_entry_checked(const RenderArgs& a, int px, int py, uint32_t k) {
+  const size_t e = tape_entry(a, px, py, k);
+  return in_range(a, (long long)e, tape_entries(a), VVLIC_CHECK_TAPE) ? e : 0;
+}
 
 // The whole lic3d_fragment.glsl main() for one pixel: returns dest, counts samples.
 template <int ST, int FL, int NL, int INTEG, bool GRAD>
@@ -725,11 +774,15 @@ __device__ __forceinline__ float4 trace_pixel(const RenderArgs& a, const float* 
       il.w *= a.intensity_scale;
       if (a.tape_is) {  // record for the adjoint
         if (samples % kSegment == 0 && samples / kSegment < (uint32_t)a.tape_nck) {
-          float4* ck = a.tape_ck + tape_ck_entry(a, px, py, samples / kSegment);
-          ck[0] = make_float4(pos.x, pos.y, pos.z, 0.f);
-          ck[32] = dest;
+          const size_t ce = tape_ck_entry(a, px, py, samples / kSegment);
+          if (in_range(a, (long long)ce + 32, tape_ck_entries(a), VVLIC_CHECK_TAPE)) {
+            float4* ck = a.tape_ck + ce;
+            ck[0] = make_float4(pos.x, pos.y, pos.z, 0.f);
+            ck[32] = dest;
+          }
         }
-        if (samples < (uint32_t)a.tape_stride) {
+        if (samples < (uint32_t)a.tape_stride &&
+            in_range(a, (long long)tape_entry(a, px, py, samples), tape_entries(a), VVLIC_CHECK_TAPE)) {
           const size_t e = tape_entry(a, px, py, samples);
           a.tape_is[e] = make_float2(il.w, tfc);
           if (GRAD) {
@@ -780,11 +833,15 @@ __device__ __forceinline__ float4 trace_pixel2(const RenderArgs& a, const float*
       l.w *= a.intensity_scale;
       if (a.tape_is) {  // record for the adjoint
         if (samples % kSegment == 0 && samples / kSegment < (uint32_t)a.tape_nck) {
-          float4* ck = a.tape_ck + tape_ck_entry(a, px, py, samples / kSegment);
-          ck[0] = make_float4(p.x, p.y, p.z, 0.f);
-          ck[32] = dest;
+          const size_t ce = tape_ck_entry(a, px, py, samples / kSegment);
+          if (in_range(a, (long long)ce + 32, tape_ck_entries(a), VVLIC_CHECK_TAPE)) {
+            float4* ck = a.tape_ck + ce;
+            ck[0] = make_float4(p.x, p.y, p.z, 0.f);
+            ck[32] = dest;
+          }
         }
-        if (samples < (uint32_t)a.tape_stride) {
+        if (samples < (uint32_t)a.tape_stride &&
+            in_range(a, (long long)tape_entry(a, px, py, samples), tape_entries(a), VVLIC_CHECK_TAPE)) {
           const size_t e = tape_entry(a, px, py, samples);
           a.tape_is[e] = make_float2(l.w, tfc);
           if (GRAD) {

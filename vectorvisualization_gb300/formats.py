@@ -57,7 +57,7 @@ def read_dat(info: DatInfo, timestep: int | None = None) -> np.ndarray:
     nx, ny, nz = info.resolution
     dt = info.dtype
     if dt is None:
-        raise capi.VVLICError(capi.ERR_FORMAT if hasattr(capi, "ERR_FORMAT") else 10, "read_dat: no data type")
+        raise capi.VVLICError(capi.ERR_FORMAT, "read_dat: no data type")
     out = np.empty((nz, ny, nx, info.components), dt)
     st = capi.load().vvlic_dat_read(C.byref(info._c), t, out.ctypes.data, out.nbytes)
     if st:
@@ -69,7 +69,7 @@ def load_vector_dataset(path: str, timestep: int | None = None):
     """VectorDataSet::loadData: a 3-component UCHAR or FLOAT field and its slice distances."""
     info = parse_dat(path)
     if info.components != 3 or info.format not in (capi.DAT_UCHAR, capi.DAT_FLOAT):
-        raise capi.VVLICError(10, f"{path} is not a 3-component UCHAR/FLOAT vector data set")
+        raise capi.VVLICError(capi.ERR_FORMAT, f"{path} is not a 3-component UCHAR/FLOAT vector data set")
     return read_dat(info, timestep), info.slice_thickness
 
 
