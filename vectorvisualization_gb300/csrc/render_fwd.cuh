@@ -18,9 +18,10 @@ constexpr int kThreads = 128;
 // Minimum resident CTAs per SM requested from the compiler for the render kernels, i.e. a cap
 // of 65536 / (kThreads * VVLIC_MIN_BLOCKS) registers per thread.  6 (80 registers, no spills)
 // measured 155 Gsample-steps/s on the lit 1024^2 frame against 142 with the compiler's own
-// choice; 8 (64 registers, ~100 B spilled) measured the same as 6.
+// choice; 7 (73 registers, ~60 B spilled) beat 6 on the same GPU by 2 % (lit 1024^2 frame),
+// 5 % (the 64-volume batch) and 1 % (the 512^3 RK4 frame); 8 (64 registers) measured as 6.
 #ifndef VVLIC_MIN_BLOCKS
-#define VVLIC_MIN_BLOCKS 6
+#define VVLIC_MIN_BLOCKS 7
 #endif
 
 __device__ __forceinline__ void load_tf(const RenderArgs& a, float* s_tf) {
