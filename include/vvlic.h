@@ -284,6 +284,8 @@ vvlic_status vvlic_upload_scalar(vvlic_ctx* ctx, const float* scalar,
  * TF_AlphaOpac).  Either may be NULL to keep the current table.  Initial tables are the
  * reference default (transferEdit.cpp:76-82). */
 vvlic_status vvlic_set_tf(vvlic_ctx* ctx, const float* rgba, const float* opacity);
+/* The current tables (either pointer may be NULL). */
+vvlic_status vvlic_get_tf(const vvlic_ctx* ctx, float* rgba, float* opacity);
 
 /* Filter kernel: LICFilter::createTexture (dataset.cpp:1470-1500) + Renderer::setLICFilter.
  * The tap weights w[-L_b..L_f] and the inverse filter area (calcFilterKernelInvArea,
@@ -469,6 +471,25 @@ vvlic_status vvlic_noise_write(const char* path, const uint8_t* noise, const int
 enum { VVLIC_IMAGE_PPM = 0, VVLIC_IMAGE_PNG = 1 };
 vvlic_status vvlic_image_write(const char* path, const float* rgba, int32_t w, int32_t h, int32_t kind,
                                int32_t composite);
+
+/* pngRead (imageUtils.cpp:20-100): an 8-bit gray, gray+alpha, RGB or RGBA PNG, rows top first,
+ * `channels` bytes per pixel (interlaced images: VVLIC_ERR_UNSUPPORTED).  With out == NULL only
+ * w, h and channels are written. */
+vvlic_status vvlic_png_read(const char* path, uint8_t* out, uint64_t capacity, int32_t* w, int32_t* h,
+                            int32_t* channels);
+/* LICFilter::loadData (dataset.cpp:1416-1467) + Renderer::setLICFilter: the first channel of
+ * the PNG's first row becomes the filter table (centred in the next power of two, GL_CLAMP). */
+vvlic_status vvlic_load_filter_png(vvlic_ctx* ctx, const char* path);
+/* TransferEdit::loadTF (transferEdit.cpp:224-313) with setTFFileNames (:113-158): `name`
+ * becomes "<name>_rgba.png" / "<name>_alpha.png" (or the suffixes go before the extension).
+ * The first 256 pixels of the RGBA file set TF r, g, b (gray copied) and alpha (a second or
+ * fourth channel).  As in the reference (`!loadRGBATF() && !loadAlphaOpacTF()`), the
+ * alpha/opacity file (first channel alpha, second opacity) is read only when the RGBA file
+ * cannot be. */
+vvlic_status vvlic_load_tf_png(vvlic_ctx* ctx, const char* name);
+/* TransferEdit::saveTF (transferEdit.cpp:163-221): 256 x 10 RGBA and gray+alpha (alpha,
+ * opacity) PNGs of the current tables, each entry round(255 * v). */
+vvlic_status vvlic_save_tf_png(vvlic_ctx* ctx, const char* name);
 
 /* Message of the last failing call of this section on the calling thread. */
 const char* vvlic_io_error(void);

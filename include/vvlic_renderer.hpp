@@ -108,6 +108,16 @@ class Renderer {
   void setLICFilter(const unsigned char* table, int width, int clamp = VVLIC_KERNEL_CLAMP_BORDER) {
     check(vvlic_set_filter_table(ctx_, table, width, clamp), "setLICFilter");
   }
+  /* LICFilter::loadData(png) + setLICFilter */
+  void loadFilter(const char* png) {
+    vvlic_status s = vvlic_load_filter_png(ctx_, png);
+    if (s != VVLIC_OK) throw Error(s, std::string("loadFilter: ") + vvlic_io_error());
+  }
+  /* TransferEdit::loadTF(name) + setTFrgbTex / setTFalphaOpacTex */
+  void loadTF(const char* name) {
+    vvlic_status s = vvlic_load_tf_png(ctx_, name);
+    if (s != VVLIC_OK) throw Error(s, std::string("loadTF: ") + vvlic_io_error());
+  }
   /* LICFilter::createBoxFilter */
   void setBoxFilter(int width = 256) {
     unsigned char t[1024];

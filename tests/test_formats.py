@@ -225,3 +225,128 @@ def test_upload_dat_matches_upload_field(ctx, oracle, tmp_path):
     formats.write_dat(p2, None, timesteps=steps)
     vid = ctx.upload_dat(p2, timestep=1)
     np.testing.assert_array_equal(ctx.download_field(vid, (6, 6, 6), "f32"), oracle.encode_field(steps[1]))
+
+
+# ---- PNG reading (pngRead) and the TF / filter PNG loaders -----------------------------------
+def _png(path, img, filters, level=9, ctype=None, depth=8, interlace=0, corrupt=False):
+    """A PNG written here with Python's zlib and per-row filter types (the forward filters)."""
+    h, w = img.shape[:2]
+    ch = img.shape[2] if img.ndim == 3 else 1
+    ctype = ctype if ctype is not None else {1: 0, 2: 4, 3: 2, 4: 6}[ch]
+    a = img.reshape(h, w * ch).astype(np.int64)
+    raw = bytearray()
+    for y in range(h):
+        ft = filters[y % len(filters)]
+        row = a[y]
+        up = a[y - 1] if y else np.zeros_like(row)
+        left = np.concatenate([np.zeros(ch, np.int64), row[:-ch]])
+        ul = np.concatenate([np.zeros(ch, np.int64), up[:-ch]])
+        if ft == 0:
+            pred = np.zeros_like(row)
+        elif ft == 1:
+            pred = left
+        elif ft == 2:
+            pred = up
+        elif ft == 3:
+            pred = (left + up) // 2
+        else:
+            pa, pb, pc = np.abs(up - ul), np.abs(left - ul), np.abs(left + up - 2 * ul)
+            pred = np.where((pa <= pb) & (pa <= pc), left, np.where(pb <= pc, up, ul))
+        raw.append(ft)
+        raw += bytes(((row - pred) & 0xFF).astype(np.uint8))
+
+    def chunk(t, d):
+        c = struct.pack(">I", len(d)) + t + d
+        crc = zlib.crc32(t + d) & 0xFFFFFFFF
+        return c + struct.pack(">I", crc ^ (1 if corrupt and t == b"IDAT" else 0))
+
+    z = zlib.compress(bytes(raw), level)
+    data = b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, depth, ctype, 0, 0, interlace))
+    data += chunk(b"IDAT", z[: len(z) // 2]) + chunk(b"IDAT", z[len(z) // 2:]) + chunk(b"IEND", b"")
+    with open(path, "wb") as fh:
+        fh.write(data)
+
+
+@pytest.mark.parametrize("channels", [1, 2, 3, 4])
+@pytest.mark.parametrize("level", [0, 1, 9])
+def test_png_read_all_filters_and_colour_types(tmp_path, channels, level):
+    rng = np.random.default_rng(channels * 10 + level)
+    # smooth content compresses with back-references and dynamic codes; noise with literals
+    y, x = np.mgrid[0:23, 0:37]
+    smooth = ((x * 7 + y * 3) % 256).astype(np.uint8)
+    img = np.stack([smooth] * channels, -1) if channels > 1 else smooth[..., None]
+    img[::3] = rng.integers(0, 256, img[::3].shape, dtype=np.uint8)
+    p = str(tmp_path / "t.png")
+    _png(p, img, filters=[0, 1, 2, 3, 4, 4, 3], level=level)
+    np.testing.assert_array_equal(formats.read_png(p), img)
+
+
+def test_png_read_of_the_image_dump(tmp_path):
+    img = np.random.default_rng(4).uniform(0, 1, (9, 11, 4)).astype(np.float32)
+    p = str(tmp_path / "d.png")
+    formats.write_image(p, img)
+    want = np.clip((np.float32(255.0) * img).astype(np.int64), 0, 255).astype(np.uint8)[::-1]
+    np.testing.assert_array_equal(formats.read_png(p), want)
+
+
+def test_png_read_rejects_what_pngread_rejects(tmp_path):
+    img = np.zeros((4, 4, 3), np.uint8)
+    cases = {"depth16": dict(depth=16), "palette": dict(ctype=3), "interlaced": dict(interlace=1),
+             "crc": dict(corrupt=True)}
+    for name, kw in cases.items():
+        p = str(tmp_path / f"{name}.png")
+        _png(p, img, [0], **kw)
+        with pytest.raises(capi.VVLICError):
+            formats.read_png(p)
+    p = str(tmp_path / "text.png")
+    open(p, "wb").write(b"not a png at all")
+    with pytest.raises(capi.VVLICError, match="not a PNG"):
+        formats.read_png(p)
+    with pytest.raises(capi.VVLICError, match="cannot open"):
+        formats.read_png(str(tmp_path / "missing.png"))
+
+
+@pytest.mark.gpu
+def test_tf_and_filter_png_loaders(ctx, tmp_path):
+    rng = np.random.default_rng(8)
+    n = capi.TF_ENTRIES
+    # RGBA file present: r, g, b, a set; opacity untouched, the alpha file is not read
+    rgba = rng.integers(0, 256, (2, n, 4), dtype=np.uint8)
+    alpha = rng.integers(0, 256, (1, n, 2), dtype=np.uint8)
+    _png(str(tmp_path / "tf_rgba.png"), rgba, [1])
+    _png(str(tmp_path / "tf_alpha.png"), alpha, [2])
+    _, op0 = ctx.get_tf()
+    ctx.load_tf_png(str(tmp_path / "tf.png"))
+    got, op = ctx.get_tf()
+    np.testing.assert_array_equal(got, rgba[0].astype(np.float32) / 255.0)
+    np.testing.assert_array_equal(op, op0)
+    # no RGBA file: the alpha file sets alpha and opacity; a name without extension
+    _png(str(tmp_path / "only_alpha.png"), alpha, [4])
+    ctx.load_tf_png(str(tmp_path / "only"))
+    got2, op2 = ctx.get_tf()
+    np.testing.assert_array_equal(got2[:, :3], got[:, :3])
+    np.testing.assert_array_equal(got2[:, 3], alpha[0, :, 0].astype(np.float32) / 255.0)
+    np.testing.assert_array_equal(op2, alpha[0, :, 1].astype(np.float32) / 255.0)
+    with pytest.raises(capi.VVLICError):
+        ctx.load_tf_png(str(tmp_path / "nothing.png"))
+    # a gray RGBA file too short for 256 entries
+    _png(str(tmp_path / "short_rgba.png"), rng.integers(0, 256, (10, 20, 1), dtype=np.uint8), [0])
+    with pytest.raises(capi.VVLICError):
+        ctx.load_tf_png(str(tmp_path / "short.png"))
+    # save and load back
+    ctx.save_tf_png(str(tmp_path / "saved.png"))
+    a = formats.read_png(str(tmp_path / "saved_rgba.png"))
+    b = formats.read_png(str(tmp_path / "saved_alpha.png"))
+    assert a.shape == (10, n, 4) and b.shape == (10, n, 2)
+    np.testing.assert_array_equal(a[3], np.round(got2 * 255).astype(np.uint8))
+    np.testing.assert_array_equal(b[7, :, 1], np.round(op2 * 255).astype(np.uint8))
+    # filter kernel: the first channel of the first row, centred like vvlic_set_filter_table
+    k = np.zeros((3, 100, 2), np.uint8)
+    k[0, :, 0] = (255 * np.hanning(100)).astype(np.uint8)
+    _png(str(tmp_path / "kernel.png"), k, [3])
+    ctx.load_filter_png(str(tmp_path / "kernel.png"))
+    t1, ia1 = ctx.filter_taps()
+    ctx.set_filter_table(k[0, :, 0])
+    t2, ia2 = ctx.filter_taps()
+    np.testing.assert_array_equal(t1, t2)
+    assert ia1 == ia2 and ia1 != 0.5  # not the box filter

@@ -165,6 +165,11 @@ _SIGS = {
     "vvlic_image_write": (_I, [C.c_char_p, _P, _I, _I, _I, _I]),
     "vvlic_io_error": (C.c_char_p, []),
     "vvlic_synchronize": (_I, [_P, _P, _I]),
+    "vvlic_get_tf": (_I, [_P, _P, _P]),
+    "vvlic_png_read": (_I, [C.c_char_p, _P, C.c_uint64, C.POINTER(_I), C.POINTER(_I), C.POINTER(_I)]),
+    "vvlic_load_filter_png": (_I, [_P, C.c_char_p]),
+    "vvlic_load_tf_png": (_I, [_P, C.c_char_p]),
+    "vvlic_save_tf_png": (_I, [_P, C.c_char_p]),
     "vvlic_create": (_I, [C.POINTER(_P), _I]),
     "vvlic_destroy": (_I, [_P]),
     "vvlic_last_error": (C.c_char_p, [_P]),
@@ -440,6 +445,28 @@ class Context:
         self._check(self._lib.vvlic_get_illum_luts(self.h, out[0].ctypes.data, out[1].ctypes.data,
                                                     out[2].ctypes.data, None, None), "illum_luts")
         return out
+
+    def get_tf(self):
+        rgba = np.empty((TF_ENTRIES, 4), np.float32)
+        op = np.empty(TF_ENTRIES, np.float32)
+        self._check(self._lib.vvlic_get_tf(self.h, rgba.ctypes.data, op.ctypes.data), "get_tf")
+        return rgba, op
+
+    def _io(self, st: int, what: str):
+        if st:
+            msg = self._lib.vvlic_io_error().decode() or self._lib.vvlic_last_error(self.h).decode()
+            raise VVLICError(st, f"{what}: {msg}")
+
+    def load_tf_png(self, name: str):
+        """TransferEdit::loadTF: <name>_rgba.png (else <name>_alpha.png)."""
+        self._io(self._lib.vvlic_load_tf_png(self.h, os.fsencode(name)), "load_tf_png")
+
+    def save_tf_png(self, name: str):
+        self._io(self._lib.vvlic_save_tf_png(self.h, os.fsencode(name)), "save_tf_png")
+
+    def load_filter_png(self, path: str):
+        """LICFilter::loadData: the first row's first channel as the filter table."""
+        self._io(self._lib.vvlic_load_filter_png(self.h, os.fsencode(path)), "load_filter_png")
 
     def set_filter_table(self, table: np.ndarray, clamp: int = KERNEL_CLAMP_BORDER):
         t = np.ascontiguousarray(table, dtype=np.uint8)

@@ -630,6 +630,13 @@ extern "C" vvlic_status vvlic_set_tf(vvlic_ctx* c, const float* rgba, const floa
   return VVLIC_OK;
 }
 
+extern "C" vvlic_status vvlic_get_tf(const vvlic_ctx* c, float* rgba, float* opacity) {
+  if (!c) return VVLIC_ERR_BAD_HANDLE;
+  if (rgba) std::memcpy(rgba, c->tf, sizeof(float) * 4 * VVLIC_TF_ENTRIES);
+  if (opacity) std::memcpy(opacity, c->tf + 4 * VVLIC_TF_ENTRIES, sizeof(float) * VVLIC_TF_ENTRIES);
+  return VVLIC_OK;
+}
+
 extern "C" vvlic_status vvlic_set_filter_table(vvlic_ctx* c, const uint8_t* table, int32_t width, int32_t clamp_mode) {
   if (!c) return VVLIC_ERR_BAD_HANDLE;
   if (!table || width < 1 || width > 1024 || (clamp_mode != VVLIC_KERNEL_CLAMP_BORDER && clamp_mode != VVLIC_KERNEL_CLAMP_EDGE))

@@ -128,6 +128,20 @@ def write_image(path: str, rgba: np.ndarray, kind: str | None = None, composite:
         _err(st, f"write_image({path})")
 
 
+def read_png(path: str) -> np.ndarray:
+    """pngRead: (h, w, channels) uint8, rows top first (8-bit gray / gray+alpha / RGB / RGBA)."""
+    w, h, ch = capi._I(0), capi._I(0), capi._I(0)
+    lib = capi.load()
+    st = lib.vvlic_png_read(os.fsencode(path), None, 0, C.byref(w), C.byref(h), C.byref(ch))
+    if st:
+        _err(st, f"read_png({path})")
+    out = np.empty((h.value, w.value, ch.value), np.uint8)
+    st = lib.vvlic_png_read(os.fsencode(path), out.ctypes.data, out.nbytes, C.byref(w), C.byref(h), C.byref(ch))
+    if st:
+        _err(st, f"read_png({path})")
+    return out
+
+
 def present(path: str, rgba: np.ndarray):
     """The window image: the render composited over white, written as an image file."""
     write_image(path, rgba, composite=True)
