@@ -272,6 +272,10 @@ vvlic_status vvlic_volume_bytes(const vvlic_ctx* ctx, int32_t vol_id, uint64_t* 
  * and pack RGBA = (gradient, noise) like dataset.cpp:1270-1286.  Wrap is REPEAT. */
 vvlic_status vvlic_upload_noise(vvlic_ctx* ctx, const uint8_t* noise,
                                 int32_t mx, int32_t my, int32_t mz, int32_t mode);
+/* Noise with precomputed gradients: mx*my*mz RGBA texels (quantised gradient x, y, z, noise)
+ * as vvlic_upload_noise builds them; `mode` (SOBEL or CENTRAL) records their kind. */
+vvlic_status vvlic_upload_noise_rgba(vvlic_ctx* ctx, const uint8_t* rgba, int32_t mx, int32_t my, int32_t mz,
+                                     int32_t mode);
 
 /* Optional secondary scalar volume for the freqSampling gate (VolumeDataSet, dataset.cpp:840-1050,
  * Renderer::setScalarTex).  Host float32, values as the shader sees them (.r). */
@@ -455,6 +459,13 @@ vvlic_status vvlic_dat_read(const vvlic_dat_info* info, int32_t timestep, void* 
  * upload it with the .dat's slice thickness.  timestep < 0 takes timestep_begin. */
 vvlic_status vvlic_upload_dat(vvlic_ctx* ctx, const char* dat_path, int32_t timestep, int32_t storage,
                               int32_t* vol_id);
+
+/* NoiseDataSet::createTexture with the gradient cache (dataset.cpp:1230-1286, gradient.cpp:91-187):
+ * load the noise file `path`; with gradients, take them from "<path>.grd" when that file holds
+ * at least 3 bytes per voxel (the quantised x, y, z of quantizeGradients, x fastest), else
+ * compute them on the device and write that file for the next time (a failed write is not an
+ * error, as in the reference).  The cache does not record the gradient mode. */
+vvlic_status vvlic_upload_noise_file(vvlic_ctx* ctx, const char* path, int32_t mode);
 
 /* Noise volume file of NoiseDataSet::loadRawData (dataset.cpp:1347-1389): a 12-byte header of
  * three native int32 sizes (x, y, z) followed by x*y*z bytes, x fastest.  With out == NULL only

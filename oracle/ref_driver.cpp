@@ -85,3 +85,26 @@ extern "C" int vvref_dat_read(const char* path, int timestep, void* out, long by
   delete[] (char*)d;
   return 0;
 }
+
+/* saveGradients (gradient.cpp:149-187) of the reference's own gradients: writes "<path>.grd". */
+extern "C" int vvref_save_gradients(const unsigned char* noise, const int m[3], const char* path) {
+  VolumeData vd;
+  vd.data = (void*)noise;
+  vd.newData = NULL;
+  vd.dataType = DATRAW_UCHAR;
+  vd.dataDim = 1;
+  for (int i = 0; i < 3; ++i) {
+    vd.size[i] = m[i];
+    vd.texSize[i] = m[i];
+    vd.sliceDist[i] = 1.0f;
+  }
+  float* g = computeGradients(&vd);
+  if (!g) return -1;
+  filterGradients(&vd, g);
+  unsigned char* q = (unsigned char*)quantizeGradients(&vd, g, DATRAW_UCHAR);
+  std::string p(path);
+  const bool ok = q && saveGradients(&vd, &p[0], q, DATRAW_UCHAR, false);
+  delete[] g;
+  delete[] q;
+  return ok ? 0 : -2;
+}

@@ -350,3 +350,51 @@ def test_tf_and_filter_png_loaders(ctx, tmp_path):
     t2, ia2 = ctx.filter_taps()
     np.testing.assert_array_equal(t1, t2)
     assert ia1 == ia2 and ia1 != 0.5  # not the box filter
+
+
+# ---- the noise gradient cache (.grd) ------------------------------------------------------------
+def test_reference_grd_layout_is_the_quantised_gradient_xyz(tmp_path):
+    """The reference's own saveGradients writes 3 bytes per voxel, x fastest: the RGB of the
+    gradient texels (pins the cache format vvlic_upload_noise_file reads and writes)."""
+    lib = _ref_lib()
+    from oracle import pyoracle
+
+    noise = np.random.default_rng(11).integers(0, 256, (5, 6, 7), dtype=np.uint8)
+    dims = np.array([7, 6, 5], np.int32)
+    base = str(tmp_path / "n")
+    lib.vvref_save_gradients.argtypes = [C.c_void_p, C.c_void_p, C.c_char_p]
+    assert lib.vvref_save_gradients(noise.ctypes.data, dims.ctypes.data, base.encode()) == 0
+    grd = np.fromfile(base + ".grd", np.uint8)
+    want = pyoracle.noise_gradients(noise, capi.NOISE_GRAD_SOBEL)[..., :3]
+    np.testing.assert_array_equal(grd, want.reshape(-1))
+
+
+@pytest.mark.gpu
+def test_noise_file_gradient_cache(ctx, oracle, tmp_path):
+    noise = np.random.default_rng(12).integers(0, 256, (9, 10, 11), dtype=np.uint8)
+    path = str(tmp_path / "noise_11")
+    formats.write_noise(path, noise)
+    ctx.upload_noise_file(path, capi.NOISE_GRAD_SOBEL)
+    ref = oracle.noise_gradients(noise, capi.NOISE_GRAD_SOBEL)
+    np.testing.assert_array_equal(ctx.download_noise((11, 10, 9), 4), ref)
+    # the cache written for the next time: the quantised gradient xyz
+    grd = np.fromfile(path + ".grd", np.uint8)
+    np.testing.assert_array_equal(grd, ref[..., :3].reshape(-1))
+    # a cache present is used as is (the reference does not record the gradient mode either)
+    fake = np.full(grd.shape, 7, np.uint8)
+    fake.tofile(path + ".grd")
+    ctx.upload_noise_file(path, capi.NOISE_GRAD_CENTRAL)
+    got = ctx.download_noise((11, 10, 9), 4)
+    assert (got[..., :3] == 7).all()
+    np.testing.assert_array_equal(got[..., 3], noise)
+    # a short cache is ignored and rewritten
+    fake[:10].tofile(path + ".grd")
+    ctx.upload_noise_file(path, capi.NOISE_GRAD_SOBEL)
+    np.testing.assert_array_equal(ctx.download_noise((11, 10, 9), 4), ref)
+    assert os.path.getsize(path + ".grd") == 3 * noise.size
+    # scalar noise needs no cache
+    p2 = str(tmp_path / "noise_scalar")
+    formats.write_noise(p2, noise)
+    ctx.upload_noise_file(p2, capi.NOISE_SCALAR)
+    assert not os.path.exists(p2 + ".grd")
+    np.testing.assert_array_equal(ctx.download_noise((11, 10, 9), 1), noise)

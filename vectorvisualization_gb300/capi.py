@@ -166,6 +166,8 @@ _SIGS = {
     "vvlic_io_error": (C.c_char_p, []),
     "vvlic_synchronize": (_I, [_P, _P, _I]),
     "vvlic_get_tf": (_I, [_P, _P, _P]),
+    "vvlic_upload_noise_rgba": (_I, [_P, _P, _I, _I, _I, _I]),
+    "vvlic_upload_noise_file": (_I, [_P, C.c_char_p, _I]),
     "vvlic_png_read": (_I, [C.c_char_p, _P, C.c_uint64, C.POINTER(_I), C.POINTER(_I), C.POINTER(_I)]),
     "vvlic_load_filter_png": (_I, [_P, C.c_char_p]),
     "vvlic_load_tf_png": (_I, [_P, C.c_char_p]),
@@ -456,6 +458,15 @@ class Context:
         if st:
             msg = self._lib.vvlic_io_error().decode() or self._lib.vvlic_last_error(self.h).decode()
             raise VVLICError(st, f"{what}: {msg}")
+
+    def upload_noise_file(self, path: str, mode: int = NOISE_GRAD_SOBEL):
+        """A noise file, with gradients from (or cached to) <path>.grd."""
+        self._io(self._lib.vvlic_upload_noise_file(self.h, os.fsencode(path), mode), "upload_noise_file")
+
+    def upload_noise_rgba(self, rgba: np.ndarray, mode: int = NOISE_GRAD_SOBEL):
+        a = np.ascontiguousarray(rgba, dtype=np.uint8)
+        mz, my, mx = a.shape[:3]
+        self._check(self._lib.vvlic_upload_noise_rgba(self.h, a.ctypes.data, mx, my, mz, mode), "upload_noise_rgba")
 
     def load_tf_png(self, name: str):
         """TransferEdit::loadTF: <name>_rgba.png (else <name>_alpha.png)."""

@@ -592,6 +592,30 @@ extern "C" vvlic_status vvlic_upload_noise(vvlic_ctx* c, const uint8_t* noise, i
   return VVLIC_OK;
 }
 
+extern "C" vvlic_status vvlic_upload_noise_rgba(vvlic_ctx* c, const uint8_t* rgba, int32_t mx, int32_t my, int32_t mz,
+                                               int32_t mode) {
+  if (!c) return VVLIC_ERR_BAD_HANDLE;
+  const int m[3] = {mx, my, mz};
+  if (!rgba || !valid_dims(m)) return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "upload_noise_rgba: bad arguments");
+  if (mode != VVLIC_NOISE_GRAD_SOBEL && mode != VVLIC_NOISE_GRAD_CENTRAL)
+    return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "upload_noise_rgba: mode %d is not a gradient mode", mode);
+  DeviceGuard g(c->device);
+  free_noise(c->noise);
+  NoiseTex& n = c->noise;
+  const size_t bytes = (size_t)mx * my * mz * 4;
+  n.m[0] = mx;
+  n.m[1] = my;
+  n.m[2] = mz;
+  n.ch = 4;
+  n.mode = mode;
+  cudaError_t e = cudaMalloc(&n.d_texels, bytes);
+  if (e != cudaSuccess) return cuda_fail(c, e, "noise allocation");
+  e = cudaMemcpyAsync(n.d_texels, rgba, bytes, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "upload_noise_rgba");
+  return VVLIC_OK;
+}
+
 extern "C" vvlic_status vvlic_upload_scalar(vvlic_ctx* c, const float* scalar, int32_t nx, int32_t ny, int32_t nz) {
   if (!c) return VVLIC_ERR_BAD_HANDLE;
   const int n[3] = {nx, ny, nz};

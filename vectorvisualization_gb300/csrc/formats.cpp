@@ -717,3 +717,40 @@ extern "C" vvlic_status vvlic_save_tf_png(vvlic_ctx* ctx, const char* name) {
   }
   return VVLIC_OK;
 }
+
+extern "C" vvlic_status vvlic_upload_noise_file(vvlic_ctx* ctx, const char* path, int32_t mode) {
+  if (!ctx) return VVLIC_ERR_BAD_HANDLE;
+  if (!path) return io_fail(VVLIC_ERR_INVALID_ARGUMENT, "upload_noise_file: null path");
+  int32_t d[3];
+  vvlic_status st = vvlic_noise_read(path, nullptr, 0, d);
+  if (st) return st;
+  const size_t n = (size_t)d[0] * d[1] * d[2];
+  std::vector<uint8_t> noise(n);
+  if ((st = vvlic_noise_read(path, noise.data(), n, d))) return st;
+  if (mode == VVLIC_NOISE_SCALAR) return vvlic_upload_noise(ctx, noise.data(), d[0], d[1], d[2], mode);
+  // loadGradients (gradient.cpp:112-146): "<path>.grd" with at least 3 bytes per voxel
+  const std::string grd = std::string(path) + ".grd";
+  std::vector<uint8_t> cached;
+  if (read_file(grd.c_str(), cached) == VVLIC_OK && cached.size() >= 3 * n) {
+    std::vector<uint8_t> rgba(4 * n);
+    for (size_t i = 0; i < n; ++i) {  // the RGBA pack of dataset.cpp:1270-1286
+      rgba[4 * i] = cached[3 * i];
+      rgba[4 * i + 1] = cached[3 * i + 1];
+      rgba[4 * i + 2] = cached[3 * i + 2];
+      rgba[4 * i + 3] = noise[i];
+    }
+    return vvlic_upload_noise_rgba(ctx, rgba.data(), d[0], d[1], d[2], mode);
+  }
+  if ((st = vvlic_upload_noise(ctx, noise.data(), d[0], d[1], d[2], mode))) return st;
+  // saveGradients (gradient.cpp:149-187): the quantised x, y, z per voxel for the next time
+  std::vector<uint8_t> rgba(4 * n), xyz(3 * n);
+  if ((st = vvlic_download_noise(ctx, rgba.data(), rgba.size()))) return st;
+  for (size_t i = 0; i < n; ++i)
+    for (int c = 0; c < 3; ++c) xyz[3 * i + c] = rgba[4 * i + c];
+  FILE* fp = fopen(grd.c_str(), "wb");
+  if (fp) {
+    const bool ok = fwrite(xyz.data(), 1, xyz.size(), fp) == xyz.size();
+    if (fclose(fp) != 0 || !ok) remove(grd.c_str());  // no partial cache
+  }
+  return VVLIC_OK;
+}
