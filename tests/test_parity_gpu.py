@@ -342,6 +342,17 @@ def test_one_sided_streamlines(ctx, oracle):
     check_small(ctx, oracle, small(steps_forward=5, steps_backward=0))
 
 
+def test_longest_streamlines(ctx, oracle):
+    """L_f = L_b = VVLIC_MAX_STEPS (513 taps), asymmetric lengths at the limit, every integrator."""
+    for integ, lb, lf in ((capi.HEUN, capi.MAX_STEPS, capi.MAX_STEPS), (capi.RK4, capi.MAX_STEPS, 3),
+                          (capi.EULER, 1, capi.MAX_STEPS)):
+        w = small(integ, steps_backward=lb, steps_forward=lf)
+        w.width, w.height = 12, 10
+        check_small(ctx, oracle, w)
+    with pytest.raises(capi.VVLICError):
+        ctx.set_params(small(steps_forward=capi.MAX_STEPS + 1).params)
+
+
 def test_tiny_images_and_volumes(ctx, oracle):
     w = small()
     w.width, w.height = 1, 1
@@ -412,3 +423,37 @@ def test_errors_are_reported(ctx):
     ctx.free_volume(vid)
     with pytest.raises(capi.VVLICError):
         ctx.render(vid, 8, 8)
+
+
+def test_contexts_are_independent_across_threads(oracle):
+    """Contexts used from separate host threads at the same time (ctypes releases the GIL
+    during each call) render exactly what they render alone."""
+    import threading
+
+    cases = [small(capi.HEUN), small(capi.RK4, illum=capi.ILLUM_GRADIENT), small(capi.EULER, speed_of_flow=1)]
+    cases[1].noise_mode = capi.NOISE_GRAD_CENTRAL
+    alone = []
+    for w in cases:
+        with capi.Context(0) as c:
+            vid = wl.setup_context(c, w)
+            alone.append(c.render(vid, w.width, w.height))
+    results = [None] * len(cases)
+    errors = []
+
+    def run(k):
+        try:
+            with capi.Context(0) as c:
+                vid = wl.setup_context(c, cases[k])
+                for _ in range(3):
+                    results[k] = c.render(vid, cases[k].width, cases[k].height)
+        except Exception as e:  # surfaced below
+            errors.append(e)
+
+    threads = [threading.Thread(target=run, args=(k,)) for k in range(len(cases))]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors
+    for got, want in zip(results, alone):
+        np.testing.assert_array_equal(got, want)
