@@ -11,20 +11,25 @@
  *
  * What it follows (file:line within VectorVisualization/):
  *   GLSL hot path      shader/lic3d_fragment.glsl:5-99, shader/inc_lic.glsl:134-265,
- *                      shader/inc_illum.glsl:1-41 and 257-271, shader/inc_header.glsl:22-63
+ *                      shader/inc_illum.glsl:1-154 and 257-271, shader/inc_header.glsl:22-63
+ *   other techniques   shader/lic3d_slicing_fragment.glsl, vectorfield_fragment.glsl:39-101,
+ *                      lic3d_volume_fragment.glsl, raycast_lic3d_fragment.glsl, slicing.cpp:42-103
  *   uniforms           renderer.cpp:925-996 (setRenderVolParams)
  *   volume geometry    dataset.cpp:139-176 (VectorDataSet::loadData)
  *   view               camera.cpp:56-67 (Camera::setCamera), renderer.cpp:146, 682-736
- *   field encoding     dataset.cpp:533-635 (fillTexDataFloatInterp, interpolation index 0)
+ *   field encoding     dataset.cpp:533-635 (fillTexDataFloatInterp, with its time lerp)
  *   noise gradients    gradient.cpp:190-531, gradient.h:37-39, dataset.cpp:1270-1286
  *   filter kernel      dataset.cpp:1405-1413, 1470-1512
  *   transfer function  transferEdit.cpp:76-82, 480-543
+ *   line illumination  illumination.cpp:96-391 (Zoeckler and Mallo tables)
+ *   adjoint            reverse mode of the above (no reference counterpart), FD-checked
  * GL sampler behaviour (texel centres, LINEAR, CLAMP_TO_EDGE / REPEAT / GL_CLAMP with a zero
  * border, uint8 read as x/255) is restated from the OpenGL 2.1 specification, section 3.8.
  *
  * Parity of the GLSL part is unpinned by reference tests (the reference has none and its
- * inputs are not shipped); the preprocessing restatements are pinned against the reference's
- * own gradient.cpp compiled here (oracle/build_ref.sh).
+ * inputs are not shipped); the noise gradients are pinned against the reference's own
+ * gradient.cpp and the .dat reader against its reader.cpp, both compiled here
+ * (oracle/build_ref.sh).
  */
 #ifndef VVLIC_ORACLE_HPP_
 #define VVLIC_ORACLE_HPP_
