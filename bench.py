@@ -619,12 +619,6 @@ def run_ours(args, dist):
             if storage == w.storage:
                 variants[storage] = {"gss": value / dist.world, "ms": ms_per_step}
                 continue
-            note = None
-            if storage == "bf16" and args.sampler in ("texture", "hybrid"):
-                # no bf16 texture format: bf16 runs on the corner-packed cells
-                p.sampler = capi.SAMPLER["cell"]
-                ctx.set_params(p)
-                note = "cell sampler (no bf16 texture format)"
             vid2 = ctx.upload_field(w.field, storage=storage)
             with torch.cuda.stream(stream):
                 frame2 = lambda: ctx.render_device(vid2, out.data_ptr(), W, H, None, sh)  # noqa: E731
@@ -639,10 +633,6 @@ def run_ours(args, dist):
             ms = e0.elapsed_time(e1)
             s2 = ctx.stats()
             variants[storage] = {"gss": s2.sample_steps / (ms / 1e3) / 1e9, "ms": ms}
-            if note:
-                variants[storage]["sampler"] = note
-                p.sampler = capi.SAMPLER[args.sampler]
-                ctx.set_params(p)
             ctx.free_volume(vid2)
         line["storage_variants"] = variants
 

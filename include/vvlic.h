@@ -62,7 +62,8 @@ enum { VVLIC_STORAGE_F32 = 0, VVLIC_STORAGE_F16 = 1, VVLIC_STORAGE_BF16 = 2, VVL
  *   CELL    - corner-packed cells: the 8 corners of every trilinear cell stored contiguously
  *             (8x the memory, one or two vector loads per trilinear);
  *   TEXTURE - hardware-filtered cudaTextureObjects for field and noise (8-bit fixed-point
- *             filter weights);
+ *             filter weights); a BF16 field's texture is a half4 copy of its BF16 texels
+ *             (exact for the encoded texel values down to 2^-14);
  *   HYBRID  - field through the texture unit, noise from corner-packed cells through the
  *             load/store path, splitting the gathers over both L1 data pipes. */
 enum { VVLIC_SAMPLER_GATHER = 0, VVLIC_SAMPLER_CELL = 1, VVLIC_SAMPLER_TEXTURE = 2, VVLIC_SAMPLER_HYBRID = 3 };

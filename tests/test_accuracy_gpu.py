@@ -40,8 +40,7 @@ def c2_full(oracle):
     return w, refs
 
 
-CASES = [(st, sm) for st in ("f32", "f16", "bf16", "u8") for sm in ("gather", "cell", "texture", "hybrid")
-         if not (st == "bf16" and sm in ("texture", "hybrid"))]
+CASES = [(st, sm) for st in ("f32", "f16", "bf16", "u8") for sm in ("gather", "cell", "texture", "hybrid")]
 
 
 def test_accuracy_table(ctx, c2_full):

@@ -69,7 +69,7 @@ def target_image(oracle, w, taps, storage="f32"):
 @pytest.mark.parametrize("sampler,storage,lit", [("cell", "f32", False), ("hybrid", "f16", False),
                                                  ("gather", "f32", False), ("cell", "f32", "gradient"),
                                                  ("hybrid", "f16", "gradient"), ("cell", "f32", "zoeckler"),
-                                                 ("cell", "f32", "mallo")])
+                                                 ("cell", "f32", "mallo"), ("hybrid", "bf16", False)])
 def test_adjoint_matches_fp64_oracle(ctx, oracle, sampler, storage, lit):
     w, taps = case(sampler=sampler, storage=storage, lit=lit)
     target = target_image(oracle, w, taps, storage)

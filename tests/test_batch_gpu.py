@@ -32,10 +32,11 @@ def small_batch(ctx, n_vol=5, image=48, storage="f16", sampler="hybrid"):
     return jobs, outs, specs
 
 
-def test_batch_equals_single_renders(ctx):
+@pytest.mark.parametrize("storage", ["f16", "bf16"])
+def test_batch_equals_single_renders(ctx, storage):
     import torch
 
-    jobs, outs, specs = small_batch(ctx)
+    jobs, outs, specs = small_batch(ctx, storage=storage)
     stream = torch.cuda.Stream()
     ctx.batch_render(jobs, stream.cuda_stream)
     stream.synchronize()

@@ -64,7 +64,8 @@ VIEWS = [wl.ortho_view(), wl.perspective_view(wl.quat_axis_angle((1, 2, 0), 50.0
 
 
 @pytest.mark.parametrize("sampler,storage", [("gather", "f32"), ("cell", "f16"), ("cell", "bf16"), ("cell", "u8"),
-                                             ("texture", "f16"), ("hybrid", "u8"), ("hybrid", "f32")])
+                                             ("texture", "f16"), ("hybrid", "u8"), ("hybrid", "f32"),
+                                             ("hybrid", "bf16")])
 def test_no_out_of_range_access_and_same_images(checked_lib, sampler, storage):
     default = capi.load()
     for integ, illum in ((capi.EULER, capi.ILLUM_NONE), (capi.RK4, capi.ILLUM_GRADIENT),

@@ -211,11 +211,6 @@ def c2_refs(oracle):
 @pytest.mark.parametrize("storage", STORAGES)
 @pytest.mark.parametrize("sampler", SAMPLERS)
 def test_c2_small_parity(ctx, c2_refs, storage, sampler):
-    if storage == "bf16" and sampler in ("texture", "hybrid"):
-        with pytest.raises(capi.VVLICError) as e:
-            render_gpu(ctx, c2_small(), sampler=sampler, storage=storage)
-        assert e.value.status == capi.ERR_UNSUPPORTED
-        return
     img, smp = render_gpu(ctx, c2_small(), sampler=sampler, storage=storage, samples=True)
     ref, ref_smp = c2_refs[storage]
     e = rmse(img, ref)
@@ -236,6 +231,30 @@ def small(integrator=capi.HEUN, **kw):
     for k, v in kw.items():
         setattr(w.params, k, v)
     return w
+
+
+def axis_aligned_field(shape, seed):
+    """Vectors along +-x, +-y or +-z with lengths k/4 (k = 1..4): every encoded texel component
+    (0, 1/2, 1 and k/4) is exact in FP16 and BF16 alike."""
+    rng = np.random.default_rng(seed)
+    axis = rng.integers(0, 3, shape)
+    val = (rng.choice([-1.0, 1.0], shape) * rng.integers(1, 5, shape) / 4.0).astype(np.float32)
+    f = np.zeros(tuple(shape) + (3,), np.float32)
+    np.put_along_axis(f, axis[..., None], val[..., None], axis=3)
+    f[0, 0, 0] = (1.0, 0.0, 0.0)
+    return f
+
+
+@pytest.mark.parametrize("sampler", ["texture", "hybrid"])
+def test_bf16_texture_holds_the_bf16_texels(ctx, sampler):
+    # the texture of a BF16 volume is a half4 copy of its BF16 texels: where both formats hold
+    # the texels exactly, BF16 and FP16 storage give the same image bit for bit
+    w = small()
+    w.field = axis_aligned_field(w.field.shape[:3], seed=17)
+    a, _ = render_gpu(ctx, w, sampler=sampler, storage="f16")
+    b, _ = render_gpu(ctx, w, sampler=sampler, storage="bf16")
+    np.testing.assert_array_equal(a, b)
+    assert float(a[..., 3].max()) > 0.05
 
 
 def check_small(ctx, oracle, w, sampler="cell", view=None, tol=RMSE_TOL):

@@ -367,7 +367,7 @@ static cudaError_t launch_adjoint_storage(const RenderArgs& a, int sampler, int 
     case VVLIC_SAMPLER_GATHER: return launch_adjoint_layout<ST, kGather, kGather>(a, integ, lit, g_img, acc, sch, s);
     case VVLIC_SAMPLER_CELL: return launch_adjoint_layout<ST, kCell, kCell>(a, integ, lit, g_img, acc, sch, s);
     case VVLIC_SAMPLER_TEXTURE:
-      if constexpr (ST == VVLIC_STORAGE_BF16) return cudaErrorNotSupported;
+      if constexpr (ST == VVLIC_STORAGE_BF16) return cudaErrorNotSupported;  // runs as F16 (kernel_storage)
       else return launch_adjoint_layout<ST, kTexture, kTexture>(a, integ, lit, g_img, acc, sch, s);
     case VVLIC_SAMPLER_HYBRID:
       if constexpr (ST == VVLIC_STORAGE_BF16) return cudaErrorNotSupported;

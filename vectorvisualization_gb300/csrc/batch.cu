@@ -116,7 +116,7 @@ void drop_graph(vvlic_ctx* c) {
 }
 
 cudaError_t launch_batch(int storage, const BatchLaunch& b, int sampler, int integ, bool grad, cudaStream_t s) {
-  switch (storage) {
+  switch (kernel_storage(storage, sampler)) {
     case VVLIC_STORAGE_F32: return launch_batch_f32(b, sampler, integ, grad, s);
     case VVLIC_STORAGE_F16: return launch_batch_f16(b, sampler, integ, grad, s);
     case VVLIC_STORAGE_UNORM8: return launch_batch_u8(b, sampler, integ, grad, s);
@@ -192,8 +192,6 @@ vvlic_status prepare_batch(vvlic_ctx* c, const vvlic_job* jobs, int n, int tw, i
   *sampler = sampler_override >= 0 ? sampler_override : jobs[0].params.sampler;
   *integ = jobs[0].params.integrator;
   *grad = jobs[0].params.illum == VVLIC_ILLUM_GRADIENT;
-  if (*storage == VVLIC_STORAGE_BF16 && (*sampler == VVLIC_SAMPLER_TEXTURE || *sampler == VVLIC_SAMPLER_HYBRID))
-    return fail(c, VVLIC_ERR_UNSUPPORTED, "batch: the texture samplers have no BF16 format");
   return VVLIC_OK;
 }
 
@@ -284,7 +282,6 @@ extern "C" vvlic_status vvlic_batch_autotune(vvlic_ctx* c, const vvlic_job* jobs
   auto it = c->vols.find(jobs[0].vol_id);
   if (it == c->vols.end()) return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "batch_autotune: unknown volume");
   std::vector<int> samplers = {VVLIC_SAMPLER_HYBRID, VVLIC_SAMPLER_CELL};
-  if (it->second.storage == VVLIC_STORAGE_BF16) samplers = {VVLIC_SAMPLER_CELL};
   const int tws[4] = {8, 4, 16, 32};
   float best = 1e30f;
   int bt = c->batch_tile_w, bs = jobs[0].params.sampler;

@@ -90,7 +90,7 @@ static cudaError_t launch_batch_storage(const BatchLaunch& b, int sampler, int i
     case VVLIC_SAMPLER_GATHER: return launch_batch_layout<ST, kGather, kGather>(b, integ, grad, s);
     case VVLIC_SAMPLER_CELL: return launch_batch_layout<ST, kCell, kCell>(b, integ, grad, s);
     case VVLIC_SAMPLER_TEXTURE:
-      if constexpr (ST == VVLIC_STORAGE_BF16) return cudaErrorNotSupported;
+      if constexpr (ST == VVLIC_STORAGE_BF16) return cudaErrorNotSupported;  // runs as F16 (kernel_storage)
       else return launch_batch_layout<ST, kTexture, kTexture>(b, integ, grad, s);
     case VVLIC_SAMPLER_HYBRID:
       if constexpr (ST == VVLIC_STORAGE_BF16) return cudaErrorNotSupported;

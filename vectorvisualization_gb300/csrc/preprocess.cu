@@ -243,6 +243,17 @@ inline int grid_for(size_t count) {
   return (int)(b < 152 * 64 ? (b == 0 ? 1 : b) : 152 * 64);
 }
 
+// One RGBA texel per iteration: four bf16 values (8 bytes) -> four halves (8 bytes), the
+// component order kept (x in the low half of the first word).
+__global__ void bf16_to_half_kernel(const uint2* in, size_t count, uint2* out) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x) {
+    const uint2 r = in[i];
+    __half2 lo = __floats2half2_rn(__uint_as_float(r.x << 16), __uint_as_float(r.x & 0xffff0000u));
+    __half2 hi = __floats2half2_rn(__uint_as_float(r.y << 16), __uint_as_float(r.y & 0xffff0000u));
+    out[i] = make_uint2(*reinterpret_cast<uint32_t*>(&lo), *reinterpret_cast<uint32_t*>(&hi));
+  }
+}
+
 }  // namespace
 
 namespace {
@@ -311,6 +322,12 @@ cudaError_t launch_build_field_cells(const void* d_texels, const int n[3], int s
     field_cells_kernel<VVLIC_STORAGE_UNORM8><<<grid_for(count), kThreads, 0, s>>>(d_texels, n[0], n[1], n[2], d_cells);
   else
     field_cells_kernel<VVLIC_STORAGE_BF16><<<grid_for(count), kThreads, 0, s>>>(d_texels, n[0], n[1], n[2], d_cells);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bf16_to_half(const void* d_bf16, size_t count, void* d_half, cudaStream_t s) {
+  bf16_to_half_kernel<<<grid_for(count), kThreads, 0, s>>>(reinterpret_cast<const uint2*>(d_bf16), count,
+                                                          reinterpret_cast<uint2*>(d_half));
   return cudaGetLastError();
 }
 

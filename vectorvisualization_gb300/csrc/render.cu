@@ -41,22 +41,40 @@ vvlic_status ensure_noise_cells(vvlic_ctx* c, NoiseTex& n, cudaStream_t s) {
 
 vvlic_status ensure_texture(vvlic_ctx* c, Volume& v, cudaStream_t s) {
   if (v.tex) return VVLIC_OK;
-  if (v.storage == VVLIC_STORAGE_BF16) return fail(c, VVLIC_ERR_UNSUPPORTED, "TEXTURE sampler has no BF16 format");
-  cudaChannelFormatDesc desc = v.storage == VVLIC_STORAGE_F32   ? cudaCreateChannelDesc<float4>()
-                               : v.storage == VVLIC_STORAGE_F16 ? cudaCreateChannelDescHalf4()
-                                                                : cudaCreateChannelDesc<uchar4>();
+  // The texture unit has no bf16 format: a BF16 volume's texture is a half4 array holding its
+  // BF16 texels converted to half (exact for the encoded texels, all in [0, 1], down to 2^-14).
+  const bool bf16 = v.storage == VVLIC_STORAGE_BF16;
+  cudaChannelFormatDesc desc = v.storage == VVLIC_STORAGE_F32 ? cudaCreateChannelDesc<float4>()
+                               : (v.storage == VVLIC_STORAGE_F16 || bf16) ? cudaCreateChannelDescHalf4()
+                                                                          : cudaCreateChannelDesc<uchar4>();
   cudaExtent ext = make_cudaExtent(v.n[0], v.n[1], v.n[2]);
   cudaError_t e = cudaMalloc3DArray(&v.array, &desc, ext);
   if (e != cudaSuccess) return cuda_fail(c, e, "texture array allocation");
-  const size_t tb = texel_bytes(v.storage);
-  v.array_bytes = (size_t)v.n[0] * v.n[1] * v.n[2] * tb;
+  const size_t tb = texel_bytes(v.storage);  // 8 bytes for F16, BF16 and their half4 copy alike
+  const size_t count = (size_t)v.n[0] * v.n[1] * v.n[2];
+  v.array_bytes = count * tb;
+  void* src = v.d_texels;
+  if (bf16) {
+    // stream-ordered scratch: freed behind the array copy that reads it
+    e = cudaMallocAsync(&src, count * tb, s);
+    if (e != cudaSuccess) return cuda_fail(c, e, "BF16 texture staging allocation");
+    e = launch_bf16_to_half(v.d_texels, count, src, s);
+    if (e != cudaSuccess) {
+      cudaFreeAsync(src, s);
+      return cuda_fail(c, e, "BF16 texture conversion");
+    }
+  }
   cudaMemcpy3DParms cp;
   std::memset(&cp, 0, sizeof cp);
-  cp.srcPtr = make_cudaPitchedPtr(v.d_texels, v.n[0] * tb, v.n[0], v.n[1]);
+  cp.srcPtr = make_cudaPitchedPtr(src, v.n[0] * tb, v.n[0], v.n[1]);
   cp.dstArray = v.array;
   cp.extent = ext;
   cp.kind = cudaMemcpyDeviceToDevice;
   e = cudaMemcpy3DAsync(&cp, s);
+  if (bf16) {
+    cudaError_t ef = cudaFreeAsync(src, s);
+    if (e == cudaSuccess) e = ef;
+  }
   if (e != cudaSuccess) return cuda_fail(c, e, "texture array copy");
   cudaResourceDesc rd;
   std::memset(&rd, 0, sizeof rd);
@@ -221,7 +239,7 @@ vvlic_status build_render_args_ex(vvlic_ctx* c, Volume& v, int W, int H, cudaStr
 
 cudaError_t launch_technique(int storage, const RenderArgs& a, const TechArgs& t, int sampler, int integ, bool grad,
                              cudaStream_t s) {
-  switch (storage) {
+  switch (kernel_storage(storage, sampler)) {
     case VVLIC_STORAGE_F32: return launch_technique_f32(a, t, sampler, integ, grad, s);
     case VVLIC_STORAGE_F16: return launch_technique_f16(a, t, sampler, integ, grad, s);
     case VVLIC_STORAGE_UNORM8: return launch_technique_u8(a, t, sampler, integ, grad, s);
@@ -231,7 +249,7 @@ cudaError_t launch_technique(int storage, const RenderArgs& a, const TechArgs& t
 
 cudaError_t launch_raycast(const RenderArgs& a, int storage, int sampler, int integ, bool grad, const Schedule& sch,
                            cudaStream_t s) {
-  switch (storage) {
+  switch (kernel_storage(storage, sampler)) {
     case VVLIC_STORAGE_F32: return launch_raycast_f32(a, sampler, integ, grad, sch, s);
     case VVLIC_STORAGE_F16: return launch_raycast_f16(a, sampler, integ, grad, sch, s);
     case VVLIC_STORAGE_UNORM8: return launch_raycast_u8(a, sampler, integ, grad, sch, s);
@@ -511,7 +529,7 @@ extern "C" vvlic_status vvlic_render_adjoint(vvlic_ctx* c, int32_t vol_id, const
   const float4* gi = (const float4*)d_dl_drgba;
   if (e == cudaSuccess) {
     const bool lit = c->tape_illum == VVLIC_ILLUM_GRADIENT;
-    switch (c->tape_storage) {
+    switch (kernel_storage(c->tape_storage, c->tape_sampler)) {
       case VVLIC_STORAGE_F32: e = launch_adjoint_f32(a, c->tape_sampler, c->tape_integ, lit, gi, c->d_acc, sch, s); break;
       case VVLIC_STORAGE_F16: e = launch_adjoint_f16(a, c->tape_sampler, c->tape_integ, lit, gi, c->d_acc, sch, s); break;
       case VVLIC_STORAGE_UNORM8:

@@ -127,7 +127,7 @@ static cudaError_t launch_storage(const RenderArgs& a, int sampler, int integ, b
     case VVLIC_SAMPLER_GATHER: return launch_layout<ST, kGather, kGather>(a, integ, grad, sch, s);
     case VVLIC_SAMPLER_CELL: return launch_layout<ST, kCell, kCell>(a, integ, grad, sch, s);
     case VVLIC_SAMPLER_TEXTURE:
-      if constexpr (ST == VVLIC_STORAGE_BF16) return cudaErrorNotSupported;  // no bf16 texture format
+      if constexpr (ST == VVLIC_STORAGE_BF16) return cudaErrorNotSupported;  // runs as F16 (kernel_storage)
       else return launch_layout<ST, kTexture, kTexture>(a, integ, grad, sch, s);
     case VVLIC_SAMPLER_HYBRID:
       if constexpr (ST == VVLIC_STORAGE_BF16) return cudaErrorNotSupported;

@@ -168,7 +168,7 @@ static cudaError_t launch_tech_storage(const RenderArgs& a, const TechArgs& t, i
     case VVLIC_SAMPLER_GATHER: return launch_tech_layout<ST, kGather, kGather>(a, t, integ, grad, s);
     case VVLIC_SAMPLER_CELL: return launch_tech_layout<ST, kCell, kCell>(a, t, integ, grad, s);
     case VVLIC_SAMPLER_TEXTURE:
-      if constexpr (ST == VVLIC_STORAGE_BF16) return cudaErrorNotSupported;
+      if constexpr (ST == VVLIC_STORAGE_BF16) return cudaErrorNotSupported;  // runs as F16 (kernel_storage)
       else return launch_tech_layout<ST, kTexture, kTexture>(a, t, integ, grad, s);
     case VVLIC_SAMPLER_HYBRID:
       if constexpr (ST == VVLIC_STORAGE_BF16) return cudaErrorNotSupported;

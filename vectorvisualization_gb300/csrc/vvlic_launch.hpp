@@ -6,6 +6,8 @@
 
 #include <algorithm>
 
+#include "../../include/vvlic.h"
+
 namespace vvlic {
 
 struct RenderArgs;
@@ -118,7 +120,21 @@ cudaError_t launch_build_field_cells(const void* d_texels, const int n[3], int s
 cudaError_t launch_build_noise_cells(const uint8_t* d_texels, const int m[3], int ch, uint8_t* d_cells,
                                      cudaStream_t s);
 
+// BF16 texels (count RGBA quadruples) -> half-precision RGBA, the format of a BF16 volume's
+// texture copy.  Exact for every texel value in [2^-14, 65504]; smaller magnitudes round to the
+// nearest half subnormal (absolute error <= 2^-25).
+cudaError_t launch_bf16_to_half(const void* d_bf16, size_t count, void* d_half, cudaStream_t s);
+
 // Bytes per texel of a field storage.
 inline int texel_bytes(int storage) { return storage == 0 ? 16 : (storage == 3 ? 4 : 8); }
+
+// Storage whose kernel instantiation a launch uses.  Texture-sampled kernels see the field only
+// through the texture, whose format is float4 (F32), half4 (F16) or uchar4 (UNORM8); the texture
+// of a BF16 volume holds half-precision copies of its BF16 texels, so its TEXTURE and HYBRID
+// launches run the F16 instantiations.
+inline int kernel_storage(int storage, int sampler) {
+  const bool tex = sampler == VVLIC_SAMPLER_TEXTURE || sampler == VVLIC_SAMPLER_HYBRID;
+  return (storage == VVLIC_STORAGE_BF16 && tex) ? VVLIC_STORAGE_F16 : storage;
+}
 
 }  // namespace vvlic
