@@ -371,7 +371,7 @@ static cudaError_t launch_adjoint_storage(const RenderArgs& a, int sampler, int 
       else return launch_adjoint_layout<ST, kTexture, kTexture>(a, integ, lit, g_img, acc, sch, s);
     case VVLIC_SAMPLER_HYBRID:
       if constexpr (ST == VVLIC_STORAGE_BF16) return cudaErrorNotSupported;
-      else return launch_adjoint_layout<ST, kTexture, kCell>(a, integ, lit, g_img, acc, sch, s);
+      else return launch_adjoint_layout<ST, kTexture, kCellFast>(a, integ, lit, g_img, acc, sch, s);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -94,7 +94,7 @@ static cudaError_t launch_batch_storage(const BatchLaunch& b, int sampler, int i
       else return launch_batch_layout<ST, kTexture, kTexture>(b, integ, grad, s);
     case VVLIC_SAMPLER_HYBRID:
       if constexpr (ST == VVLIC_STORAGE_BF16) return cudaErrorNotSupported;
-      else return launch_batch_layout<ST, kTexture, kCell>(b, integ, grad, s);
+      else return launch_batch_layout<ST, kTexture, kCellFast>(b, integ, grad, s);
     default: return cudaErrorInvalidValue;
   }
 }

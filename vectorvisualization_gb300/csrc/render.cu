@@ -205,6 +205,11 @@ vvlic_status build_render_args_ex(vvlic_ctx* c, Volume& v, int W, int H, cudaStr
   const float h = p.low_res ? 1.0f / 64.0f : p.step_size_lic;
   a.step_size = p.low_res ? 2.0f * p.step_size_vol : p.step_size_vol;
   a.freq_scale = p.low_res ? 0.7f * p.freq_scale : p.freq_scale;
+  const bool nofreq = (p.quirks & VVLIC_QUIRK_GRAD_NOISE_NO_FREQ) != 0;
+  for (int i = 0; i < 3; ++i) {
+    a.nscale[i] = (float)((double)a.freq_scale * a.m[i]);
+    a.nscale_grad[i] = nofreq ? (float)a.m[i] : a.nscale[i];
+  }
   a.alpha_corr = p.low_res ? 2.0f * p.step_size_vol * 128.0f : p.step_size_vol * 128.0f;
   a.h_eff = h * p.eye_dist_factor;
   a.intensity_scale = inv_area / (float)(lf + lb) * p.gradient_scale;  // licKernel.b * gradient.r

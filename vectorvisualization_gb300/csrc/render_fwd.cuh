@@ -23,6 +23,16 @@ constexpr int kThreads = 128;
 #ifndef VVLIC_MIN_BLOCKS
 #define VVLIC_MIN_BLOCKS 7
 #endif
+// The same for the RK4 kernels, which hold four slopes per step: at 73 registers the lit RK4
+// kernel spills 40 B; at 6 CTAs (80 registers, 8 B) the 512^3 RK4 frame ran 1.5 % faster
+// (110.5 vs 108.9 Gsample-steps/s, two alternations).  8 CTAs (64 registers) for every kernel
+// measured the same as 7 on the lit 1024^2 frame.
+#ifndef VVLIC_RK4_MIN_BLOCKS
+#define VVLIC_RK4_MIN_BLOCKS 6
+#endif
+template <int INTEG> constexpr int min_blocks() {
+  return INTEG == VVLIC_RK4 ? VVLIC_RK4_MIN_BLOCKS : VVLIC_MIN_BLOCKS;
+}
 
 __device__ __forceinline__ void load_tf(const RenderArgs& a, float* s_tf) {
   for (int i = threadIdx.x; i < 5 * VVLIC_TF_ENTRIES; i += blockDim.x) s_tf[i] = __ldg(a.tf + i);
@@ -50,7 +60,7 @@ __device__ __forceinline__ void flush_counters(const RenderArgs& a, uint32_t sam
 }
 
 template <int ST, int FL, int NL, int INTEG, bool GRAD>
-__global__ void __launch_bounds__(kThreads, VVLIC_MIN_BLOCKS) raycast_kernel(const __grid_constant__ RenderArgs a) {
+__global__ void __launch_bounds__(kThreads, min_blocks<INTEG>()) raycast_kernel(const __grid_constant__ RenderArgs a) {
   __shared__ __align__(16) float s_tf[5 * VVLIC_TF_ENTRIES];
   load_tf(a, s_tf);
   const int px = blockIdx.x * kTileW + (threadIdx.x % kTileW);
@@ -64,7 +74,7 @@ __global__ void __launch_bounds__(kThreads, VVLIC_MIN_BLOCKS) raycast_kernel(con
 }
 
 template <int ST, int FL, int NL, int INTEG, bool GRAD>
-__global__ void __launch_bounds__(kThreads, VVLIC_MIN_BLOCKS) raycast_queue_kernel(const __grid_constant__ RenderArgs a,
+__global__ void __launch_bounds__(kThreads, min_blocks<INTEG>()) raycast_queue_kernel(const __grid_constant__ RenderArgs a,
                                                                  const uint32_t* __restrict__ order, int ntiles,
                                                                  unsigned* __restrict__ next) {
   __shared__ __align__(16) float s_tf[5 * VVLIC_TF_ENTRIES];
@@ -131,7 +141,7 @@ static cudaError_t launch_storage(const RenderArgs& a, int sampler, int integ, b
       else return launch_layout<ST, kTexture, kTexture>(a, integ, grad, sch, s);
     case VVLIC_SAMPLER_HYBRID:
       if constexpr (ST == VVLIC_STORAGE_BF16) return cudaErrorNotSupported;
-      else return launch_layout<ST, kTexture, kCell>(a, integ, grad, sch, s);
+      else return launch_layout<ST, kTexture, kCellFast>(a, integ, grad, sch, s);
     default: return cudaErrorInvalidValue;
   }
 }

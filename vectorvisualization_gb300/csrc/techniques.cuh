@@ -172,7 +172,7 @@ static cudaError_t launch_tech_storage(const RenderArgs& a, const TechArgs& t, i
       else return launch_tech_layout<ST, kTexture, kTexture>(a, t, integ, grad, s);
     case VVLIC_SAMPLER_HYBRID:
       if constexpr (ST == VVLIC_STORAGE_BF16) return cudaErrorNotSupported;
-      else return launch_tech_layout<ST, kTexture, kCell>(a, t, integ, grad, s);
+      else return launch_tech_layout<ST, kTexture, kCellFast>(a, t, integ, grad, s);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -15,8 +15,9 @@ namespace vvlic {
 
 constexpr int kMaxTaps = 2 * VVLIC_MAX_STEPS + 1;
 
-// Memory layouts a sampler reads (field and noise separately).
-enum Layout : int { kGather = 0, kCell = 1, kTexture = 2 };
+// Memory layouts a sampler reads (field and noise separately).  kCellFast is the kCell noise
+// layout filtered with biased bytes (see NoiseCells), the HYBRID sampler's noise.
+enum Layout : int { kGather = 0, kCell = 1, kTexture = 2, kCellFast = 3 };
 
 // Kernel arguments of one render job, passed by value as a __grid_constant__ parameter (in
 // the constant bank; the taps are read warp-uniformly so they broadcast).
@@ -39,6 +40,10 @@ struct RenderArgs {
   int clamp0;
   float ext[3], tex_max[3], scale_vol[3], scale_vol_inv[3];
   float step_size, h_eff, intensity_scale, alpha_corr, illum_scale, freq_scale, alpha_thr;
+  // noise texel-space scale of a streamline position per axis, m * frequency, for value taps
+  // (freq_scale) and gradient taps (1 under VVLIC_QUIRK_GRAD_NOISE_NO_FREQ): the cell samplers
+  // form u = p * scale - 1/2 with one FMA
+  float nscale[3], nscale_grad[3];
   float gate_lo, gate_hi;
   int num_iter, lb, lf, illum, tf_index, sof, gate, quirks;
   float light_pos[3], spec_exp, light_diff[3], light_spec[3], light_amb[3];
@@ -104,6 +109,12 @@ __device__ __forceinline__ float4 trilerp(float4 t000, float4 t100, float4 t010,
 // 0x4B0000bb (= 2^23 + b) with one byte permute and subtract 2^23.
 __device__ __forceinline__ float byte_as_float(uint32_t w, int k) {
   return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u + (unsigned)k)) - 8388608.0f;
+}
+
+// Byte k of w as the float 32768 + b: one byte permute assembles 0x4700bb00 (exponent 2^15,
+// the byte in mantissa bits 8..15, so b is exact and 8 mantissa bits lie below it).
+__device__ __forceinline__ float byte_biased(uint32_t w, int k) {
+  return __uint_as_float(__byte_perm(w, 0x47000000u, 0x7404u + ((unsigned)k << 4)));
 }
 
 __device__ __forceinline__ float4 unorm8x4(uint32_t r) {
@@ -272,8 +283,16 @@ __device__ __forceinline__ float bytef(uint32_t w, int k) { return (float)((w >>
 
 template <int NL> struct Noise;
 
+// Texture coordinate of a noise tap at position p: p * frequency (value taps, and gradient taps
+// without VVLIC_QUIRK_GRAD_NOISE_NO_FREQ), else p.
+template <bool GRADC> __device__ __forceinline__ float3 noise_coord(const RenderArgs& a, float3 p) {
+  if (GRADC && (a.quirks & VVLIC_QUIRK_GRAD_NOISE_NO_FREQ)) return p;
+  return scl3(p, a.freq_scale);
+}
+
 template <> struct Noise<kGather> {
-  template <bool RGBA> static __device__ __forceinline__ float4 sample(const RenderArgs& a, float3 s) {
+  template <bool RGBA, bool GRADC> static __device__ __forceinline__ float4 sample(const RenderArgs& a, float3 p) {
+    const float3 s = noise_coord<GRADC>(a, p);
     int x0, x1, y0, y1, z0, z1;
     float ax, ay, az;
     repeat_axis(s.x, a.m[0], x0, x1, ax);
@@ -311,9 +330,10 @@ template <> struct Noise<kGather> {
   }
 };
 
-// REPEAT wrap: power-of-two extents use a mask, others the integer remainder.
-__device__ __forceinline__ void repeat_axis_fast(float s, int m, int& i0, int& i1, float& a) {
-  float u = fmaf(s, (float)m, -0.5f);
+// REPEAT wrap of the position p along an axis of m texels, pm = m * (texture coordinate per
+// unit of p): power-of-two extents use a mask, others the integer remainder.
+__device__ __forceinline__ void repeat_axis_fast(float p, float pm, int m, int& i0, int& i1, float& a) {
+  float u = fmaf(p, pm, -0.5f);
   u = fminf(fmaxf(u, -16777216.0f), 16777216.0f);
   float fl = floorf(u);
   a = u - fl;
@@ -328,17 +348,31 @@ __device__ __forceinline__ void repeat_axis_fast(float s, int m, int& i0, int& i
     i1 = (b + 1 == m) ? 0 : b + 1;
   }
 }
+__device__ __forceinline__ void repeat_axis_fast(float s, int m, int& i0, int& i1, float& a) {
+  repeat_axis_fast(s, (float)m, m, i0, i1, a);
+}
 
 // Noise cells (REPEAT): cell (x0,y0,z0) holds the 8 corners; RGBA: 32 bytes, value-only: 8 bytes.
 // The eight trilinear weights are formed once and applied to every channel.
-template <> struct Noise<kCell> {
-  template <bool RGBA> static __device__ __forceinline__ float4 sample(const RenderArgs& a, float3 s) {
+//   EXACT (kCell): each byte becomes an exact float (byte_as_float) before the weighted sum,
+//     the trilinear to float rounding.
+//   !EXACT (kCellFast): each byte enters the weighted sum as 32768 + b (byte_biased) and the
+//     bias comes off once per channel, because the weights sum to 1.  That saves one add per
+//     corner and channel.  The accumulator then carries 8 bits below a noise step: the filtered
+//     value is within 0.011 of a step (RMS 0.002, no bias) of the exact trilinear.  The texture
+//     unit's 8-bit filter weights allow up to about 1.5 steps.
+template <bool EXACT> struct NoiseCells {
+  static __device__ __forceinline__ float corner(uint32_t w, int k) {
+    return EXACT ? byte_as_float(w, k) : byte_biased(w, k);
+  }
+  template <bool RGBA, bool GRADC> static __device__ __forceinline__ float4 sample(const RenderArgs& a, float3 p) {
     int x0, x1, y0, y1, z0, z1;
     float ax, ay, az;
-    repeat_axis_fast(s.x, a.m[0], x0, x1, ax);
-    repeat_axis_fast(s.y, a.m[1], y0, y1, ay);
-    repeat_axis_fast(s.z, a.m[2], z0, z1, az);
+    repeat_axis_fast(p.x, GRADC ? a.nscale_grad[0] : a.nscale[0], a.m[0], x0, x1, ax);
+    repeat_axis_fast(p.y, GRADC ? a.nscale_grad[1] : a.nscale[1], a.m[1], y0, y1, ay);
+    repeat_axis_fast(p.z, GRADC ? a.nscale_grad[2] : a.nscale[2], a.m[2], z0, z1, az);
     const float k = 1.0f / 255.0f;
+    const float bias = EXACT ? 0.0f : 32768.0f;
     const float bx = 1.0f - ax, by = 1.0f - ay, bz = 1.0f - az;
     const float w00 = by * bz, w10 = ay * bz, w01 = by * az, w11 = ay * az;
     const float w[8] = {bx * w00, ax * w00, bx * w10, ax * w10, bx * w01, ax * w01, bx * w11, ax * w11};
@@ -351,36 +385,40 @@ template <> struct Noise<kCell> {
       float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
       for (int i = 0; i < 8; ++i) {
-        r.x = fmaf(w[i], byte_as_float(t[i], 0), r.x);
-        r.y = fmaf(w[i], byte_as_float(t[i], 1), r.y);
-        r.z = fmaf(w[i], byte_as_float(t[i], 2), r.z);
-        r.w = fmaf(w[i], byte_as_float(t[i], 3), r.w);
+        r.x = fmaf(w[i], corner(t[i], 0), r.x);
+        r.y = fmaf(w[i], corner(t[i], 1), r.y);
+        r.z = fmaf(w[i], corner(t[i], 2), r.z);
+        r.w = fmaf(w[i], corner(t[i], 3), r.w);
       }
-      return make_float4(r.x * k, r.y * k, r.z * k, r.w * k);
+      return make_float4((r.x - bias) * k, (r.y - bias) * k, (r.z - bias) * k, (r.w - bias) * k);
     }
     const uint2 q = __ldg(reinterpret_cast<const uint2*>(a.noise) + cidx);
     float v = 0.0f;
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-      v = fmaf(w[i], byte_as_float(q.x, i), v);
-      v = fmaf(w[4 + i], byte_as_float(q.y, i), v);
+      v = fmaf(w[i], corner(q.x, i), v);
+      v = fmaf(w[4 + i], corner(q.y, i), v);
     }
-    return make_float4(0.f, 0.f, 0.f, v * k);
+    return make_float4(0.f, 0.f, 0.f, (v - bias) * k);
   }
 };
+template <> struct Noise<kCell> : NoiseCells<true> {};
+template <> struct Noise<kCellFast> : NoiseCells<false> {};
 
 // Noise through the texture unit: RGBA8 / R8 read as normalised float (x/255), LINEAR filter,
 // WRAP addressing on normalised coordinates — GL's REPEAT.
 template <> struct Noise<kTexture> {
-  template <bool RGBA> static __device__ __forceinline__ float4 sample(const RenderArgs& a, float3 s) {
+  template <bool RGBA, bool GRADC> static __device__ __forceinline__ float4 sample(const RenderArgs& a, float3 p) {
+    const float3 s = noise_coord<GRADC>(a, p);
     if (RGBA) return tex3D<float4>(a.noise_tex, s.x, s.y, s.z);
     return make_float4(0.f, 0.f, 0.f, tex3D<float>(a.noise_tex, s.x, s.y, s.z));
   }
 };
 
 // Value of the noise (.a): from an RGBA (-g) noise or a one-channel one.
-template <int NL> __device__ __forceinline__ float noise_value(const RenderArgs& a, float3 s) {
-  return a.noise_ch == 4 ? Noise<NL>::template sample<true>(a, s).w : Noise<NL>::template sample<false>(a, s).w;
+template <int NL> __device__ __forceinline__ float noise_value(const RenderArgs& a, float3 p) {
+  return a.noise_ch == 4 ? Noise<NL>::template sample<true, false>(a, p).w
+                         : Noise<NL>::template sample<false, false>(a, p).w;
 }
 
 __device__ __forceinline__ float sample_scalar(const RenderArgs& a, float3 s) {
@@ -430,18 +468,25 @@ __device__ __forceinline__ float4 tf_rgba(const float* tab, float s) {
 // LIC: computeLIC / singleLICstep (inc_lic.glsl:157-265)
 // ------------------------------------------------------------------------------------------
 __device__ __forceinline__ float3 slope(float4 f) { return f3(2.0f * f.x - 1.0f, 2.0f * f.y - 1.0f, 2.0f * f.z - 1.0f); }
+// h * slope(f) rounded once: (2f - 1) * h = f * 2h - h, one FMA per component.  It keeps 2h
+// and h live; RK4, which holds four slopes, keeps the two-step form to stay within the
+// register cap.
+__device__ __forceinline__ float3 slope_h(float4 f, float h) {
+  const float h2 = 2.0f * h;
+  return f3(fmaf(f.x, h2, -h), fmaf(f.y, h2, -h), fmaf(f.z, h2, -h));
+}
 
 // One streamline step; replaces `step` with the field value at the new position (the
 // first-same-as-last reuse of the reference's `step` in/out argument).
 template <int ST, int FL, int INTEG>
 __device__ __forceinline__ float3 lic_step(const RenderArgs& a, float3 p, float4& step, float dirs) {
   using F = Field<ST, FL>;
-  const float hs = a.h_eff * dirs * (a.sof ? step.w : 1.0f);
-  float3 k1 = scl3(slope(step), hs);
+  const float hs = a.sof ? a.h_eff * dirs * step.w : a.h_eff * dirs;
+  float3 k1 = INTEG == VVLIC_RK4 ? scl3(slope(step), hs) : slope_h(step, hs);
   if (INTEG == VVLIC_EULER) {
     p = add3(p, k1);
   } else if (INTEG == VVLIC_HEUN) {
-    float3 k2 = scl3(slope(F::sample(a, add3(p, k1))), hs);
+    float3 k2 = slope_h(F::sample(a, add3(p, k1)), hs);
     p = add3(p, scl3(add3(k1, k2), 0.5f));
   } else {
     float3 k2 = scl3(slope(F::sample(a, add3(p, scl3(k1, 0.5f)))), hs);
@@ -455,16 +500,13 @@ __device__ __forceinline__ float3 lic_step(const RenderArgs& a, float3 p, float4
 
 // freqSampling / freqSamplingGrad (inc_lic.glsl:124-153)
 template <int NL, bool GRAD> __device__ __forceinline__ float4 noise_tap(const RenderArgs& a, float3 p) {
-  if (GRAD) {
-    const bool nofreq = (a.quirks & VVLIC_QUIRK_GRAD_NOISE_NO_FREQ) != 0;
-    return Noise<NL>::template sample<true>(a, nofreq ? p : scl3(p, a.freq_scale));
-  }
+  if (GRAD) return Noise<NL>::template sample<true, true>(a, p);
   if (a.gate) {
     float s = sample_scalar(a, p);
     if (!(s > a.gate_lo && s < a.gate_hi)) return make_float4(0.f, 0.f, 0.f, 0.f);
   }
   if (a.quirks & VVLIC_QUIRK_LUMINANCE_NOISE) return make_float4(0.f, 0.f, 0.f, 1.0f);
-  return make_float4(0.f, 0.f, 0.f, noise_value<NL>(a, scl3(p, a.freq_scale)));
+  return make_float4(0.f, 0.f, 0.f, noise_value<NL>(a, p));
 }
 
 template <bool GRAD> __device__ __forceinline__ void accumulate(float4& acc, float4 n, float w) {
