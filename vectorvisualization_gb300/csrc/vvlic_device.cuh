@@ -105,6 +105,14 @@ __device__ __forceinline__ float4 trilerp(float4 t000, float4 t100, float4 t010,
 // ------------------------------------------------------------------------------------------
 // texel decoding per storage precision
 // ------------------------------------------------------------------------------------------
+// One 32-byte read-only load: the 256-bit vector load of sm_100 and later, one L1 request for
+// a whole 32-byte cell instead of two 16-byte ones.  p must be 32-byte aligned.
+__device__ __forceinline__ void ldg256(const void* p, uint32_t (&r)[8]) {
+  asm("ld.global.nc.v8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+      : "l"(p));
+}
+
 // Byte k of w as an exact float without a conversion instruction: assemble the bit pattern
 // 0x4B0000bb (= 2^23 + b) with one byte permute and subtract 2^23.
 __device__ __forceinline__ float byte_as_float(uint32_t w, int k) {
@@ -229,32 +237,41 @@ __device__ __forceinline__ int cell_index(const RenderArgs& a, float3 s, float& 
   return c;
 }
 
-template <> struct Field<VVLIC_STORAGE_F32, kCell> {  // 128-byte cells, eight 16-byte loads
+__device__ __forceinline__ float4 f4(const uint32_t* r) {
+  return make_float4(__uint_as_float(r[0]), __uint_as_float(r[1]), __uint_as_float(r[2]), __uint_as_float(r[3]));
+}
+template <> struct Field<VVLIC_STORAGE_F32, kCell> {  // 128-byte cells, four 32-byte loads
   static __device__ __forceinline__ float4 sample(const RenderArgs& a, float3 s) {
     float ax, ay, az;
     const float4* c = reinterpret_cast<const float4*>(a.field) + 8 * (size_t)cell_index(a, s, ax, ay, az);
-    return trilerp(__ldg(c + 0), __ldg(c + 1), __ldg(c + 2), __ldg(c + 3), __ldg(c + 4), __ldg(c + 5), __ldg(c + 6),
-                   __ldg(c + 7), ax, ay, az);
+    uint32_t q0[8], q1[8], q2[8], q3[8];
+    ldg256(c + 0, q0);
+    ldg256(c + 2, q1);
+    ldg256(c + 4, q2);
+    ldg256(c + 6, q3);
+    return trilerp(f4(q0), f4(q0 + 4), f4(q1), f4(q1 + 4), f4(q2), f4(q2 + 4), f4(q3), f4(q3 + 4), ax, ay, az);
   }
 };
-template <int ST> struct Field<ST, kCell> {  // F16 / BF16: 64-byte cells, four 16-byte loads
+template <int ST> struct Field<ST, kCell> {  // F16 / BF16: 64-byte cells, two 32-byte loads
   static __device__ __forceinline__ float4 sample(const RenderArgs& a, float3 s) {
     float ax, ay, az;
     const uint4* c = reinterpret_cast<const uint4*>(a.field) + 4 * (size_t)cell_index(a, s, ax, ay, az);
-    uint4 q0 = __ldg(c + 0), q1 = __ldg(c + 1), q2 = __ldg(c + 2), q3 = __ldg(c + 3);
-    return trilerp(Texel<ST>::decode(make_uint2(q0.x, q0.y)), Texel<ST>::decode(make_uint2(q0.z, q0.w)),
-                   Texel<ST>::decode(make_uint2(q1.x, q1.y)), Texel<ST>::decode(make_uint2(q1.z, q1.w)),
-                   Texel<ST>::decode(make_uint2(q2.x, q2.y)), Texel<ST>::decode(make_uint2(q2.z, q2.w)),
-                   Texel<ST>::decode(make_uint2(q3.x, q3.y)), Texel<ST>::decode(make_uint2(q3.z, q3.w)), ax, ay, az);
+    uint32_t q0[8], q1[8];
+    ldg256(c + 0, q0);
+    ldg256(c + 2, q1);
+    return trilerp(Texel<ST>::decode(make_uint2(q0[0], q0[1])), Texel<ST>::decode(make_uint2(q0[2], q0[3])),
+                   Texel<ST>::decode(make_uint2(q0[4], q0[5])), Texel<ST>::decode(make_uint2(q0[6], q0[7])),
+                   Texel<ST>::decode(make_uint2(q1[0], q1[1])), Texel<ST>::decode(make_uint2(q1[2], q1[3])),
+                   Texel<ST>::decode(make_uint2(q1[4], q1[5])), Texel<ST>::decode(make_uint2(q1[6], q1[7])), ax, ay, az);
   }
 };
-template <> struct Field<VVLIC_STORAGE_UNORM8, kCell> {  // 32-byte cells, two 16-byte loads
+template <> struct Field<VVLIC_STORAGE_UNORM8, kCell> {  // 32-byte cells, one 32-byte load
   static __device__ __forceinline__ float4 sample(const RenderArgs& a, float3 s) {
     float ax, ay, az;
-    const uint4* c = reinterpret_cast<const uint4*>(a.field) + 2 * (size_t)cell_index(a, s, ax, ay, az);
-    uint4 q0 = __ldg(c + 0), q1 = __ldg(c + 1);
-    return trilerp(unorm8x4(q0.x), unorm8x4(q0.y), unorm8x4(q0.z), unorm8x4(q0.w), unorm8x4(q1.x), unorm8x4(q1.y),
-                   unorm8x4(q1.z), unorm8x4(q1.w), ax, ay, az);
+    uint32_t q[8];
+    ldg256(reinterpret_cast<const uint4*>(a.field) + 2 * (size_t)cell_index(a, s, ax, ay, az), q);
+    return trilerp(unorm8x4(q[0]), unorm8x4(q[1]), unorm8x4(q[2]), unorm8x4(q[3]), unorm8x4(q[4]), unorm8x4(q[5]),
+                   unorm8x4(q[6]), unorm8x4(q[7]), ax, ay, az);
   }
 };
 
@@ -379,9 +396,8 @@ template <bool EXACT> struct NoiseCells {
     int cidx = (z0 * a.m[1] + y0) * a.m[0] + x0;
     if (VVLIC_BOUNDS_CHECK && !in_range(a, cidx, (long long)a.m[0] * a.m[1] * a.m[2], VVLIC_CHECK_NOISE)) cidx = 0;
     if (RGBA) {
-      const uint4* c = reinterpret_cast<const uint4*>(a.noise) + 2 * (size_t)cidx;
-      const uint4 q0 = __ldg(c), q1 = __ldg(c + 1);
-      const uint32_t t[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
+      uint32_t t[8];
+      ldg256(reinterpret_cast<const uint4*>(a.noise) + 2 * (size_t)cidx, t);
       float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
       for (int i = 0; i < 8; ++i) {
