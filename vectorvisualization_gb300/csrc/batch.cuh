@@ -11,8 +11,19 @@ namespace vvlic {
 
 constexpr int kWarpsPerCta = kThreads / 32;
 
+// Register cap of the unlit Euler / Heun batch kernels, whose arguments come from shared memory
+// rather than the constant bank.  On the 64-volume unlit batch: 8 CTAs/SM (64 registers) 1253 ms,
+// 7 1283 ms, 6 1326 ms.  (The single-render unlit kernels measured best at 7: 27.5 ms against
+// 29.7 at 8 and 33.5 at 9 on the 128^3 4-view forward.)
+#ifndef VVLIC_BATCH_UNLIT_MIN_BLOCKS
+#define VVLIC_BATCH_UNLIT_MIN_BLOCKS 8
+#endif
+template <int INTEG, bool GRAD> constexpr int batch_min_blocks() {
+  return (!GRAD && INTEG != VVLIC_RK4) ? VVLIC_BATCH_UNLIT_MIN_BLOCKS : min_blocks<INTEG, GRAD>();
+}
+
 template <int ST, int FL, int NL, int INTEG, bool GRAD>
-__global__ void __launch_bounds__(kThreads, VVLIC_MIN_BLOCKS)
+__global__ void __launch_bounds__(kThreads, batch_min_blocks<INTEG, GRAD>())
     raycast_batch_kernel(const RenderArgs* __restrict__ jobs, const uint2* __restrict__ order, int nitems,
                          unsigned* __restrict__ next, const float* __restrict__ tf, unsigned long long* counters,
                          int tw) {

@@ -30,8 +30,12 @@ constexpr int kThreads = 128;
 #ifndef VVLIC_RK4_MIN_BLOCKS
 #define VVLIC_RK4_MIN_BLOCKS 6
 #endif
-template <int INTEG> constexpr int min_blocks() {
-  return INTEG == VVLIC_RK4 ? VVLIC_RK4_MIN_BLOCKS : VVLIC_MIN_BLOCKS;
+// Unlit (and line-lit) Euler / Heun kernels: no noise gradients to carry.
+#ifndef VVLIC_UNLIT_MIN_BLOCKS
+#define VVLIC_UNLIT_MIN_BLOCKS VVLIC_MIN_BLOCKS
+#endif
+template <int INTEG, bool GRAD> constexpr int min_blocks() {
+  return INTEG == VVLIC_RK4 ? VVLIC_RK4_MIN_BLOCKS : (GRAD ? VVLIC_MIN_BLOCKS : VVLIC_UNLIT_MIN_BLOCKS);
 }
 
 __device__ __forceinline__ void load_tf(const RenderArgs& a, float* s_tf) {
@@ -60,7 +64,7 @@ __device__ __forceinline__ void flush_counters(const RenderArgs& a, uint32_t sam
 }
 
 template <int ST, int FL, int NL, int INTEG, bool GRAD>
-__global__ void __launch_bounds__(kThreads, min_blocks<INTEG>()) raycast_kernel(const __grid_constant__ RenderArgs a) {
+__global__ void __launch_bounds__(kThreads, min_blocks<INTEG, GRAD>()) raycast_kernel(const __grid_constant__ RenderArgs a) {
   __shared__ __align__(16) float s_tf[5 * VVLIC_TF_ENTRIES];
   load_tf(a, s_tf);
   const int px = blockIdx.x * kTileW + (threadIdx.x % kTileW);
@@ -74,7 +78,7 @@ __global__ void __launch_bounds__(kThreads, min_blocks<INTEG>()) raycast_kernel(
 }
 
 template <int ST, int FL, int NL, int INTEG, bool GRAD>
-__global__ void __launch_bounds__(kThreads, min_blocks<INTEG>()) raycast_queue_kernel(const __grid_constant__ RenderArgs a,
+__global__ void __launch_bounds__(kThreads, min_blocks<INTEG, GRAD>()) raycast_queue_kernel(const __grid_constant__ RenderArgs a,
                                                                  const uint32_t* __restrict__ order, int ntiles,
                                                                  unsigned* __restrict__ next) {
   __shared__ __align__(16) float s_tf[5 * VVLIC_TF_ENTRIES];

@@ -437,7 +437,10 @@ template <int NL> __device__ __forceinline__ float noise_value(const RenderArgs&
                          : Noise<NL>::template sample<false, false>(a, p).w;
 }
 
-__device__ __forceinline__ float sample_scalar(const RenderArgs& a, float3 s) {
+// Scalar-gate volume (freqSampling's scalarSampler), trilinear + CLAMP_TO_EDGE.  Not inlined:
+// the gate is off unless a scalar volume is set, and keeping its gathers out of the tap loop's
+// register allocation measured 2.4 % faster on the 64-volume unlit batch (1253 vs 1283 ms).
+static __device__ __noinline__ float sample_scalar(const RenderArgs& a, float3 s) {
   int x0, x1, y0, y1, z0, z1;
   float ax, ay, az;
   clamp_axis(s.x, a.sn[0], x0, x1, ax);
