@@ -257,6 +257,22 @@ vvlic_status vvlic_upload_field_interp(vvlic_ctx* ctx, const void* xyz0, const v
 vvlic_status vvlic_upload_field_device(vvlic_ctx* ctx, const float* d_xyz,
                                        int32_t nx, int32_t ny, int32_t nz, const float* slice_dist,
                                        int32_t storage, void* stream, int32_t* vol_id);
+/* Replace the field of volume `vol_id` with new raw vectors of the same dimensions, in place.
+ * The reference re-creates its field texture on every animation frame (idle(), 3DLIC.cpp:129-145
+ * -> VectorDataSet::createTextureIterp, dataset.cpp:290-366).  Here:
+ *   - the encoded texels and any cell or texture copies are rewritten without reallocation,
+ *     so volume ids, the device pointers in batch job tables and captured batch graphs stay valid;
+ *   - storage and slice distances stay the volume's;
+ *   - a precomputed LIC volume turns stale: LICVOLUME renders return VVLIC_ERR_NOT_READY until
+ *     vvlic_compute_lic_volume runs again (the reference calls updateLICVolume in that mode);
+ *   - a recorded adjoint tape of this volume is dropped.
+ * Waits for the device's in-flight work, then returns when the update is complete. */
+vvlic_status vvlic_update_field(vvlic_ctx* ctx, int32_t vol_id, const void* xyz, int32_t dtype,
+                                int32_t nx, int32_t ny, int32_t nz);
+/* The same with the time interpolation of vvlic_upload_field_interp. */
+vvlic_status vvlic_update_field_interp(vvlic_ctx* ctx, int32_t vol_id, const void* xyz0, const void* xyz1,
+                                       int32_t dtype, int32_t nx, int32_t ny, int32_t nz,
+                                       int32_t interp_index, int32_t interp_size);
 vvlic_status vvlic_free_volume(vvlic_ctx* ctx, int32_t vol_id);
 /* Copy a volume's encoded texels (RGBA per voxel, x fastest, at the volume's storage precision:
  * 16 bytes per voxel for F32, 8 for F16/BF16) to host memory; `capacity` is the size of `out`
@@ -270,7 +286,10 @@ vvlic_status vvlic_volume_bytes(const vvlic_ctx* ctx, int32_t vol_id, uint64_t* 
 /* Noise upload: NoiseDataSet::createTexture (dataset.cpp:1176-1344) + Renderer::setNoiseTex.
  * `noise` is host uint8, mx*my*mz, x fastest.  mode = VVLIC_NOISE_*; gradient modes run
  * computeGradients -> filterGradients -> quantizeGradients (gradient.cpp:190-531) on the device
- * and pack RGBA = (gradient, noise) like dataset.cpp:1270-1286.  Wrap is REPEAT. */
+ * and pack RGBA = (gradient, noise) like dataset.cpp:1270-1286.  Wrap is REPEAT.  A noise of
+ * the same extent and channel count as the current one is rewritten in place (texels, cell and
+ * texture copies) after the device's in-flight work; any other replaces it.  Either way a
+ * recorded adjoint tape is dropped. */
 vvlic_status vvlic_upload_noise(vvlic_ctx* ctx, const uint8_t* noise,
                                 int32_t mx, int32_t my, int32_t mz, int32_t mode);
 /* Noise with precomputed gradients: mx*my*mz RGBA texels (quantised gradient x, y, z, noise)

@@ -72,6 +72,16 @@ class Renderer {
     return id;
   }
   void useVolume(int id) { vol_ = id; }
+  /* The animation step of idle() (3DLIC.cpp:129-145): createTextureIterp of the next
+   * interpolation stage, here rewriting the current volume in place (same dimensions). */
+  void updateDataTex(const float* xyz0, const float* xyz1, int nx, int ny, int nz, int interpIndex,
+                     int interpSize) {
+    check(vvlic_update_field_interp(ctx_, vol_, xyz0, xyz1, VVLIC_DTYPE_FLOAT32, nx, ny, nz, interpIndex, interpSize),
+          "updateDataTex");
+  }
+  void updateDataTex(const float* xyz, int nx, int ny, int nz) {
+    check(vvlic_update_field(ctx_, vol_, xyz, VVLIC_DTYPE_FLOAT32, nx, ny, nz), "updateDataTex");
+  }
   /* VectorDataSet::loadData(file) + createTextureIterp: a .dat/.raw vector data set (the
    * timestep, or the first one for -1) becomes the current volume */
   int loadData(const char* datFile, int timestep = -1, int storage = VVLIC_STORAGE_F16) {

@@ -1,0 +1,180 @@
+"""In-place input updates: vvlic_update_field / vvlic_update_field_interp (the reference's per-frame
+createTextureIterp of its animation loop, 3DLIC.cpp:129-145) and a same-shape vvlic_upload_noise.
+After an update every layout the volume or noise already had (cells, texture copy) must hold the
+new data: images equal those of a freshly uploaded volume bit for bit, on every sampler and
+storage.  Stale derived state (LIC volume, adjoint tape) is refused rather than used."""
+import numpy as np
+import pytest
+
+from vectorvisualization_gb300 import capi, workloads as wl
+
+pytestmark = pytest.mark.gpu
+
+SAMPLERS = ["gather", "cell", "texture", "hybrid"]
+
+
+def small():
+    w = wl.c1(size=24, image=40)
+    w.params.steps_forward = w.params.steps_backward = 6
+    return w
+
+
+def render(ctx, vid, w, sampler):
+    p = w.params
+    p.sampler = capi.SAMPLER[sampler]
+    ctx.set_params(p)
+    return ctx.render(vid, w.width, w.height)
+
+
+def other_field(w, seed):
+    return wl.vortex_field(w.field.shape[2::-1], seed=seed).astype(np.float32)
+
+
+@pytest.mark.parametrize("storage", ["f16", "bf16", "u8"])
+def test_update_field_equals_fresh_upload(ctx, storage):
+    w = small()
+    vid = wl.setup_context(ctx, w, storage=storage)
+    for sm in SAMPLERS:  # build every layout of the old field
+        render(ctx, vid, w, sm)
+    new = other_field(w, seed=77)
+    ctx.update_field(vid, new)
+    fresh = ctx.upload_field(new, storage=storage)
+    for sm in SAMPLERS:
+        a = render(ctx, vid, w, sm)
+        b = render(ctx, fresh, w, sm)
+        np.testing.assert_array_equal(a, b, err_msg=f"{storage}/{sm}")
+    nz, ny, nx = new.shape[:3]
+    np.testing.assert_array_equal(ctx.download_field(vid, (nx, ny, nz), storage),
+                                  ctx.download_field(fresh, (nx, ny, nz), storage))
+    ctx.free_volume(fresh)
+    ctx.free_volume(vid)
+
+
+def test_update_field_interp_equals_upload_field_interp(ctx):
+    w = small()
+    f0, f1 = w.field, other_field(w, seed=5)
+    vid = wl.setup_context(ctx, w, storage="f16")
+    render(ctx, vid, w, "hybrid")
+    for index in (1, 3):
+        ctx.update_field_interp(vid, f0, f1, index, 4)
+        fresh = ctx.upload_field_interp(f0, f1, index, 4, storage="f16")
+        np.testing.assert_array_equal(render(ctx, vid, w, "hybrid"), render(ctx, fresh, w, "hybrid"))
+        ctx.free_volume(fresh)
+    ctx.free_volume(vid)
+
+
+def test_update_field_rejects_other_dimensions(ctx):
+    w = small()
+    vid = wl.setup_context(ctx, w)
+    bad = np.zeros((w.field.shape[0] + 1,) + w.field.shape[1:], np.float32)
+    with pytest.raises(capi.VVLICError) as e:
+        ctx.update_field(vid, bad)
+    assert e.value.status == capi.ERR_INVALID_ARGUMENT
+    with pytest.raises(capi.VVLICError) as e:
+        ctx.update_field(vid + 1000, w.field)
+    assert e.value.status == capi.ERR_INVALID_ARGUMENT
+    ctx.free_volume(vid)
+
+
+def test_lic_volume_is_stale_after_update(ctx):
+    w = small()
+    vid = wl.setup_context(ctx, w)
+    ctx.compute_lic_volume(vid, (24, 24, 24))
+    p = w.params
+    p.technique = capi.TECHNIQUE["licvolume"]
+    ctx.set_params(p)
+    ctx.render(vid, w.width, w.height)
+    ctx.update_field(vid, other_field(w, seed=3))
+    with pytest.raises(capi.VVLICError) as e:
+        ctx.render(vid, w.width, w.height)
+    assert e.value.status == capi.ERR_NOT_READY
+    p.technique = capi.TECHNIQUE["raycast"]
+    ctx.set_params(p)
+    ctx.compute_lic_volume(vid, (24, 24, 24))
+    fresh = ctx.upload_field(other_field(w, seed=3))
+    ctx.compute_lic_volume(fresh, (24, 24, 24))
+    p.technique = capi.TECHNIQUE["licvolume"]
+    ctx.set_params(p)
+    np.testing.assert_array_equal(ctx.render(vid, w.width, w.height), ctx.render(fresh, w.width, w.height))
+    p.technique = capi.TECHNIQUE["raycast"]
+    ctx.set_params(p)
+    ctx.free_volume(fresh)
+    ctx.free_volume(vid)
+
+
+@pytest.mark.parametrize("sampler", ["cell", "texture", "hybrid"])
+def test_same_shape_noise_upload_rewrites_every_layout(sampler):
+    w = small()
+    rng = np.random.default_rng(12)
+    noise2 = rng.integers(0, 256, w.noise.shape, dtype=np.uint8)
+    with capi.Context(0) as a, capi.Context(0) as b:
+        va = wl.setup_context(a, w)
+        render(a, va, w, sampler)  # builds the noise layout of the first noise
+        a.upload_noise(noise2, w.noise_mode)
+        got = render(a, va, w, sampler)
+        vb = wl.setup_context(b, w)
+        b.upload_noise(noise2, w.noise_mode)
+        np.testing.assert_array_equal(got, render(b, vb, w, sampler))
+
+
+def test_adjoint_tape_dropped_by_input_changes(ctx):
+    import torch
+
+    w = small()
+    vid = wl.setup_context(ctx, w, storage="f16")
+    g = torch.zeros((w.height, w.width, 4), dtype=torch.float32, device="cuda")
+    d = [torch.zeros(n, dtype=torch.float32, device="cuda") for n in (1024, 256, 2 * 6 + 1)]
+
+    def record():
+        p = w.params
+        p.sampler = capi.SAMPLER["hybrid"]
+        p.record_tape = 1
+        ctx.set_params(p)
+        ctx.render(vid, w.width, w.height)
+        p.record_tape = 0
+        ctx.set_params(p)
+
+    def adjoint():
+        ctx.render_adjoint(vid, g.data_ptr(), w.width, w.height, *(x.data_ptr() for x in d))
+        torch.cuda.synchronize()
+
+    record()
+    adjoint()  # a valid tape
+    ctx.update_field(vid, other_field(w, seed=9))
+    with pytest.raises(capi.VVLICError) as e:
+        adjoint()
+    assert e.value.status == capi.ERR_NOT_READY
+    record()
+    ctx.upload_noise(w.noise, w.noise_mode)
+    with pytest.raises(capi.VVLICError) as e:
+        adjoint()
+    assert e.value.status == capi.ERR_NOT_READY
+    record()
+    ctx.free_volume(vid)
+    with pytest.raises(capi.VVLICError) as e:
+        adjoint()
+    assert e.value.status in (capi.ERR_NOT_READY, capi.ERR_INVALID_ARGUMENT)
+
+
+def test_batch_replay_follows_an_updated_field(ctx):
+    import torch
+
+    w = small()
+    vid = wl.setup_context(ctx, w, storage="f16")
+    p = w.params
+    p.sampler = capi.SAMPLER["hybrid"]
+    outs = [torch.zeros((w.height, w.width, 4), dtype=torch.float32, device="cuda") for _ in range(2)]
+    views = [w.views[0], wl.perspective_view(wl.quat_axis_angle((0, 1, 0), 40.0), distance=2.2)]
+    jobs = [capi.make_job(vid, o.data_ptr(), w.width, w.height, v, p, w.filter_table) for o, v in zip(outs, views)]
+    stream = torch.cuda.Stream()
+    ctx.batch_render(jobs, stream.cuda_stream)  # captures the graph
+    stream.synchronize()
+    ctx.update_field(vid, other_field(w, seed=21))
+    ctx.batch_render(jobs, stream.cuda_stream)
+    stream.synchronize()
+    ctx.set_filter_table(w.filter_table)
+    ctx.set_params(p)
+    for o, v in zip(outs, views):
+        ctx.set_view(v)
+        np.testing.assert_array_equal(o.cpu().numpy(), ctx.render(vid, w.width, w.height))
+    ctx.free_volume(vid)

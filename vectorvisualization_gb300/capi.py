@@ -178,6 +178,8 @@ _SIGS = {
     "vvlic_upload_field": (_I, [_P, _P, _I, _I, _I, _I, _P, _I, C.POINTER(_I)]),
     "vvlic_upload_field_device": (_I, [_P, _P, _I, _I, _I, _P, _I, _P, C.POINTER(_I)]),
     "vvlic_upload_field_interp": (_I, [_P, _P, _P, _I, _I, _I, _I, _P, _I, _I, _I, C.POINTER(_I)]),
+    "vvlic_update_field": (_I, [_P, _I, _P, _I, _I, _I, _I]),
+    "vvlic_update_field_interp": (_I, [_P, _I, _P, _P, _I, _I, _I, _I, _I, _I]),
     "vvlic_free_volume": (_I, [_P, _I]),
     "vvlic_volume_bytes": (_I, [_P, _I, C.POINTER(C.c_uint64)]),
     "vvlic_upload_noise": (_I, [_P, _P, _I, _I, _I, _I]),
@@ -360,6 +362,29 @@ class Context:
                                                          _ptr(sd), STORAGE[storage], index, size, C.byref(vid)),
                     "upload_field_interp")
         return vid.value
+
+    def update_field(self, vid: int, xyz: np.ndarray):
+        """Replace volume `vid`'s field in place with new (nz, ny, nx, 3) vectors of its dimensions."""
+        a = np.ascontiguousarray(xyz)
+        if a.ndim != 4 or a.shape[3] != 3:
+            raise ValueError("field must have shape (nz, ny, nx, 3)")
+        dtype = DTYPE_UINT8 if a.dtype == np.uint8 else DTYPE_FLOAT32
+        if dtype == DTYPE_FLOAT32:
+            a = a.astype(np.float32, copy=False)
+        nz, ny, nx = a.shape[:3]
+        self._check(self._lib.vvlic_update_field(self.h, vid, a.ctypes.data, dtype, nx, ny, nz), "update_field")
+
+    def update_field_interp(self, vid: int, xyz0: np.ndarray, xyz1: np.ndarray, index: int, size: int):
+        """Replace volume `vid`'s field in place with the time interpolation at index/size."""
+        a0, a1 = np.ascontiguousarray(xyz0), np.ascontiguousarray(xyz1)
+        if a0.shape != a1.shape or a0.dtype != a1.dtype or a0.ndim != 4:
+            raise ValueError("timesteps must have the same (nz, ny, nx, 3) shape and dtype")
+        dtype = DTYPE_UINT8 if a0.dtype == np.uint8 else DTYPE_FLOAT32
+        if dtype == DTYPE_FLOAT32:
+            a0, a1 = a0.astype(np.float32, copy=False), a1.astype(np.float32, copy=False)
+        nz, ny, nx = a0.shape[:3]
+        self._check(self._lib.vvlic_update_field_interp(self.h, vid, a0.ctypes.data, a1.ctypes.data, dtype, nx, ny,
+                                                         nz, index, size), "update_field_interp")
 
     def upload_field_device(self, d_xyz: int, dims, slice_dist=None, storage: str = "f32", stream: int = 0) -> int:
         nx, ny, nz = dims

@@ -501,6 +501,75 @@ extern "C" vvlic_status vvlic_upload_field_interp(vvlic_ctx* c, const void* xyz0
   return VVLIC_OK;
 }
 
+// Re-encodes the raw vectors at d_xyz into the existing volume and rewrites its cell and texture
+// copies, on the context stream; the caller has waited for renders that read the old texels.
+static vvlic_status reencode_volume(vvlic_ctx* c, int32_t vol_id, Volume& v, const void* d_xyz, int dtype) {
+  cudaError_t e = launch_encode_field(d_xyz, dtype, v.n, v.storage, v.d_texels, c->d_scratch_word, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "field encoding");
+  vvlic_status st = refresh_volume_layouts(c, v, c->stream);
+  if (st) return st;
+  v.licvol_valid = false;  // the precomputed LIC volume belongs to the previous field
+  if (c->tape_vol == vol_id) c->tape_valid = false;
+  e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "field update");
+  return VVLIC_OK;
+}
+
+static vvlic_status update_target(vvlic_ctx* c, int32_t vol_id, int32_t dtype, int32_t nx, int32_t ny, int32_t nz,
+                                  const char* what, Volume** v) {
+  auto it = c->vols.find(vol_id);
+  if (it == c->vols.end()) return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "%s: unknown volume %d", what, vol_id);
+  if (it->second.n[0] != nx || it->second.n[1] != ny || it->second.n[2] != nz)
+    return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "%s: %dx%dx%d does not match the volume's %dx%dx%d", what, nx, ny, nz,
+                it->second.n[0], it->second.n[1], it->second.n[2]);
+  if (dtype != VVLIC_DTYPE_FLOAT32 && dtype != VVLIC_DTYPE_UINT8)
+    return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "%s: dtype %d", what, dtype);
+  *v = &it->second;
+  return VVLIC_OK;
+}
+
+extern "C" vvlic_status vvlic_update_field(vvlic_ctx* c, int32_t vol_id, const void* xyz, int32_t dtype, int32_t nx,
+                                          int32_t ny, int32_t nz) {
+  if (!c) return VVLIC_ERR_BAD_HANDLE;
+  if (!xyz) return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "update_field: null data");
+  Volume* v = nullptr;
+  vvlic_status st = update_target(c, vol_id, dtype, nx, ny, nz, "update_field", &v);
+  if (st) return st;
+  DeviceGuard g(c->device);
+  const size_t bytes = (size_t)nx * ny * nz * 3 * (dtype == VVLIC_DTYPE_FLOAT32 ? 4 : 1);
+  if ((st = grow(c, &c->d_upload, &c->upload_cap, bytes))) return st;
+  // renders launched on any stream may still read the volume's texels
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(c->d_upload, xyz, bytes, cudaMemcpyHostToDevice, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "update_field copy");
+  return reencode_volume(c, vol_id, *v, c->d_upload, dtype);
+}
+
+extern "C" vvlic_status vvlic_update_field_interp(vvlic_ctx* c, int32_t vol_id, const void* xyz0, const void* xyz1,
+                                                 int32_t dtype, int32_t nx, int32_t ny, int32_t nz,
+                                                 int32_t interp_index, int32_t interp_size) {
+  if (!c) return VVLIC_ERR_BAD_HANDLE;
+  if (!xyz0 || !xyz1 || interp_size < 1 || interp_index < 0 || interp_index >= interp_size)
+    return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "update_field_interp: bad arguments");
+  Volume* v = nullptr;
+  vvlic_status st = update_target(c, vol_id, dtype, nx, ny, nz, "update_field_interp", &v);
+  if (st) return st;
+  DeviceGuard g(c->device);
+  const int n[3] = {nx, ny, nz};
+  const size_t bytes = (size_t)nx * ny * nz * 3 * (dtype == VVLIC_DTYPE_FLOAT32 ? 4 : 1);
+  const size_t slot = (bytes + 255) & ~(size_t)255;
+  if ((st = grow(c, &c->d_upload, &c->upload_cap, 3 * slot))) return st;
+  char* base = (char*)c->d_upload;
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(base, xyz0, bytes, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(base + slot, xyz1, bytes, cudaMemcpyHostToDevice, c->stream);
+  // (float)interpIndex / InterpSize, as the reference computes it
+  const float t = (float)interp_index / (float)interp_size;
+  if (e == cudaSuccess) e = launch_interp_field(base, base + slot, dtype, n, t, base + 2 * slot, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "update_field_interp");
+  return reencode_volume(c, vol_id, *v, base + 2 * slot, dtype);
+}
+
 extern "C" vvlic_status vvlic_upload_field_device(vvlic_ctx* c, const float* d_xyz, int32_t nx, int32_t ny, int32_t nz,
                                                  const float* slice_dist, int32_t storage, void* stream,
                                                  int32_t* vol_id) {
@@ -521,6 +590,7 @@ extern "C" vvlic_status vvlic_free_volume(vvlic_ctx* c, int32_t vol_id) {
   cudaStreamSynchronize(c->stream);
   free_volume(it->second);
   c->vols.erase(it);
+  if (c->tape_vol == vol_id) c->tape_valid = false;  // the tape points at the freed buffers
   return VVLIC_OK;
 }
 
@@ -556,6 +626,26 @@ extern "C" vvlic_status vvlic_noise_gradients_device(const uint8_t* d_noise, int
   return VVLIC_OK;
 }
 
+// Upload-buffer layout for noise gradients: the noise bytes, then (256-byte aligned) the raw
+// float gradients.
+static size_t noise_grad_offset(size_t count) { return (count + 255) & ~(size_t)255; }
+static size_t noise_staging_bytes(size_t count) { return noise_grad_offset(count) + count * 3 * sizeof(float); }
+
+// Noise gradients (computeGradients + filterGradients + quantizeGradients + pack) of the noise
+// bytes staged at the start of the context's upload buffer (noise_staging_bytes of capacity),
+// into d_rgba.
+static vvlic_status noise_gradients_staged(vvlic_ctx* c, const int m[3], int mode, uint8_t* d_rgba) {
+  const size_t count = (size_t)m[0] * m[1] * m[2];
+  const size_t off = noise_grad_offset(count);
+  const float sd[3] = {1.f, 1.f, 1.f};
+  float w27[27];
+  noise_filter_weights(w27);
+  cudaError_t e = launch_noise_gradients((const uint8_t*)c->d_upload, m, mode, sd,
+                                         (float*)((char*)c->d_upload + off), d_rgba, w27, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "noise gradients");
+  return VVLIC_OK;
+}
+
 extern "C" vvlic_status vvlic_upload_noise(vvlic_ctx* c, const uint8_t* noise, int32_t mx, int32_t my, int32_t mz,
                                           int32_t mode) {
   if (!c) return VVLIC_ERR_BAD_HANDLE;
@@ -566,26 +656,43 @@ extern "C" vvlic_status vvlic_upload_noise(vvlic_ctx* c, const uint8_t* noise, i
   if (mode != VVLIC_NOISE_SCALAR && (mx < 2 || my < 2 || mz < 2))
     return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "upload_noise: gradients need at least 2 voxels per axis");
   DeviceGuard g(c->device);
-  free_noise(c->noise);
   NoiseTex& n = c->noise;
   const size_t count = (size_t)mx * my * mz;
-  n.m[0] = mx;
-  n.m[1] = my;
-  n.m[2] = mz;
-  n.ch = mode == VVLIC_NOISE_SCALAR ? 1 : 4;
+  const int ch = mode == VVLIC_NOISE_SCALAR ? 1 : 4;
+  c->tape_valid = false;  // a recorded tape read the previous noise
+  if (mode != VVLIC_NOISE_SCALAR) {
+    vvlic_status st = grow(c, &c->d_upload, &c->upload_cap, noise_staging_bytes(count));
+    if (st) return st;
+  }
+  // Same extent and layout: rewrite the texels and the cell / texture copies in place once the
+  // renders already launched on any stream (which read the previous noise) have finished.
+  const bool in_place = n.d_texels && n.m[0] == mx && n.m[1] == my && n.m[2] == mz && n.ch == ch;
+  cudaError_t e = cudaSuccess;
+  if (in_place) {
+    e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return cuda_fail(c, e, "upload_noise");
+  } else {
+    free_noise(n);
+    e = cudaMalloc(&n.d_texels, count * ch);
+    if (e != cudaSuccess) return cuda_fail(c, e, "noise allocation");
+    n.m[0] = mx;
+    n.m[1] = my;
+    n.m[2] = mz;
+    n.ch = ch;
+  }
   n.mode = mode;
-  cudaError_t e = cudaMalloc(&n.d_texels, count * n.ch);
-  if (e != cudaSuccess) return cuda_fail(c, e, "noise allocation");
   if (mode == VVLIC_NOISE_SCALAR) {
     e = cudaMemcpyAsync(n.d_texels, noise, count, cudaMemcpyHostToDevice, c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "noise copy");
   } else {
-    vvlic_status st = grow(c, &c->d_upload, &c->upload_cap, count);
-    if (st) return st;
     e = cudaMemcpyAsync(c->d_upload, noise, count, cudaMemcpyHostToDevice, c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "noise copy");
-    st = vvlic_noise_gradients_device((const uint8_t*)c->d_upload, mx, my, mz, mode, nullptr, n.d_texels, c->stream);
-    if (st) return fail(c, st, "noise gradients: %s", cudaGetErrorString(cudaGetLastError()));
+    vvlic_status st = noise_gradients_staged(c, m, mode, n.d_texels);
+    if (st) return st;
+  }
+  if (in_place) {
+    vvlic_status st = refresh_noise_layouts(c, n, c->stream);
+    if (st) return st;
   }
   e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "upload_noise");
@@ -601,6 +708,7 @@ extern "C" vvlic_status vvlic_upload_noise_rgba(vvlic_ctx* c, const uint8_t* rgb
     return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "upload_noise_rgba: mode %d is not a gradient mode", mode);
   DeviceGuard g(c->device);
   free_noise(c->noise);
+  c->tape_valid = false;
   NoiseTex& n = c->noise;
   const size_t bytes = (size_t)mx * my * mz * 4;
   n.m[0] = mx;
@@ -623,6 +731,7 @@ extern "C" vvlic_status vvlic_upload_scalar(vvlic_ctx* c, const float* scalar, i
   DeviceGuard g(c->device);
   if (c->d_scalar) cudaFree(c->d_scalar);
   c->d_scalar = nullptr;
+  c->tape_valid = false;
   const size_t bytes = (size_t)nx * ny * nz * sizeof(float);
   cudaError_t e = cudaMalloc(&c->d_scalar, bytes);
   if (e != cudaSuccess) return cuda_fail(c, e, "scalar allocation");

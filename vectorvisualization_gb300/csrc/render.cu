@@ -39,21 +39,15 @@ vvlic_status ensure_noise_cells(vvlic_ctx* c, NoiseTex& n, cudaStream_t s) {
   return VVLIC_OK;
 }
 
-vvlic_status ensure_texture(vvlic_ctx* c, Volume& v, cudaStream_t s) {
-  if (v.tex) return VVLIC_OK;
-  // The texture unit has no bf16 format: a BF16 volume's texture is a half4 array holding its
-  // BF16 texels converted to half (exact for the encoded texels, all in [0, 1], down to 2^-14).
+// Copies the volume's texels into its texture array (allocated by ensure_texture).  The texture
+// unit has no bf16 format: a BF16 volume's texture is a half4 array holding its BF16 texels
+// converted to half (exact for the encoded texels, all in [0, 1], down to 2^-14).
+vvlic_status copy_field_texture(vvlic_ctx* c, Volume& v, cudaStream_t s) {
   const bool bf16 = v.storage == VVLIC_STORAGE_BF16;
-  cudaChannelFormatDesc desc = v.storage == VVLIC_STORAGE_F32 ? cudaCreateChannelDesc<float4>()
-                               : (v.storage == VVLIC_STORAGE_F16 || bf16) ? cudaCreateChannelDescHalf4()
-                                                                          : cudaCreateChannelDesc<uchar4>();
-  cudaExtent ext = make_cudaExtent(v.n[0], v.n[1], v.n[2]);
-  cudaError_t e = cudaMalloc3DArray(&v.array, &desc, ext);
-  if (e != cudaSuccess) return cuda_fail(c, e, "texture array allocation");
   const size_t tb = texel_bytes(v.storage);  // 8 bytes for F16, BF16 and their half4 copy alike
   const size_t count = (size_t)v.n[0] * v.n[1] * v.n[2];
-  v.array_bytes = count * tb;
   void* src = v.d_texels;
+  cudaError_t e;
   if (bf16) {
     // stream-ordered scratch: freed behind the array copy that reads it
     e = cudaMallocAsync(&src, count * tb, s);
@@ -68,7 +62,7 @@ vvlic_status ensure_texture(vvlic_ctx* c, Volume& v, cudaStream_t s) {
   std::memset(&cp, 0, sizeof cp);
   cp.srcPtr = make_cudaPitchedPtr(src, v.n[0] * tb, v.n[0], v.n[1]);
   cp.dstArray = v.array;
-  cp.extent = ext;
+  cp.extent = make_cudaExtent(v.n[0], v.n[1], v.n[2]);
   cp.kind = cudaMemcpyDeviceToDevice;
   e = cudaMemcpy3DAsync(&cp, s);
   if (bf16) {
@@ -76,6 +70,21 @@ vvlic_status ensure_texture(vvlic_ctx* c, Volume& v, cudaStream_t s) {
     if (e == cudaSuccess) e = ef;
   }
   if (e != cudaSuccess) return cuda_fail(c, e, "texture array copy");
+  return VVLIC_OK;
+}
+
+vvlic_status ensure_texture(vvlic_ctx* c, Volume& v, cudaStream_t s) {
+  if (v.tex) return VVLIC_OK;
+  const bool bf16 = v.storage == VVLIC_STORAGE_BF16;
+  cudaChannelFormatDesc desc = v.storage == VVLIC_STORAGE_F32 ? cudaCreateChannelDesc<float4>()
+                               : (v.storage == VVLIC_STORAGE_F16 || bf16) ? cudaCreateChannelDescHalf4()
+                                                                          : cudaCreateChannelDesc<uchar4>();
+  cudaExtent ext = make_cudaExtent(v.n[0], v.n[1], v.n[2]);
+  cudaError_t e = cudaMalloc3DArray(&v.array, &desc, ext);
+  if (e != cudaSuccess) return cuda_fail(c, e, "texture array allocation");
+  v.array_bytes = (size_t)v.n[0] * v.n[1] * v.n[2] * texel_bytes(v.storage);
+  vvlic_status st = copy_field_texture(c, v, s);
+  if (st) return st;
   cudaResourceDesc rd;
   std::memset(&rd, 0, sizeof rd);
   rd.resType = cudaResourceTypeArray;
@@ -92,6 +101,18 @@ vvlic_status ensure_texture(vvlic_ctx* c, Volume& v, cudaStream_t s) {
 }
 
 // Noise as an R8 / RGBA8 texture read as normalised float with WRAP addressing (GL REPEAT).
+vvlic_status copy_noise_texture(vvlic_ctx* c, NoiseTex& n, cudaStream_t s) {
+  cudaMemcpy3DParms cp;
+  std::memset(&cp, 0, sizeof cp);
+  cp.srcPtr = make_cudaPitchedPtr(n.d_texels, (size_t)n.m[0] * n.ch, n.m[0], n.m[1]);
+  cp.dstArray = n.array;
+  cp.extent = make_cudaExtent(n.m[0], n.m[1], n.m[2]);
+  cp.kind = cudaMemcpyDeviceToDevice;
+  cudaError_t e = cudaMemcpy3DAsync(&cp, s);
+  if (e != cudaSuccess) return cuda_fail(c, e, "noise texture copy");
+  return VVLIC_OK;
+}
+
 vvlic_status ensure_noise_texture(vvlic_ctx* c, NoiseTex& n, cudaStream_t s) {
   if (n.tex) return VVLIC_OK;
   cudaChannelFormatDesc desc =
@@ -99,14 +120,8 @@ vvlic_status ensure_noise_texture(vvlic_ctx* c, NoiseTex& n, cudaStream_t s) {
   cudaExtent ext = make_cudaExtent(n.m[0], n.m[1], n.m[2]);
   cudaError_t e = cudaMalloc3DArray(&n.array, &desc, ext);
   if (e != cudaSuccess) return cuda_fail(c, e, "noise texture allocation");
-  cudaMemcpy3DParms cp;
-  std::memset(&cp, 0, sizeof cp);
-  cp.srcPtr = make_cudaPitchedPtr(n.d_texels, (size_t)n.m[0] * n.ch, n.m[0], n.m[1]);
-  cp.dstArray = n.array;
-  cp.extent = ext;
-  cp.kind = cudaMemcpyDeviceToDevice;
-  e = cudaMemcpy3DAsync(&cp, s);
-  if (e != cudaSuccess) return cuda_fail(c, e, "noise texture copy");
+  vvlic_status st = copy_noise_texture(c, n, s);
+  if (st) return st;
   cudaResourceDesc rd;
   std::memset(&rd, 0, sizeof rd);
   rd.resType = cudaResourceTypeArray;
@@ -125,6 +140,24 @@ vvlic_status ensure_noise_texture(vvlic_ctx* c, NoiseTex& n, cudaStream_t s) {
 }  // namespace
 
 namespace vvlic {
+
+vvlic_status refresh_volume_layouts(vvlic_ctx* c, Volume& v, cudaStream_t s) {
+  if (v.d_cells) {
+    cudaError_t e = launch_build_field_cells(v.d_texels, v.n, v.storage, v.d_cells, s);
+    if (e != cudaSuccess) return cuda_fail(c, e, "cell layout rebuild");
+  }
+  if (v.array) return copy_field_texture(c, v, s);
+  return VVLIC_OK;
+}
+
+vvlic_status refresh_noise_layouts(vvlic_ctx* c, NoiseTex& n, cudaStream_t s) {
+  if (n.d_cells) {
+    cudaError_t e = launch_build_noise_cells(n.d_texels, n.m, n.ch, n.d_cells, s);
+    if (e != cudaSuccess) return cuda_fail(c, e, "noise cell rebuild");
+  }
+  if (n.array) return copy_noise_texture(c, n, s);
+  return VVLIC_OK;
+}
 
 // Fill the kernel argument block for one volume and image size.
 vvlic_status build_render_args(vvlic_ctx* c, Volume& v, int W, int H, cudaStream_t s, RenderArgs& a) {
@@ -430,7 +463,7 @@ extern "C" vvlic_status vvlic_render_device(vvlic_ctx* c, int32_t vol_id, float*
       derive_slicing(c->view, v.geom, a.step_size, t.v, &t.depth, &t.nslices);
       for (int i = 0; i < 3; ++i) t.c[i] = v.geom.center[i];
     } else if (t.technique == VVLIC_TECHNIQUE_LICVOLUME) {
-      if (!v.d_licvol)
+      if (!v.d_licvol || !v.licvol_valid)
         return fail(c, VVLIC_ERR_NOT_READY, "render: LICVOLUME needs vvlic_compute_lic_volume for volume %d", vol_id);
       t.licvol = v.d_licvol;
       for (int i = 0; i < 3; ++i) t.ln[i] = v.ln[i];
@@ -528,7 +561,9 @@ extern "C" vvlic_status vvlic_render_adjoint(vvlic_ctx* c, int32_t vol_id, const
   const RenderArgs& a = c->tape_args;
   Schedule sch;
   sch.num_sms = c->num_sms;
-  vvlic_status st = make_schedule(c, a, c->vols[vol_id].geom, w, h, s, sch);
+  auto vt = c->vols.find(vol_id);
+  if (vt == c->vols.end()) return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "render_adjoint: unknown volume %d", vol_id);
+  vvlic_status st = make_schedule(c, a, vt->second.geom, w, h, s, sch);
   if (st) return st;
   e = cudaEventRecord(c->ev0, s);
   const float4* gi = (const float4*)d_dl_drgba;
@@ -638,13 +673,14 @@ extern "C" vvlic_status vvlic_compute_lic_volume(vvlic_ctx* c, int32_t vol_id, i
   cudaError_t e = launch_technique(v.storage, a, t, c->params.sampler, c->params.integrator, false, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return cuda_fail(c, e, "compute_lic_volume");
+  v.licvol_valid = true;
   return VVLIC_OK;
 }
 
 extern "C" vvlic_status vvlic_download_lic_volume(vvlic_ctx* c, int32_t vol_id, float* out, uint64_t capacity) {
   if (!c) return VVLIC_ERR_BAD_HANDLE;
   auto it = c->vols.find(vol_id);
-  if (it == c->vols.end() || !it->second.d_licvol)
+  if (it == c->vols.end() || !it->second.d_licvol || !it->second.licvol_valid)
     return fail(c, VVLIC_ERR_NOT_READY, "download_lic_volume: no LIC volume for volume %d", vol_id);
   const size_t bytes = (size_t)it->second.ln[0] * it->second.ln[1] * it->second.ln[2] * sizeof(float);
   if (!out || capacity < bytes) return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "download_lic_volume: need %zu bytes", bytes);

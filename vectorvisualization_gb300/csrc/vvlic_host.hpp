@@ -32,6 +32,7 @@ struct Volume {
   size_t array_bytes = 0;
   float* d_licvol = nullptr;      // precomputed LIC volume (vvlic_compute_lic_volume)
   int ln[3] = {0, 0, 0};
+  bool licvol_valid = false;      // false after a field update until the next precompute
 };
 
 struct NoiseTex {
@@ -146,6 +147,9 @@ vvlic_status ensure_illum_luts(vvlic_ctx* c);
 // Orders the context stream after the context's last launch (device-table updates).
 cudaError_t after_launches(vvlic_ctx* c);
 vvlic_status cuda_fail(vvlic_ctx* c, cudaError_t e, const char* what);
+// Rewrite the cell and texture copies that exist from the texels, in place (render.cu).
+vvlic_status refresh_volume_layouts(vvlic_ctx* c, Volume& v, cudaStream_t s);
+vvlic_status refresh_noise_layouts(vvlic_ctx* c, NoiseTex& n, cudaStream_t s);
 Geometry make_geometry(const int n[3], const float* slice_dist);
 vvlic_status derive_taps(const vvlic_ctx* c, int lb, int lf, float* taps, float* inv_area);
 void derive_taps_from_table(const uint8_t* t, int W, int clamp, bool is_box, int lb, int lf, float* taps,
