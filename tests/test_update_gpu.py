@@ -178,3 +178,27 @@ def test_batch_replay_follows_an_updated_field(ctx):
         ctx.set_view(v)
         np.testing.assert_array_equal(o.cpu().numpy(), ctx.render(vid, w.width, w.height))
     ctx.free_volume(vid)
+
+
+def test_repeated_updates_allocate_nothing(ctx):
+    # 96^3 FP16 field (7 MB texels, 57 MB cells, 7 MB texture array): a reallocation of any of
+    # them would move the device's free memory by megabytes
+    import torch
+
+    w = wl.c1(size=96, image=64)
+    w.params.steps_forward = w.params.steps_backward = 4
+    vid = wl.setup_context(ctx, w, storage="f16")
+    for sm in SAMPLERS:  # every layout exists before the updates
+        render(ctx, vid, w, sm)
+    ctx.update_field(vid, other_field(w, seed=40))  # grows the staging buffers once
+    ctx.upload_noise(w.noise, w.noise_mode)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for k in range(3):
+        ctx.update_field(vid, other_field(w, seed=41 + k))
+        ctx.upload_noise(w.noise, w.noise_mode)
+        for sm in SAMPLERS:
+            render(ctx, vid, w, sm)
+    torch.cuda.synchronize()
+    assert abs(torch.cuda.mem_get_info()[0] - free0) < (1 << 20)
+    ctx.free_volume(vid)
