@@ -165,18 +165,36 @@ __global__ void noise_grad_filter_kernel(const uint8_t* v, const float* g, int n
     const int x = (int)(a % nx), y = (int)((a / nx) % ny), z = (int)(a / ((size_t)nx * ny));
     int bd = min(min(min(x, nx - x - 1), min(y, ny - y - 1)), min(z, nz - z - 1));
     const int fw = min(2, bd);
-    float acc[3];
-    for (int c = 0; c < 3; ++c) {
-      float s = 0.0f;
+    // One pass over the window with the three channel sums side by side: each channel adds its
+    // terms in the reference's (k, j, i) order, so the sums are the per-channel loops' bit for bit.
+    float acc[3] = {0.0f, 0.0f, 0.0f};
+    if (fw == 2) {  // interior: k, j, i in {-2, -1, 0}, table entries (k+2, j+2, i+2)
+#pragma unroll
+      for (int k = -2; k < 1; ++k)
+#pragma unroll
+        for (int j = -2; j < 1; ++j) {
+          const float* row = g + 3 * (((size_t)(z + k) * ny + (y + j)) * nx + x);
+#pragma unroll
+          for (int i = -2; i < 1; ++i) {
+            const float w = fw27.w[((k + 2) * 3 + (j + 2)) * 3 + (i + 2)];
+            acc[0] += w * row[3 * i];
+            acc[1] += w * row[3 * i + 1];
+            acc[2] += w * row[3 * i + 2];
+          }
+        }
+    } else {
       for (int k = -fw; k < fw - 1; ++k)
         for (int j = -fw; j < fw - 1; ++j)
           for (int i = -fw; i < fw - 1; ++i) {
             // the reference indexes its 5x5x5 table with the shrunken fw; only entries with
             // all three indices in [0, 2] are ever used
             const int wk = fw + k, wj = fw + j, wi = fw + i;
-            s += fw27.w[(wk * 3 + wj) * 3 + wi] * g[3 * (((size_t)(z + k) * ny + (y + j)) * nx + (x + i)) + c];
+            const float w = fw27.w[(wk * 3 + wj) * 3 + wi];
+            const float* q = g + 3 * (((size_t)(z + k) * ny + (y + j)) * nx + (x + i));
+            acc[0] += w * q[0];
+            acc[1] += w * q[1];
+            acc[2] += w * q[2];
           }
-      acc[c] = s;
     }
     float len = sqrtf(acc[0] * acc[0] + acc[1] * acc[1] + acc[2] * acc[2]);
     if (len < 1e-5f) {
@@ -224,16 +242,24 @@ __global__ void noise_cells_kernel(const uint8_t* texels, int mx, int my, int mz
     const int x = (int)(a % mx), y = (int)((a / mx) % my), z = (int)(a / ((size_t)mx * my));
     const int xs[2] = {x, x + 1 == mx ? 0 : x + 1}, ys[2] = {y, y + 1 == my ? 0 : y + 1},
               zs[2] = {z, z + 1 == mz ? 0 : z + 1};
+    // the cell is assembled in registers and written with 16-byte (RGBA: 32-byte cells) or one
+    // 8-byte (value: 8-byte cells) stores; cells are 32- / 8-byte aligned
     if (ch == 4) {
       const uint32_t* t = reinterpret_cast<const uint32_t*>(texels);
-      uint32_t* c = reinterpret_cast<uint32_t*>(cells);
+      uint32_t q[8];
 #pragma unroll
-      for (int k = 0; k < 8; ++k)
-        c[8 * a + k] = t[((size_t)zs[(k >> 2) & 1] * my + ys[(k >> 1) & 1]) * mx + xs[k & 1]];
+      for (int k = 0; k < 8; ++k) q[k] = t[((size_t)zs[(k >> 2) & 1] * my + ys[(k >> 1) & 1]) * mx + xs[k & 1]];
+      uint4* c = reinterpret_cast<uint4*>(cells) + 2 * a;
+      c[0] = make_uint4(q[0], q[1], q[2], q[3]);
+      c[1] = make_uint4(q[4], q[5], q[6], q[7]);
     } else {
+      uint32_t lo = 0, hi = 0;
 #pragma unroll
-      for (int k = 0; k < 8; ++k)
-        cells[8 * a + k] = texels[((size_t)zs[(k >> 2) & 1] * my + ys[(k >> 1) & 1]) * mx + xs[k & 1]];
+      for (int k = 0; k < 4; ++k) {
+        lo |= (uint32_t)texels[((size_t)zs[(k >> 2) & 1] * my + ys[(k >> 1) & 1]) * mx + xs[k & 1]] << (8 * k);
+        hi |= (uint32_t)texels[((size_t)zs[1] * my + ys[(k >> 1) & 1]) * mx + xs[k & 1]] << (8 * k);
+      }
+      reinterpret_cast<uint2*>(cells)[a] = make_uint2(lo, hi);
     }
   }
 }
