@@ -98,17 +98,17 @@ enum { VVLIC_PERSPECTIVE = 0, VVLIC_ORTHOGRAPHIC = 1 };
 
 /* Reproduced reference behaviours that differ from what the code evidently intends.
  *   LUMINANCE_NOISE    without gradients the noise texture is GL_LUMINANCE whose .a samples
- *                      as 1.0, so the LIC is flat (dataset.cpp:1291-1318, inc_lic.glsl:148).
+ *                      as 1.0, so the LIC is flat (dataset.cpp:1291-1318, inc_lic.glsl:85).
  *   UNIFORM_SCALE_BUG  setRenderVolParams writes scaleInv into the scaleVol uniform and leaves
  *                      scaleVolInv at 0 whenever the shading variant uses scaleVolInv
  *                      (renderer.cpp:941-944); the light direction then ignores the sample
  *                      position.
  *   GRAD_NOISE_NO_FREQ the gradient-noise fetch freqSamplingGrad ignores freqScale
- *                      (inc_lic.glsl:124-131).
+ *                      (inc_lic.glsl:61-68).
  *   ZOECKLER_LUMINANCE the Zoeckler table is a LUMINANCE_ALPHA texture (illumination.cpp:113,
  *                      172), so illumZoeckler's `.rg` reads (L, L): the specular term adds
  *                      0.9 * diffuse-table value and the stored specular alpha is never read
- *                      (inc_illum.glsl:133-143).  Off: `.g` reads the stored specular.
+ *                      (inc_illum.glsl:133-145).  Off: `.g` reads the stored specular.
  * VVLIC_QUIRKS_REFERENCE is what the reference actually computes. */
 enum {
   VVLIC_QUIRK_LUMINANCE_NOISE = 1u << 0,
@@ -138,7 +138,7 @@ typedef struct vvlic_params {
   int32_t tf_index;       /* VVLIC_TF_INDEX_* (DIR_Z) */
   int32_t speed_of_flow;  /* SPEED_OF_FLOW define: scale steps by the magnitude (0) */
   int32_t low_res;        /* Renderer::_lowRes preview overrides, renderer.cpp:947-966 (0) */
-  int32_t scalar_gate;    /* freqSampling's scalar gate, inc_lic.glsl:143 (0 = off) */
+  int32_t scalar_gate;    /* freqSampling's scalar gate, inc_lic.glsl:80 (0 = off) */
   float gate_lo, gate_hi; /* gate bounds (0.1, 0.3) */
   float eye_dist_factor;  /* (logEyeDist*0.5 + 0.3) with the never-written logEyeDist = 0 (0.3) */
   float alpha_threshold;  /* early ray termination on the sample's src.a (0.95) */
@@ -154,7 +154,11 @@ typedef struct vvlic_params {
   int32_t schedule;       /* VVLIC_SCHEDULE_* (QUEUE) */
   int32_t record_tape;    /* renders record what vvlic_render_adjoint needs (0) */
   int32_t technique;      /* VVLIC_TECHNIQUE_* = the reference's RenderTechnique (RAYCAST) */
-  int32_t reserved[4];
+  int32_t tape_max_samples; /* recording renders: cap on the samples a ray's tape holds
+                               (0 = the longest chord / spacing, which no ray exceeds).  A ray
+                               with more samples than its tape sets VVLIC_CHECK_TAPE_OVERFLOW
+                               and turns the adjoint's gradients to NaN. */
+  int32_t reserved[3];
 } vvlic_params;
 
 /* Render technique, numbered like the reference's RenderTechnique (types.h:63-72):
@@ -198,8 +202,10 @@ typedef struct vvlic_stats {
   uint64_t sample_steps;  /* samples * (L_f + L_b): the throughput unit */
   uint64_t rays;          /* pixels whose ray hit the volume */
   float kernel_ms;        /* device time of the render kernel (CUDA events) */
-  uint32_t check_flags;   /* libraries built with VVLIC_BOUNDS_CHECK: VVLIC_CHECK_* bits of the
-                             out-of-range accesses the render caught (and skipped); else 0 */
+  uint32_t check_flags;   /* VVLIC_CHECK_* bits: libraries built with VVLIC_BOUNDS_CHECK set
+                             those of the out-of-range accesses the render caught (and skipped);
+                             every build sets VVLIC_CHECK_TAPE_OVERFLOW after a recording render
+                             or an adjoint whose tape was too short */
 } vvlic_stats;
 
 /* Index classes of the VVLIC_BOUNDS_CHECK build. */
@@ -208,7 +214,10 @@ enum {
   VVLIC_CHECK_NOISE = 1u << 1,
   VVLIC_CHECK_SCALAR = 1u << 2,
   VVLIC_CHECK_TAPE = 1u << 3,
-  VVLIC_CHECK_IMAGE = 1u << 4
+  VVLIC_CHECK_IMAGE = 1u << 4,
+  /* a ray of the last recording render had more samples than its tape holds
+     (vvlic_params.tape_max_samples): that render's adjoint gradients are NaN */
+  VVLIC_CHECK_TAPE_OVERFLOW = 1u << 5
 };
 
 /* ---- defaults and helpers (no device work) ------------------------------------------- */
@@ -548,7 +557,9 @@ vvlic_status vvlic_noise_gradients_device(const uint8_t* d_noise, int32_t mx, in
  * the process exits); the caller still passes the input and output buffers.
  *   - Runs on the current CUDA device.  The first call on a device looks up that array's
  *     device address (cudaGetSymbolAddress) and caches it; make that first call before any
- *     stream capture.
+ *     stream capture.  The cached address does not survive cudaDeviceReset: do not call this
+ *     entry point on a device after resetting it.  A call whose launch fails forgets the
+ *     address, and the next call looks it up again.
  *   - mx*my*mz above VVLIC_NOALLOC_MAX_VOXELS (or an axis below 2) returns
  *     VVLIC_ERR_INVALID_ARGUMENT without launching anything.
  *   - Every call shares the array and it keeps the last call's contents; calls that overlap on

@@ -6,10 +6,14 @@
 # headers include GL headers by Windows-style names.  The include shim generated below only maps
 # those names (`GL\glew.h` with a backslash, `dataSet.h` vs dataset.h) onto the GLEW header the
 # reference vendors and an empty freeglut header.  Nothing here provides or loads any graphics
-# library.  Usage: sh oracle/build_ref.sh [reference-root]
+# library.  Usage: sh oracle/build_ref.sh <reference-root>   (or $VVLIC_REFERENCE_ROOT)
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
-ROOT=${1:-${VVLIC_REFERENCE_ROOT:-/root/reference}}
+ROOT=${1:-$VVLIC_REFERENCE_ROOT}
+if [ -z "$ROOT" ]; then
+  echo "build_ref: give the reference checkout as the argument or in VVLIC_REFERENCE_ROOT" >&2
+  exit 2
+fi
 SRC="$ROOT/VectorVisualization"
 OUT="$HERE/_ref"
 if [ ! -f "$SRC/gradient.cpp" ]; then

@@ -35,6 +35,11 @@ typedef struct vvo_inputs {
 
 int32_t vvo_abi(void) { return 1; }
 
+void vvo_params_default(vvlic_params* p) { vvo::params_default(*p); }
+void vvo_view_default(vvlic_view* v) { vvo::view_default(*v); }
+void vvo_line_material_default(vvlic_line_material* m) { vvo::line_material_default(*m); }
+int32_t vvo_filter_table(int32_t kind, int32_t width, uint8_t* out) { return vvo::filter_table(kind, width, out); }
+
 void vvo_encode_field(const void* xyz, int32_t dtype, const int32_t n[3], float* out_rgba) {
   int nn[3] = {n[0], n[1], n[2]};
   vvo::encode_field(xyz, dtype, nn, out_rgba);

@@ -79,8 +79,55 @@ def lib() -> C.CDLL:
         l.vvo_max_threads.restype = I
         l.vvo_adjoint.argtypes = [C.POINTER(Inputs), P, P, I, I, P, P, P, P, I]
         l.vvo_adjoint.restype = I
+        l.vvo_params_default.argtypes = [C.POINTER(capi.Params)]
+        l.vvo_view_default.argtypes = [C.POINTER(capi.View)]
+        l.vvo_line_material_default.argtypes = [C.POINTER(capi.LineMaterial)]
+        l.vvo_filter_table.argtypes = [I, I, P]
+        l.vvo_filter_table.restype = I
         _lib = l
     return _lib
+
+
+# ---- defaults and filter tables restated by the oracle (no libvvlic involved) -------------
+def params_default() -> capi.Params:
+    """LICParams() and the reference's fixed shader state (oracle restatement)."""
+    p = capi.Params()
+    lib().vvo_params_default(C.byref(p))
+    return p
+
+
+def view_default() -> capi.View:
+    v = capi.View()
+    lib().vvo_view_default(C.byref(v))
+    return v
+
+
+def line_material_default() -> capi.LineMaterial:
+    m = capi.LineMaterial()
+    lib().vvo_line_material_default(C.byref(m))
+    return m
+
+
+def filter_table(kind, width: int = 256) -> np.ndarray:
+    """Filter-kernel table (uint8) of `kind` ("box", "triangle", "cos2", "gaussian")."""
+    k = capi.FILTER[kind] if isinstance(kind, str) else int(kind)
+    out = np.zeros(1024, np.uint8)
+    w = lib().vvo_filter_table(k, width, out.ctypes.data)
+    if w == 0:
+        raise ValueError(f"oracle filter_table: bad kind {kind!r} or width {width}")
+    return out[:w].copy()
+
+
+class Defaults:
+    """The provider workloads.* take as `defaults=`: inputs of a configuration built by the
+    oracle alone, so a CPU run of the oracle needs no libvvlic."""
+
+    params = staticmethod(params_default)
+    view = staticmethod(view_default)
+    filter_table = staticmethod(filter_table)
+
+
+DEFAULTS = Defaults()
 
 
 def _dims(a: np.ndarray) -> np.ndarray:
@@ -112,7 +159,7 @@ def encode_field_interp(xyz0: np.ndarray, xyz1: np.ndarray, index: int, size: in
 
 def illum_luts(material: "capi.LineMaterial | None" = None) -> np.ndarray:
     """Zoeckler, Mallo diffuse and Mallo specular tables, (3, h, w, 4) uint8."""
-    m = material if material is not None else capi.line_material_default()
+    m = material if material is not None else line_material_default()
     w, h = capi.lut_size(m.width), capi.lut_size(m.height)
     out = np.empty((3, h, w, 4), np.uint8)
     lib().vvo_illum_luts(C.byref(m), w, h, out.ctypes.data)

@@ -10,8 +10,8 @@
  *   - the FP32 OpenMP CPU baseline (Real = float).
  *
  * What it follows (file:line within VectorVisualization/):
- *   GLSL hot path      shader/lic3d_fragment.glsl:5-99, shader/inc_lic.glsl:134-265,
- *                      shader/inc_illum.glsl:1-154 and 257-271, shader/inc_header.glsl:22-63
+ *   GLSL hot path      shader/lic3d_fragment.glsl:5-99, shader/inc_lic.glsl:61-202,
+ *                      shader/inc_illum.glsl:1-172, shader/inc_header.glsl:22-63
  *   other techniques   shader/lic3d_slicing_fragment.glsl, vectorfield_fragment.glsl:39-101,
  *                      lic3d_volume_fragment.glsl, raycast_lic3d_fragment.glsl, slicing.cpp:42-103
  *   uniforms           renderer.cpp:925-996 (setRenderVolParams)
@@ -237,6 +237,10 @@ static inline void noise_gradients(const uint8_t* noise, const int m[3], int mod
       {{{-1, -3, -1}, {-3, -6, -3}, {-1, -3, -1}}, {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, {{1, 3, 1}, {3, 6, 3}, {1, 3, 1}}},
       {{{-1, -3, -1}, {0, 0, 0}, {1, 3, 1}}, {{-3, -6, -3}, {0, 0, 0}, {3, 6, 3}}, {{-1, -3, -1}, {0, 0, 0}, {1, 3, 1}}},
       {{{-1, 0, 1}, {-3, 0, 3}, {-1, 0, 1}}, {{-3, 0, 3}, {-6, 0, 6}, {-3, 0, 3}}, {{-1, 0, 1}, {-3, 0, 3}, {-1, 0, 1}}}};
+  /* slices in parallel: every voxel's sums keep their order, so the result is thread-count free */
+#if defined(_OPENMP)
+#pragma omp parallel for schedule(static)
+#endif
   for (int z = 0; z < nz; ++z)
     for (int y = 0; y < ny; ++y)
       for (int x = 0; x < nx; ++x) {
@@ -273,6 +277,9 @@ static inline void noise_gradients(const uint8_t* noise, const int m[3], int mod
       }
   float w[27];
   noise_gradient_filter_weights(w);
+#if defined(_OPENMP)
+#pragma omp parallel for schedule(static)
+#endif
   for (int z = 0; z < nz; ++z)
     for (int y = 0; y < ny; ++y)
       for (int x = 0; x < nx; ++x) {
@@ -343,7 +350,7 @@ template <class R> static inline R kernel_lookup(const uint8_t* t, int W, R s, i
 }
 
 /* taps[j + L_b] = kernel weight of tap j (j = -L_b..L_f), offsets as accumulated by
- * computeLIC (inc_lic.glsl:219-262): 0.5, then -= 0.5/L_b per backward step, += 0.5/L_f per
+ * computeLIC (inc_lic.glsl:156, 172, 182, 191, 196): 0.5, then -= 0.5/L_b per backward step, += 0.5/L_f per
  * forward step. */
 template <class R> static inline void filter_taps(const uint8_t* t, int W, int clamp_mode, int lb, int lf, R* taps) {
   taps[lb] = kernel_lookup<R>(t, W, R(0.5), clamp_mode);
@@ -690,7 +697,7 @@ template <class R> static inline bool ray_entry(const R o[3], const R d[3], cons
 }
 
 /* ------------------------------------------------------------------------------------- */
-/* LIC: computeLIC / singleLICstep (inc_lic.glsl:134-265)                                  */
+/* LIC: computeLIC / singleLICstep (inc_lic.glsl:93-202)                                    */
 /* ------------------------------------------------------------------------------------- */
 template <class R> struct LicCtx {
   const Inputs* in;
@@ -699,7 +706,7 @@ template <class R> struct LicCtx {
   bool grad;      /* USE_NOISE_GRADIENTS (ILLUM_GRADIENT) */
 };
 
-/* freqSampling (inc_lic.glsl:134-153) / freqSamplingGrad (:124-131) */
+/* freqSampling (inc_lic.glsl:71-90) / freqSamplingGrad (:61-68) */
 template <class R> static inline V4<R> noise_tap(const LicCtx<R>& c, V3<R> p) {
   const Inputs& in = *c.in;
   if (c.grad) {
@@ -725,7 +732,7 @@ template <class R> static inline V3<R> lic_step(const LicCtx<R>& c, V3<R> p, V4<
   const Inputs& in = *c.in;
   R h = c.u->h_eff;
   R sof = c.p->speed_of_flow ? step.w : R(1);
-  V3<R> k1 = slope(step) * dirs * sof * h; /* licdir (inc_lic.glsl:243/257, 172, 177) */
+  V3<R> k1 = slope(step) * dirs * sof * h; /* licdir (inc_lic.glsl:180/194, 109, 114) */
   int integ = c.p->integrator;
   if (integ == VVLIC_EULER) {
     p = p + k1;
@@ -769,7 +776,7 @@ template <class R> static inline V4<R> compute_lic(const LicCtx<R>& c, V3<R> pos
 }
 
 /* ------------------------------------------------------------------------------------- */
-/* shading: illumLIC (inc_illum.glsl:257-271), illumGradient (:100-140)                    */
+/* shading: illumLIC (inc_illum.glsl:158-172), illumGradient (:1-41)                        */
 /* ------------------------------------------------------------------------------------- */
 template <class R> static inline R alpha_correct(R a, R corr) {
   R base = R(1) - a;
@@ -1008,7 +1015,7 @@ template <class R> static inline uint32_t render_pixel(const Inputs& in, const v
   bool outside = false;
   const R thr = R(p.alpha_threshold);
   if (p.technique == VVLIC_TECHNIQUE_VOLUME || p.technique == VVLIC_TECHNIQUE_LICVOLUME) {
-    /* vectorfield_fragment.glsl:67-97 / raycast_lic3d_fragment.glsl:55-89: stop on dest.a */
+    /* vectorfield_fragment.glsl:67-97 / raycast_lic3d_fragment.glsl:35-69: stop on dest.a */
     vvlic_params q = p;
     q.illum = VVLIC_ILLUM_NONE;
     LicCtx<R> cq{&in, &q, &u, false};
@@ -1386,6 +1393,95 @@ template <class R> static inline void render(const Inputs& in, const vvlic_param
     }
   }
   (void)threads;
+}
+
+/* ------------------------------------------------------------------------------------- */
+/* defaults and filter tables, restated independently of the library                      */
+/* ------------------------------------------------------------------------------------- */
+
+/* LICParams() (types.h:91-99) plus the fixed state the reference's shaders run with: the
+ * never-written logEyeDist (factor 0.3, inc_lic.glsl:114), the termination threshold 0.95
+ * (lic3d_fragment.glsl:91), the scalar-gate bounds (inc_lic.glsl:80), GL LIGHT0 as the
+ * application sets it (spot exponent 40, 3DLIC.cpp:736; white diffuse and specular, no
+ * ambient) and every reproduced quirk.  Kernel-selection fields stay 0. */
+static inline void params_default(vvlic_params& p) {
+  std::memset(&p, 0, sizeof p);
+  p.step_size_vol = 1.0f / 128.0f;
+  p.gradient_scale = 30.0f;
+  p.illum_scale = 1.0f;
+  p.freq_scale = 1.0f;
+  p.num_iterations = 255;
+  p.steps_forward = p.steps_backward = 32;
+  p.step_size_lic = 0.01f;
+  p.integrator = VVLIC_HEUN;
+  p.illum = VVLIC_ILLUM_NONE;
+  p.tf_index = VVLIC_TF_INDEX_DIR_Z;
+  p.gate_lo = 0.1f;
+  p.gate_hi = 0.3f;
+  p.eye_dist_factor = 0.3f;
+  p.alpha_threshold = 0.95f;
+  p.quirks = VVLIC_QUIRK_UNIFORM_SCALE_BUG | VVLIC_QUIRK_GRAD_NOISE_NO_FREQ | VVLIC_QUIRK_ZOECKLER_LUMINANCE;
+  const float light[3] = {0.5f, 0.5f, 1.5f};
+  for (int i = 0; i < 3; ++i) {
+    p.light_pos[i] = light[i];
+    p.light_diffuse[i] = p.light_specular[i] = 1.0f;
+    p.light_ambient[i] = 0.0f;
+  }
+  p.spec_exp = 40.0f;
+  p.technique = VVLIC_TECHNIQUE_RAYCAST;
+}
+
+/* Camera() (camera.cpp:42-46): identity rotation, distance 4, fovy 35 degrees; the
+ * orthographic fields default to the +z view of the unit cube. */
+static inline void view_default(vvlic_view& v) {
+  std::memset(&v, 0, sizeof v);
+  v.projection = VVLIC_PERSPECTIVE;
+  v.quat[3] = 1.0f;
+  v.distance = 4.0f;
+  v.fovy_deg = 35.0f;
+  v.ortho_center[0] = v.ortho_center[1] = 0.5f;
+  v.ortho_right[0] = 0.5f;
+  v.ortho_up[1] = 0.5f;
+  v.ortho_dir[2] = 1.0f;
+}
+
+/* LineMat() (illumination.h:42-54) and Illumination() (illumination.cpp:43): white light, ambient 0.1, diffuse
+ * 0.5, specular 0.8, exponents 40 / 2, 256 x 256 tables. */
+static inline void line_material_default(vvlic_line_material& m) {
+  for (int i = 0; i < 4; ++i) {
+    m.light_color[i] = 1.0f;
+    m.ambient[i] = 0.1f;
+    m.diffuse[i] = 0.5f;
+    m.specular[i] = 0.8f;
+  }
+  m.spec_exp = 40.0f;
+  m.diff_exp = 2.0f;
+  m.width = m.height = 256;
+}
+
+/* Filter-kernel table of `width` texels rounded up to a power of two (nextPowerTwo,
+ * dataset.cpp:1407).  Box: LICFilter::createBoxFilter, every texel 255 (dataset.cpp:1405-1413).
+ * The reference loads the other kernels from PNGs it does not ship; their profiles over the
+ * texel centres x_i = (2i + 1) / W - 1 in [-1, 1] (x = tap offset / L) are
+ *   triangle 1 - |x|,  cos^2 cos(pi x / 2)^2,  Gaussian exp(-(x L)^2 / (2 sigma^2)), sigma = L/3,
+ * stored as round(255 v).  Returns the table width, or 0 for a bad kind or width. */
+static inline int filter_table(int kind, int width, uint8_t* out) {
+  if (width < 2 || width > 1024) return 0;
+  int W = 1;
+  while (W < width) W <<= 1;
+  const double pi = 3.14159265358979323846;
+  for (int i = 0; i < W; ++i) {
+    const double x = (double)(2 * i + 1) / (double)W - 1.0;
+    double v;
+    if (kind == VVLIC_FILTER_BOX) v = 1.0;
+    else if (kind == VVLIC_FILTER_TRIANGLE) v = 1.0 - std::fabs(x);
+    else if (kind == VVLIC_FILTER_COS2) { const double c = std::cos(0.5 * pi * x); v = c * c; }
+    else if (kind == VVLIC_FILTER_GAUSSIAN) v = std::exp(-(x * x) * 4.5);  /* (x L)^2 / (2 (L/3)^2) */
+    else return 0;
+    v = std::min(std::max(v, 0.0), 1.0);
+    out[i] = (uint8_t)std::floor(255.0 * v + 0.5);
+  }
+  return W;
 }
 
 }  // namespace vvo

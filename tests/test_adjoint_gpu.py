@@ -188,3 +188,32 @@ def test_tf_fit_reduces_loss(ctx, oracle):
             op.clamp_(0.0, 1.0)
         losses.append(float(loss))
     assert losses[-1] < 0.5 * losses[0], losses
+
+
+def test_tape_overflow_sets_a_status_flag(ctx, oracle):
+    """A recording render whose rays have more samples than their tape holds (capped with
+    params.tape_max_samples) reports VVLIC_CHECK_TAPE_OVERFLOW in the stats; its adjoint's
+    gradients are NaN.  An uncapped recording render clears the flag again."""
+    import torch
+
+    w, taps = case()
+    target = target_image(oracle, w, taps)
+    w.params.tape_max_samples = 4  # rays of this case take about 50 samples
+    vid, img, d_tf, d_op, d_taps = gpu_forward_adjoint(ctx, w, taps, target)
+    st = ctx.stats()
+    assert st.check_flags & capi.CHECK_TAPE_OVERFLOW
+    assert np.isnan(d_tf).all() and np.isnan(d_op).all() and np.isnan(d_taps).all()
+    # the render itself is unaffected by the tape cap
+    p = w.params
+    p.record_tape = 0
+    ctx.set_params(p)
+    plain = torch.empty_like(torch.from_numpy(img)).cuda()
+    ctx.render_device(vid, plain.data_ptr(), w.width, w.height)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(plain.cpu().numpy(), img)
+    assert not ctx.stats().check_flags & capi.CHECK_TAPE_OVERFLOW
+    w.params.tape_max_samples = 0
+    ctx.free_volume(vid)
+    vid, img, d_tf, d_op, d_taps = gpu_forward_adjoint(ctx, w, taps, target)
+    assert not ctx.stats().check_flags & capi.CHECK_TAPE_OVERFLOW
+    assert np.isfinite(d_tf).all() and np.isfinite(d_taps).all()

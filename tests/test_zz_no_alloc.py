@@ -51,14 +51,14 @@ def test_noalloc_rejects_sizes_above_its_maximum(vvlic_lib):
     import torch
 
     lib = vvlic_lib
+    # every axis >= 2, so the voxel-count limit (VVLIC_NOALLOC_MAX_VOXELS = 2^20) is what refuses
+    # them; nothing is launched, so the small buffers are never touched
     d = torch.zeros(16, dtype=torch.uint8, device="cuda")
-    too_big = 1 << 20  # VVLIC_NOALLOC_MAX_VOXELS
-    st = lib.vvlic_noise_gradients_device_noalloc(d.data_ptr(), too_big, 2, 1, capi.NOISE_GRAD_SOBEL, None,
-                                                  d.data_ptr(), None)
-    assert st == capi.ERR_INVALID_ARGUMENT
-    st = lib.vvlic_noise_gradients_device_noalloc(d.data_ptr(), 1025, 1024, 1, capi.NOISE_GRAD_SOBEL, None,
-                                                  d.data_ptr(), None)
-    assert st == capi.ERR_INVALID_ARGUMENT
+    for dims in ((1 << 19, 2, 2), (1024, 513, 2), (129, 128, 64)):
+        assert dims[0] * dims[1] * dims[2] > (1 << 20) and min(dims) >= 2
+        st = lib.vvlic_noise_gradients_device_noalloc(d.data_ptr(), *dims, capi.NOISE_GRAD_SOBEL, None,
+                                                      d.data_ptr(), None)
+        assert st == capi.ERR_INVALID_ARGUMENT, dims
     # the largest accepted size still runs (exactly the maximum number of voxels)
     big = torch.from_numpy(wl.dense_noise((128, 128, 64), seed=33)).cuda()
     out_a = torch.zeros((64, 128, 128, 4), dtype=torch.uint8, device="cuda")
@@ -69,3 +69,24 @@ def test_noalloc_rejects_sizes_above_its_maximum(vvlic_lib):
                                             out_b.data_ptr(), None) == 0
     torch.cuda.synchronize()
     assert torch.equal(out_a, out_b)
+
+
+def test_noalloc_takes_no_device_memory(vvlic_lib):
+    """The call's defining property: device free memory is the same before and after a call at
+    the maximum size (after a first call, which loads the library's module on this device)."""
+    import torch
+
+    lib = vvlic_lib
+    big = torch.from_numpy(wl.dense_noise((128, 128, 64), seed=34)).cuda()
+    out = torch.empty((64, 128, 128, 4), dtype=torch.uint8, device="cuda")
+
+    def call():
+        assert lib.vvlic_noise_gradients_device_noalloc(big.data_ptr(), 128, 128, 64, capi.NOISE_GRAD_SOBEL, None,
+                                                        out.data_ptr(), None) == 0
+        torch.cuda.synchronize()
+
+    call()
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(3):
+        call()
+    assert torch.cuda.mem_get_info()[0] == free0

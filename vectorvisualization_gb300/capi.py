@@ -33,6 +33,7 @@ FILTER = {"box": 0, "triangle": 1, "cos2": 2, "gaussian": 3}
 PERSPECTIVE, ORTHOGRAPHIC = 0, 1
 QUIRK_LUMINANCE_NOISE, QUIRK_UNIFORM_SCALE_BUG, QUIRK_GRAD_NOISE_NO_FREQ, QUIRK_ZOECKLER_LUMINANCE = 1, 2, 4, 8
 QUIRKS_REFERENCE = QUIRK_UNIFORM_SCALE_BUG | QUIRK_GRAD_NOISE_NO_FREQ | QUIRK_ZOECKLER_LUMINANCE
+CHECK_FIELD, CHECK_NOISE, CHECK_SCALAR, CHECK_TAPE, CHECK_IMAGE, CHECK_TAPE_OVERFLOW = 1, 2, 4, 8, 16, 32
 
 _f3 = C.c_float * 3
 
@@ -69,7 +70,8 @@ class Params(C.Structure):
         ("schedule", C.c_int32),
         ("record_tape", C.c_int32),
         ("technique", C.c_int32),
-        ("reserved", C.c_int32 * 4),
+        ("tape_max_samples", C.c_int32),
+        ("reserved", C.c_int32 * 3),
     ]
 
 

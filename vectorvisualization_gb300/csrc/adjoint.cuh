@@ -62,7 +62,7 @@ __device__ __forceinline__ Lut lut(float s) {
   return L;
 }
 
-// Unlit source of one sample from its tape record (illumLIC, inc_illum.glsl:257-271).
+// Unlit source of one sample from its tape record (illumLIC, inc_illum.glsl:158-172).
 struct Src {
   Lut lt, lo;
   float4 tf;

@@ -259,6 +259,7 @@ vvlic_status batch_render(vvlic_ctx* c, const vvlic_job* jobs, int n, cudaStream
   if (e == cudaSuccess) e = cudaEventRecord(c->ev1, s);
   if (e != cudaSuccess) return cuda_fail(c, e, "batch launch");
   c->stats_pending = true;
+  c->tape_flag_pending = false;
   c->last_was_batch = true;
   c->tape_valid = false;
   return VVLIC_OK;

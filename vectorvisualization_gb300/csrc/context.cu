@@ -2,7 +2,7 @@
 //
 // The host side derives everything the reference computes on the CPU per frame
 // (Renderer::setRenderVolParams renderer.cpp:925-996, the view of Camera::setCamera
-// camera.cpp:56-67, the filter-kernel lookups of computeLIC inc_lic.glsl:219-262) and hands it
+// camera.cpp:56-67, the filter-kernel lookups of computeLIC inc_lic.glsl:156, 172, 182, 196) and hands it
 // to the kernels as one by-value argument block.
 #include <cuda_runtime.h>
 
@@ -93,7 +93,7 @@ static void effective_steps(const vvlic_params& p, int* lb, int* lf) {
   *lf = p.low_res ? 15 : p.steps_forward;
 }
 
-// Tap weights w[j], j = -L_b..L_f, at the offsets computeLIC walks (inc_lic.glsl:219-262).
+// Tap weights w[j], j = -L_b..L_f, at the offsets computeLIC walks (inc_lic.glsl:156, 182, 191, 196).
 void derive_taps_from_table(const uint8_t* t, int W, int clamp, bool is_box, int lb, int lf, float* taps,
                             float* inv_area) {
   taps[lb] = (float)kernel_lookup(t, W, 0.5, clamp);
@@ -578,6 +578,9 @@ extern "C" vvlic_status vvlic_upload_field_device(vvlic_ctx* c, const float* d_x
   if (!d_xyz || !vol_id || !valid_dims(n)) return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "upload_field_device: bad arguments");
   if (storage < VVLIC_STORAGE_F32 || storage > VVLIC_STORAGE_UNORM8)
     return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "upload_field_device: storage %d", storage);
+  if (slice_dist)
+    for (int i = 0; i < 3; ++i)
+      if (!(slice_dist[i] > 0.0f)) return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "upload_field_device: slice distance");
   DeviceGuard g(c->device);
   return encode_into_volume(c, d_xyz, VVLIC_DTYPE_FLOAT32, n, slice_dist, storage, (cudaStream_t)stream, vol_id);
 }
@@ -587,7 +590,7 @@ extern "C" vvlic_status vvlic_free_volume(vvlic_ctx* c, int32_t vol_id) {
   auto it = c->vols.find(vol_id);
   if (it == c->vols.end()) return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "free_volume: unknown volume %d", vol_id);
   DeviceGuard g(c->device);
-  cudaStreamSynchronize(c->stream);
+  cudaDeviceSynchronize();  // renders in flight on any stream may read the volume
   free_volume(it->second);
   c->vols.erase(it);
   if (c->tape_vol == vol_id) c->tape_valid = false;  // the tape points at the freed buffers
@@ -672,6 +675,10 @@ extern "C" vvlic_status vvlic_upload_noise(vvlic_ctx* c, const uint8_t* noise, i
     e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return cuda_fail(c, e, "upload_noise");
   } else {
+    // the texture object and texels are destroyed below: wait for renders in flight on any
+    // stream, as the in-place path does
+    e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return cuda_fail(c, e, "upload_noise");
     free_noise(n);
     e = cudaMalloc(&n.d_texels, count * ch);
     if (e != cudaSuccess) return cuda_fail(c, e, "noise allocation");
@@ -707,6 +714,8 @@ extern "C" vvlic_status vvlic_upload_noise_rgba(vvlic_ctx* c, const uint8_t* rgb
   if (mode != VVLIC_NOISE_GRAD_SOBEL && mode != VVLIC_NOISE_GRAD_CENTRAL)
     return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "upload_noise_rgba: mode %d is not a gradient mode", mode);
   DeviceGuard g(c->device);
+  cudaError_t e = cudaDeviceSynchronize();  // renders in flight on any stream read the old noise
+  if (e != cudaSuccess) return cuda_fail(c, e, "upload_noise_rgba");
   free_noise(c->noise);
   c->tape_valid = false;
   NoiseTex& n = c->noise;
@@ -716,7 +725,7 @@ extern "C" vvlic_status vvlic_upload_noise_rgba(vvlic_ctx* c, const uint8_t* rgb
   n.m[2] = mz;
   n.ch = 4;
   n.mode = mode;
-  cudaError_t e = cudaMalloc(&n.d_texels, bytes);
+  e = cudaMalloc(&n.d_texels, bytes);
   if (e != cudaSuccess) return cuda_fail(c, e, "noise allocation");
   e = cudaMemcpyAsync(n.d_texels, rgba, bytes, cudaMemcpyHostToDevice, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);

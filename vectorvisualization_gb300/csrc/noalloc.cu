@@ -36,10 +36,14 @@ float* g_scratch_ptr[kMaxDevices] = {};
 
 // Device address of the scratch array on the current device.  In host code the array's name
 // is only a host-side stand-in for the symbol, so the address is looked up once per device
-// with that device current, and the result is cached.
-vvlic_status scratch_address(float** out) {
+// with that device current, and the result is cached.  The cache belongs to the device's
+// primary context: cudaDeviceReset unloads the module, so a process that resets a device must
+// not call the entry point on it again.  A launch that fails drops the cached address
+// (forget_scratch_address), and the next call looks it up again.
+vvlic_status scratch_address(int* dev_out, float** out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return VVLIC_ERR_NO_DEVICE;
+  *dev_out = dev;
   std::lock_guard<std::mutex> lock(g_setup_mutex);
   if (!g_scratch_ptr[dev]) {
     void* p = nullptr;
@@ -49,6 +53,11 @@ vvlic_status scratch_address(float** out) {
   }
   *out = g_scratch_ptr[dev];
   return VVLIC_OK;
+}
+
+void forget_scratch_address(int dev) {
+  std::lock_guard<std::mutex> lock(g_setup_mutex);
+  g_scratch_ptr[dev] = nullptr;
 }
 
 }  // namespace
@@ -65,11 +74,16 @@ extern "C" vvlic_status vvlic_noise_gradients_device_noalloc(const uint8_t* d_no
   if (slice_dist)
     for (int i = 0; i < 3; ++i) sd[i] = slice_dist[i];
   float* scratch = nullptr;
-  vvlic_status st = scratch_address(&scratch);
+  int dev = 0;
+  vvlic_status st = scratch_address(&dev, &scratch);
   if (st != VVLIC_OK) return st;
   float w27[27];
   vvlic::noise_filter_weights(w27);
   const int m[3] = {mx, my, mz};
   cudaError_t e = vvlic::launch_noise_gradients(d_noise, m, mode, sd, scratch, d_rgba, w27, (cudaStream_t)stream);
-  return e == cudaSuccess ? VVLIC_OK : VVLIC_ERR_CUDA;
+  if (e != cudaSuccess) {
+    forget_scratch_address(dev);
+    return VVLIC_ERR_CUDA;
+  }
+  return VVLIC_OK;
 }

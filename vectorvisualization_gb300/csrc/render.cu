@@ -401,7 +401,8 @@ vvlic_status make_schedule(vvlic_ctx* c, const RenderArgs& a, const Geometry& gm
 vvlic_status prepare_tape(vvlic_ctx* c, const Geometry& gm, int w, int h, RenderArgs& a, cudaStream_t s) {
   const double diag = std::sqrt((double)gm.extent[0] * gm.extent[0] + (double)gm.extent[1] * gm.extent[1] +
                                 (double)gm.extent[2] * gm.extent[2]);
-  const double bound = std::min(diag / a.step_size + 3.0, (double)a.num_iter * (double)a.num_iter);
+  double bound = std::min(diag / a.step_size + 3.0, (double)a.num_iter * (double)a.num_iter);
+  if (c->params.tape_max_samples > 0) bound = std::min(bound, (double)c->params.tape_max_samples);
   const int stride = std::max(1, (int)std::ceil(bound));
   const int nck = (stride + kSegment - 1) / kSegment;
   const size_t rays = (size_t)w * h;
@@ -478,6 +479,7 @@ extern "C" vvlic_status vvlic_render_device(vvlic_ctx* c, int32_t vol_id, float*
     if (e != cudaSuccess) return cuda_fail(c, e, "render launch");
     c->stats_pending = true;
     c->last_was_batch = false;
+    c->tape_flag_pending = false;
     c->stats_steps_per_sample = t.technique == VVLIC_TECHNIQUE_SLICING ? (uint64_t)(a.lb + a.lf) : 0;
     return VVLIC_OK;
   }
@@ -502,6 +504,7 @@ extern "C" vvlic_status vvlic_render_device(vvlic_ctx* c, int32_t vol_id, float*
   c->last_was_batch = false;
   c->stats.sample_steps = 0;
   c->stats_steps_per_sample = (uint64_t)(a.lb + a.lf);
+  c->tape_flag_pending = record;
   if (record) {
     c->tape_valid = true;
     c->tape_vol = vol_id;
@@ -587,6 +590,7 @@ extern "C" vvlic_status vvlic_render_adjoint(vvlic_ctx* c, int32_t vol_id, const
   }
   if (e != cudaSuccess) return cuda_fail(c, e, "render_adjoint launch");
   c->stats_pending = true;
+  c->tape_flag_pending = true;
   return VVLIC_OK;
 }
 
@@ -629,6 +633,13 @@ extern "C" vvlic_status vvlic_get_stats(vvlic_ctx* c, vvlic_stats* out) {
     c->stats.sample_steps = c->last_was_batch ? h[2] : h[0] * c->stats_steps_per_sample;
     c->stats.kernel_ms = ms;
     c->stats.check_flags = (uint32_t)h[3];
+    if (c->tape_flag_pending && c->d_tape_flag) {
+      // rays of the recording render that outgrew their tape (store_pixel counts them)
+      unsigned long long over = 0;
+      e = cudaMemcpy(&over, c->d_tape_flag, sizeof over, cudaMemcpyDeviceToHost);
+      if (e != cudaSuccess) return cuda_fail(c, e, "get_stats");
+      if (over) c->stats.check_flags |= VVLIC_CHECK_TAPE_OVERFLOW;
+    }
     c->stats_pending = false;
   }
   *out = c->stats;

@@ -484,7 +484,7 @@ __device__ __forceinline__ float4 tf_rgba(const float* tab, float s) {
 }
 
 // ------------------------------------------------------------------------------------------
-// LIC: computeLIC / singleLICstep (inc_lic.glsl:157-265)
+// LIC: computeLIC / singleLICstep (inc_lic.glsl:152-202, 93-145)
 // ------------------------------------------------------------------------------------------
 __device__ __forceinline__ float3 slope(float4 f) { return f3(2.0f * f.x - 1.0f, 2.0f * f.y - 1.0f, 2.0f * f.z - 1.0f); }
 // h * slope(f) rounded once: (2f - 1) * h = f * 2h - h, one FMA per component.  It keeps 2h
@@ -517,7 +517,7 @@ __device__ __forceinline__ float3 lic_step(const RenderArgs& a, float3 p, float4
   return p;
 }
 
-// freqSampling / freqSamplingGrad (inc_lic.glsl:124-153)
+// freqSampling / freqSamplingGrad (inc_lic.glsl:71-90, 61-68)
 template <int NL, bool GRAD> __device__ __forceinline__ float4 noise_tap(const RenderArgs& a, float3 p) {
   if (GRAD) return Noise<NL>::template sample<true, true>(a, p);
   if (a.gate) {
@@ -618,7 +618,7 @@ __device__ __forceinline__ void compute_lic2(const RenderArgs& a, float3 pa, flo
 }
 
 // ------------------------------------------------------------------------------------------
-// shading: illumLIC (inc_illum.glsl:257-271) and illumGradient (inc_illum.glsl:100-140)
+// shading: illumLIC (inc_illum.glsl:158-172) and illumGradient (inc_illum.glsl:1-41)
 // ------------------------------------------------------------------------------------------
 __device__ __forceinline__ float alpha_correct(float al, float corr) {
   float base = fmaxf(1.0f - al, 0.0f);

@@ -116,6 +116,7 @@ struct vvlic_ctx {
   void* d_tape = nullptr;
   size_t tape_cap = 0;
   unsigned long long* d_tape_flag = nullptr;  // overflow count of the recording render
+  bool tape_flag_pending = false;  // the next get_stats reads d_tape_flag into check_flags
   long long* d_acc = nullptr;                 // fixed-point gradient accumulators
   bool tape_valid = false;
   int tape_vol = 0, tape_w = 0, tape_h = 0, tape_storage = 0, tape_sampler = 0, tape_integ = 0, tape_illum = 0;

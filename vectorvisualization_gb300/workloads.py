@@ -20,6 +20,20 @@ import numpy as np
 
 from . import capi
 
+
+class LibraryDefaults:
+    """Parameter, view and filter-table defaults of libvvlic (vvlic_params_default,
+    vvlic_view_default, vvlic_make_filter_table).  Every configuration below takes a `defaults`
+    provider with these three callables; another provider (the oracle's own restatement) builds
+    the same configuration without the library."""
+
+    params = staticmethod(capi.params_default)
+    view = staticmethod(capi.view_default)
+    filter_table = staticmethod(capi.make_filter_table)
+
+
+LIBRARY = LibraryDefaults()
+
 _GOLDEN = np.uint64(0x9E3779B97F4A7C15)
 _M1 = np.uint64(0xBF58476D1CE4E5B9)
 _M2 = np.uint64(0x94D049BB133111EB)
@@ -203,8 +217,9 @@ def quat_mul(q, r):
     )
 
 
-def ortho_view(center=(0.5, 0.5, 0.5), right=(0.5, 0.0, 0.0), up=(0.0, 0.5, 0.0), direction=(0.0, 0.0, 1.0)) -> capi.View:
-    v = capi.view_default()
+def ortho_view(center=(0.5, 0.5, 0.5), right=(0.5, 0.0, 0.0), up=(0.0, 0.5, 0.0), direction=(0.0, 0.0, 1.0),
+               defaults=LIBRARY) -> capi.View:
+    v = defaults.view()
     v.projection = capi.ORTHOGRAPHIC
     for i in range(3):
         v.ortho_center[i] = center[i]
@@ -214,8 +229,9 @@ def ortho_view(center=(0.5, 0.5, 0.5), right=(0.5, 0.0, 0.0), up=(0.0, 0.5, 0.0)
     return v
 
 
-def perspective_view(quat=(0.0, 0.0, 0.0, 1.0), distance: float = 4.0, fovy: float = 35.0, pan=(0.0, 0.0, 0.0)) -> capi.View:
-    v = capi.view_default()
+def perspective_view(quat=(0.0, 0.0, 0.0, 1.0), distance: float = 4.0, fovy: float = 35.0, pan=(0.0, 0.0, 0.0),
+                     defaults=LIBRARY) -> capi.View:
+    v = defaults.view()
     v.projection = capi.PERSPECTIVE
     for i in range(4):
         v.quat[i] = quat[i]
@@ -226,15 +242,15 @@ def perspective_view(quat=(0.0, 0.0, 0.0, 1.0), distance: float = 4.0, fovy: flo
     return v
 
 
-def orbit_view(frame: int, frames: int, distance: float = 2.2, tilt: float = 25.0) -> capi.View:
+def orbit_view(frame: int, frames: int, distance: float = 2.2, tilt: float = 25.0, defaults=LIBRARY) -> capi.View:
     q = quat_mul(quat_axis_angle((1, 0, 0), tilt), quat_axis_angle((0, 1, 0), 360.0 * frame / frames))
-    return perspective_view(q, distance)
+    return perspective_view(q, distance, defaults=defaults)
 
 
-def random_view(rng: SplitMix64, distance: float = 2.4) -> capi.View:
+def random_view(rng: SplitMix64, distance: float = 2.4, defaults=LIBRARY) -> capi.View:
     u = rng.uniform(3)
     q = quat_mul(quat_axis_angle((1, 0, 0), 80.0 * (u[0] - 0.5)), quat_axis_angle((0, 1, 0), 360.0 * u[1]))
-    return perspective_view(q, distance * (0.9 + 0.2 * u[2]))
+    return perspective_view(q, distance * (0.9 + 0.2 * u[2]), defaults=defaults)
 
 
 # -------------------------------------------------------------------------------------------
@@ -277,9 +293,9 @@ class Workload:
         }
 
 
-def c1(size: int = 64, image: int = 256) -> Workload:
+def c1(size: int = 64, image: int = 256, defaults=LIBRARY) -> Workload:
     """Plain method, small: the reference's CPU-runnable case."""
-    p = capi.params_default()
+    p = defaults.params()
     p.integrator = capi.EULER
     p.steps_forward = p.steps_backward = 20
     p.step_size_lic = 0.01
@@ -292,26 +308,26 @@ def c1(size: int = 64, image: int = 256) -> Workload:
         field=abc_field(size),
         noise=sparse_noise(size, seed=1),
         noise_mode=capi.NOISE_SCALAR,
-        filter_table=capi.make_filter_table("box", 256),
+        filter_table=defaults.filter_table("box", 256),
         filter_kind="box",
         tf_rgba=rgba,
         tf_opac=op,
         params=p,
-        views=[ortho_view()],
+        views=[ortho_view(defaults=defaults)],
         width=image,
         height=image,
         seeds={"noise": 1},
     )
 
 
-def c2_view() -> capi.View:
+def c2_view(defaults=LIBRARY) -> capi.View:
     q = quat_mul(quat_axis_angle((1, 0, 0), 20.0), quat_axis_angle((0, 1, 0), 30.0))
-    return perspective_view(q, distance=2.3)
+    return perspective_view(q, distance=2.3, defaults=defaults)
 
 
-def c2(size: int = 256, image: int = 1024, storage: str = "f32", lighting: bool = True) -> Workload:
+def c2(size: int = 256, image: int = 1024, storage: str = "f32", lighting: bool = True, defaults=LIBRARY) -> Workload:
     """Mid-size with lighting and precision."""
-    p = capi.params_default()
+    p = defaults.params()
     p.integrator = capi.HEUN
     p.steps_forward = p.steps_backward = 40
     p.step_size_lic = 0.005
@@ -325,12 +341,12 @@ def c2(size: int = 256, image: int = 1024, storage: str = "f32", lighting: bool 
         field=vortex_field(size, seed=2),
         noise=dense_noise(size, seed=20),
         noise_mode=capi.NOISE_GRAD_CENTRAL if lighting else capi.NOISE_SCALAR,
-        filter_table=capi.make_filter_table("gaussian", 256),
+        filter_table=defaults.filter_table("gaussian", 256),
         filter_kind="gaussian",
         tf_rgba=rgba,
         tf_opac=op,
         params=p,
-        views=[c2_view()],
+        views=[c2_view(defaults)],
         width=image,
         height=image,
         storage=storage,
@@ -338,9 +354,9 @@ def c2(size: int = 256, image: int = 1024, storage: str = "f32", lighting: bool 
     )
 
 
-def c4(size: int = 128, image: int = 512, views: int = 4) -> Workload:
+def c4(size: int = 128, image: int = 512, views: int = 4, defaults=LIBRARY) -> Workload:
     """Differentiable TF / filter fit setting (forward part)."""
-    p = capi.params_default()
+    p = defaults.params()
     p.integrator = capi.HEUN
     p.steps_forward = p.steps_backward = 30
     p.step_size_lic = 0.01
@@ -353,12 +369,12 @@ def c4(size: int = 128, image: int = 512, views: int = 4) -> Workload:
         field=vortex_field(size, seed=4),
         noise=dense_noise(size, seed=40),
         noise_mode=capi.NOISE_SCALAR,
-        filter_table=capi.make_filter_table("gaussian", 256),
+        filter_table=defaults.filter_table("gaussian", 256),
         filter_kind="gaussian",
         tf_rgba=rgba,
         tf_opac=op,
         params=p,
-        views=[random_view(rng) for _ in range(views)],
+        views=[random_view(rng, defaults=defaults) for _ in range(views)],
         width=image,
         height=image,
         seeds={"field": 4, "noise": 40, "tf": 404, "views": 44},
@@ -375,7 +391,8 @@ class BatchVolume:
     filter_kind: str
 
 
-def c3(volumes: int = 64, image: int = 512, seed: int = 3, max_views: int = 8, dims=tuple(range(64, 193, 16))):
+def c3(volumes: int = 64, image: int = 512, seed: int = 3, max_views: int = 8, dims=tuple(range(64, 193, 16)),
+       defaults=LIBRARY):
     """Batched uneven volumes: per-axis dims from {64, 80, ..., 192}, each an ABC or a vortex field
     from its own seed, 1..max_views random views at image^2, filters mixed box / triangle / cos^2,
     L in [15, 60].  Returns (volumes, shared noise, base params)."""
@@ -390,10 +407,10 @@ def c3(volumes: int = 64, image: int = 512, seed: int = 3, max_views: int = 8, d
         field = abc_field(n) if kind == "abc" else vortex_field(n, seed=vseed)
         nviews = 1 + min(int(u[4] * max_views), max_views - 1)
         vr = SplitMix64(vseed * 7 + 1)
-        views = [random_view(vr) for _ in range(nviews)]
+        views = [random_view(vr, defaults=defaults) for _ in range(nviews)]
         L = 15 + min(int(u[5] * 46), 45)
         out.append(BatchVolume(field, kind, vseed, views, L, kinds[min(int(u[6] * 3), 2)]))
-    p = capi.params_default()
+    p = defaults.params()
     p.integrator = capi.HEUN
     p.step_size_lic = 0.01
     p.step_size_vol = 1.0 / 128.0
@@ -401,9 +418,10 @@ def c3(volumes: int = 64, image: int = 512, seed: int = 3, max_views: int = 8, d
     return out, dense_noise(128, seed=seed * 10), p
 
 
-def c5(size: int = 512, image: int = 2048, frames: int = 64, device: str | None = None) -> Workload:
-    """Large turbulence orbit."""
-    p = capi.params_default()
+def c5(size: int = 512, image: int = 2048, frames: int = 64, device: str | None = None,
+       defaults=LIBRARY) -> Workload:
+    """Large turbulence orbit (spectral field via torch.fft on `device`, numpy otherwise)."""
+    p = defaults.params()
     p.integrator = capi.RK4
     p.steps_forward = p.steps_backward = 60
     p.step_size_lic = 1.0 / 512.0
@@ -416,12 +434,12 @@ def c5(size: int = 512, image: int = 2048, frames: int = 64, device: str | None 
         field=spectral_field(size, seed=5, device=device),
         noise=dense_noise(size, seed=50),
         noise_mode=capi.NOISE_GRAD_CENTRAL,
-        filter_table=capi.make_filter_table("gaussian", 256),
+        filter_table=defaults.filter_table("gaussian", 256),
         filter_kind="gaussian",
         tf_rgba=rgba,
         tf_opac=op,
         params=p,
-        views=[orbit_view(f, frames) for f in range(frames)],
+        views=[orbit_view(f, frames, defaults=defaults) for f in range(frames)],
         width=image,
         height=image,
         storage="f16",
