@@ -1,18 +1,26 @@
 """Benchmark of the LIC volume ray-cast hot path (one JSON line on stdout).
 
-Workload (default): the mid-size configuration with lighting and precision — a 256^3 field of a
-uniform drift plus 8 seeded Gaussian vortices, dense uint8 noise (frequency 4.0) with
-central-difference gradients, Heun streamlines L = 40 each way at step 0.005, Gaussian filter,
-1024^2 image, ray spacing 1/256, gradient Phong lighting, FP16 field storage (FP32 and BF16 are
-measured alongside).  A step is one frame.
+Headline workload: the large turbulence orbit — a 512^3 FP16 divergence-free spectral field
+(random-phase Fourier modes, E(k) ~ k^-5/3 for k in [2, 64], seed 5), dense uint8 noise with
+central-difference gradients, RK4 streamlines L = 60 each way at step 1/512, Gaussian filter,
+2048^2 image at ray spacing 1/512, gradient Phong lighting, a 64-frame orbit.  A step is one
+frame; K steps render K frames spread evenly over the orbit (all 64 when K = 64).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 `value` is device throughput in Gsample-steps/s (one LIC integration step at one ray sample),
-whole job over all ranks; `e2e` is the same metric through the C ABI with host buffers
-(field + noise upload, preprocessing, render, image download inside the timed region).
+whole job over all ranks (replicas: every rank renders its own share of frames).  `e2e` is the
+same metric through the C ABI with host buffers: every step copies the field and the noise from
+pinned host memory, re-encodes the field, recomputes the noise gradients and layouts, renders
+and downloads the image.  `roofline` compares the kernel's fetch rate with the measured L1TEX
+fetch ceiling of the GPU (vvlic_measure_fetch_ceiling); DRAM figures are reported beside it.
+Extra keys: the mid-size lit frame with FP32/FP16/BF16 storage (`c2`), the 64-volume batch
+(`batch`), the differentiable-fit forward+adjoint (`fwd_adjoint`), the orbit's forward+adjoint
+(`orbit_adjoint`).
+
 `--impl reference` times the CPU restatement of the reference's path (the reference itself is
-GLSL and cannot run without an OpenGL stack) on all host cores.
+GLSL and runs only through OpenGL) on all host cores, on stratified rows of the same orbit
+frames, with inputs built by the oracle alone (libvvlic is not loaded).
 """
 from __future__ import annotations
 
@@ -33,39 +41,42 @@ sys.path.insert(0, ROOT)
 METRIC = "Gsample-steps/s & frames/s, fwd and fwd+adjoint, at RMSE<=1e-3 vs FP64 oracle"
 UNIT = "Gsample-steps/s"
 L2_FLUSH_BYTES = 256 << 20
+ORBIT_FRAMES = 64
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=8)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--storage", default="f16", choices=["f32", "f16", "bf16", "u8"])
     ap.add_argument("--sampler", default="hybrid", choices=["gather", "cell", "texture", "hybrid"])
     ap.add_argument("--schedule", default="queue", choices=["queue", "static"])
-    ap.add_argument("--size", type=int, default=256)
-    ap.add_argument("--image", type=int, default=1024)
+    ap.add_argument("--size", type=int, default=512, help="orbit field size per axis")
+    ap.add_argument("--image", type=int, default=2048, help="orbit image size")
+    ap.add_argument("--c2-size", type=int, default=256)
+    ap.add_argument("--c2-image", type=int, default=1024)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
-    ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--no-c2", action="store_true", help="skip the mid-size lit frame and its storage variants")
+    ap.add_argument("--no-c3", action="store_true", help="skip the 64-volume batch")
+    ap.add_argument("--no-c4", action="store_true", help="skip the differentiable-fit forward+adjoint")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the orbit's forward+adjoint")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--no-adjoint", action="store_true")
-    # the batch (C3) and the large orbit (C5) run by default; --no-c3 / --no-c5 skip them
-    ap.add_argument("--c3", dest="c3", action="store_true")
-    ap.add_argument("--no-c3", dest="c3", action="store_false", help="skip the 64-volume batch")
+    ap.add_argument("--no-ceiling", action="store_true", help="skip the L1TEX fetch-ceiling measurement")
     ap.add_argument("--c3-volumes", type=int, default=64)
-    ap.add_argument("--c5", dest="c5", action="store_true")
-    ap.add_argument("--no-c5", dest="c5", action="store_false", help="skip the 512^3 RK4 lit orbit")
-    ap.add_argument("--c5-frames", type=int, default=2)
-    ap.set_defaults(c3=True, c5=True)
-    ap.add_argument("--c5-size", type=int, default=512)
-    ap.add_argument("--c5-image", type=int, default=2048)
     return ap.parse_args()
 
 
+def orbit_frames(steps: int, world: int, rank: int) -> list[int]:
+    """Frames of the 64-frame orbit that `rank` renders: the steps*world global steps spread
+    evenly over the orbit, dealt round-robin."""
+    total = steps * world
+    return [((k * world + rank) * ORBIT_FRAMES // total) % ORBIT_FRAMES for k in range(steps)]
+
+
 # ---------------------------------------------------------------------------------------------
-# distributed plumbing (one process per GPU; replicas of the same workload, no data exchange)
+# distributed plumbing (one process per GPU; replicas of the workload, no data exchange)
 # ---------------------------------------------------------------------------------------------
 def Dist(init: bool = True):
     from vectorvisualization_gb300.replicas import Replicas
@@ -126,17 +137,24 @@ class Clocks:
 
 
 # ---------------------------------------------------------------------------------------------
+# roofline helpers
+# ---------------------------------------------------------------------------------------------
+FIELD_EVALS = {0: 1, 1: 2, 2: 4}  # field evaluations per streamline step: Euler, Heun, RK4
+GROUP_KEY = {0: "euler", 1: "heun", 2: "rk4"}
+
+
 def bytes_per_texel(storage: str) -> int:
     return 16 if storage == "f32" else 8
 
 
-def algorithmic_bytes(stats, params, storage: str, lit: bool, pixels: int) -> float:
+def cacheless_bytes(sample_steps: float, samples: float, integrator: int, storage: str, lit: bool,
+                    pixels: int) -> float:
     """Cacheless trilinear-gather model: 8*(k*s_F + s_N) per sample-step, 8*s_F per sample for
     the compositing fetch, 16 B per output pixel."""
-    k = {0: 1, 1: 2, 2: 4}[params.integrator]
+    k = FIELD_EVALS[integrator]
     sF = bytes_per_texel(storage)
     sN = 4 if lit else 1
-    return stats.sample_steps * 8 * (k * sF + sN) + stats.samples * 8 * sF + pixels * 16
+    return sample_steps * 8 * (k * sF + sN) + samples * 8 * sF + pixels * 16
 
 
 def load_peaks():
@@ -149,40 +167,83 @@ def load_peaks():
 
 
 def load_traffic(workload_key: str):
+    """DRAM bytes per launch of the workload's render kernel from the committed ncu capture, if
+    that capture was made with the current kernel sources (else None: the figure is stale)."""
+    from vectorvisualization_gb300 import build
+
     p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
     if not os.path.exists(p):
         return None
     with open(p) as fh:
         d = json.load(fh)
     e = d.get(workload_key)
-    return None if e is None else e.get("bytes_per_launch")
+    if e is None or e.get("source_digest") != build.source_digest():
+        return None
+    return e.get("bytes_per_launch")
 
 
-def make_workload(args):
-    from vectorvisualization_gb300 import workloads as wl
+def roofline(steps: float, samples: float, ms: float, integrator: int, storage: str, lit: bool, pixels: int,
+             ceiling: dict | None, traffic_key: str) -> dict:
+    """The render kernel against the L1TEX fetch ceiling (the bound that applies: the field comes
+    through the texture unit, the noise cells through 256-bit loads, and both hit L1 or L2), with
+    DRAM beside it.  A fetch group is one noise-cell load plus the k field fetches of one
+    streamline step; per launch there are samples*(L_b+L_f+1) noise taps = steps + samples."""
+    peak_hbm, peak_kind = load_peaks()
+    secs = ms / 1e3
+    groups = steps + samples
+    k = FIELD_EVALS[integrator]
+    traffic = load_traffic(traffic_key)
+    alg = cacheless_bytes(steps, samples, integrator, storage, lit, pixels)
+    hbm = {"peak_gbs": peak_hbm, "peak_kind": peak_kind,
+           "dram_bytes_per_launch": traffic,
+           "dram_gbs": None if traffic is None else traffic / secs / 1e9,
+           "dram_frac": None if traffic is None else traffic / secs / 1e9 / peak_hbm,
+           "cacheless_model_bytes_per_launch": alg,
+           "cacheless_model_ratio": alg / secs / 1e9 / peak_hbm,
+           "note": "cacheless_model_ratio counts every texel of every trilinear as DRAM bytes; it "
+                   "measures cache reuse, not HBM use"}
+    r = {"bound": "l1tex", "unit": "G fetch-groups/s", "traffic": traffic,
+         "fetch_group": f"one 256-bit noise-cell load + {k} trilinear field fetches (one streamline step)",
+         "per_launch": {"noise_cell_loads": groups, "field_fetches": k * steps + samples, "kernel_ms": ms},
+         "achieved": groups / secs / 1e9, "hbm": hbm}
+    if ceiling:
+        peak = ceiling["group_per_s"][GROUP_KEY[integrator]] / 1e9
+        r.update({"peak": peak, "frac": r["achieved"] / peak, "peak_kind": "measured (vvlic_measure_fetch_ceiling)"})
+    else:
+        r.update({"peak": None, "frac": None, "peak_kind": "not measured"})
+    return r
 
-    return wl.c2(size=args.size, image=args.image, storage=args.storage)
 
-
-def cpu_sample(w, seconds: float, threads: int = 0, rows_offset: int = 0):
-    """FP32 OpenMP CPU restatement on a stratified row subset sized to ~`seconds`."""
+# ---------------------------------------------------------------------------------------------
+# CPU restatement (oracle) on stratified rows
+# ---------------------------------------------------------------------------------------------
+def cpu_scene(w):
+    """Oracle scene of a workload: the field encoded and rounded to its storage by the oracle,
+    the noise gradients computed by the oracle."""
     from oracle import pyoracle
     from vectorvisualization_gb300 import capi
 
-    rgba = pyoracle.round_storage(pyoracle.encode_field(w.field), w.storage)
+    rgba = pyoracle.encode_field(w.field)
+    if w.storage != "f32":
+        rgba = pyoracle.round_storage(rgba, w.storage)
     noise = w.noise if w.noise_mode == capi.NOISE_SCALAR else pyoracle.noise_gradients(w.noise, w.noise_mode)
-    sc = pyoracle.Scene(rgba, noise, w.tf_rgba, w.tf_opac, filter_table=w.filter_table)
+    return pyoracle.Scene(rgba, noise, w.tf_rgba, w.tf_opac, filter_table=w.filter_table)
+
+
+def cpu_sample(sc, w, view, seconds: float, threads: int = 0, rows_offset: int = 0, probe_row=None):
+    """FP32 OpenMP CPU restatement on a stratified row subset sized to ~`seconds`."""
+    from oracle import pyoracle
+
     H = w.height
-    # probe one row, then size the stratified subset
-    probe_row = [H // 2 + rows_offset % max(1, H // 2)]
+    probe = [probe_row if probe_row is not None else H // 2 + rows_offset % max(1, H // 4)]
     t0 = time.perf_counter()
-    _, s = sc.render(w.params, w.views[0], w.width, H, rows=probe_row, precision=32, threads=threads)
+    _, s = sc.render(w.params, view, w.width, H, rows=probe, precision=32, threads=threads)
     dt = max(time.perf_counter() - t0, 1e-3)
     nrows = int(max(1, min(H, seconds / dt)))
     stride = max(1, H // nrows)
-    rows = list(range((rows_offset % stride), H, stride))[:nrows]
+    rows = list(range(rows_offset % stride, H, stride))[:nrows]
     t0 = time.perf_counter()
-    img, smp = sc.render(w.params, w.views[0], w.width, H, rows=rows, precision=32, threads=threads)
+    img, smp = sc.render(w.params, view, w.width, H, rows=rows, precision=32, threads=threads)
     dt = time.perf_counter() - t0
     steps = float(smp.astype(np.float64).sum()) * (w.params.steps_forward + w.params.steps_backward)
     return {"rate": steps / dt / 1e9, "seconds": dt, "rows": rows, "img": img, "sample_steps": steps,
@@ -190,22 +251,30 @@ def cpu_sample(w, seconds: float, threads: int = 0, rows_offset: int = 0):
 
 
 def run_reference(args, dist):
-    """CPU restatement of the reference path, all host threads, bounded sample per step."""
+    """The CPU restatement of the reference path on all host threads, on stratified rows of the
+    same orbit frames as the GPU arm; the workload is built by the oracle (no libvvlic)."""
     if dist.rank != 0:
         return 0
-    w = make_workload(args)
-    per_step = max(1.0, min(args.cpu_seconds, 20.0))
+    from oracle import pyoracle
+    from vectorvisualization_gb300 import workloads as wl
+
+    t0 = time.perf_counter()
+    w = wl.c5(size=args.size, image=args.image, frames=ORBIT_FRAMES, defaults=pyoracle.DEFAULTS)
+    sc = cpu_scene(w)
+    prep_s = time.perf_counter() - t0
+    frames = orbit_frames(args.steps, 1, 0)
+    # the whole run stays within a few minutes: about 120 s of timed CPU work in all
+    per_step = max(1.0, min(args.cpu_seconds, 120.0 / max(1, args.steps)))
     for i in range(args.warmup):
-        cpu_sample(w, per_step / 4, rows_offset=i)
-    rates, secs, steps = [], 0.0, 0.0
+        cpu_sample(sc, w, w.views[frames[i % len(frames)]], per_step / 4, rows_offset=i)
+    secs, steps, rows = 0.0, 0.0, 0
     res = None
-    for i in range(args.steps):
-        res = cpu_sample(w, per_step, rows_offset=i + args.warmup)
-        rates.append(res["rate"])
+    for i, f in enumerate(frames):
+        res = cpu_sample(sc, w, w.views[f], per_step, rows_offset=i + args.warmup)
         secs += res["seconds"]
         steps += res["sample_steps"]
+        rows += len(res["rows"])
     value = steps / secs / 1e9
-    full_frame_steps = None
     line = {
         "impl": "reference",
         "metric": METRIC,
@@ -219,38 +288,92 @@ def run_reference(args, dist):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32",
-        "data": "synthetic (seeded SplitMix64 vortex field and noise)",
-        "config": {**w.describe(), "cpu_rows_per_step": len(res["rows"]) if res else 0},
+        "data": "synthetic (seeded SplitMix64 spectral field and noise; the reference ships no datasets)",
+        "config": {**w.describe(), "frames": frames, "cpu_rows_per_step": rows / max(1, len(frames)),
+                   "input_build_s": prep_s},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": res["threads"] if res else 0, "kind": "port",
-                         "sample": f"{len(res['rows']) if res else 0} stratified rows of the {w.width}x{w.height} "
-                                   f"frame per step (FP32 OpenMP restatement of the GLSL path; the reference "
+                         "sample": f"about {rows // max(1, len(frames))} stratified rows of each {w.width}x{w.height} "
+                                   f"orbit frame per step (FP32 OpenMP restatement of the GLSL path; the reference "
                                    f"itself runs only through OpenGL)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
-    del full_frame_steps
     print(json.dumps(line), flush=True)
     return 0
 
 
-def bench_adjoint(ctx, torch, stream, flush, args):
+# ---------------------------------------------------------------------------------------------
+# sections of the GPU arm
+# ---------------------------------------------------------------------------------------------
+def timed(torch, stream, flush, fn) -> float:
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        flush.zero_()
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def bench_c2(ctx, torch, stream, flush, args, ceiling):
+    """C2: 256^3 drift + 8 vortices, dense noise (freq 4) with central-difference gradients, Heun
+    L = 40 at 0.005, Gaussian filter, 1024^2, spacing 1/256, gradient lighting; f16 field, with
+    the f32 and bf16 storage of the same frame beside it."""
+    from vectorvisualization_gb300 import capi, workloads as wl
+
+    w = wl.c2(size=args.c2_size, image=args.c2_image, storage="f16")
+    vid = wl.setup_context(ctx, w)
+    p = w.params
+    p.sampler = capi.SAMPLER[args.sampler]
+    p.schedule = capi.SCHEDULE[args.schedule]
+    ctx.set_params(p)
+    W, H = w.width, w.height
+    out = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+    sh = stream.cuda_stream
+    frame = lambda v: ctx.render_device(v, out.data_ptr(), W, H, None, sh)  # noqa: E731
+    for _ in range(2):
+        timed(torch, stream, flush, lambda: frame(vid))
+    n = max(3, min(args.steps, 10))
+    ms = [timed(torch, stream, flush, lambda: frame(vid)) for _ in range(n)]
+    st = ctx.stats()
+    mean = sum(ms) / len(ms)
+    res = {"workload": w.name, "frames": n, "ms_per_frame": mean, "gss": st.sample_steps / (mean / 1e3) / 1e9,
+           "sample_steps_per_frame": int(st.sample_steps), "samples_per_frame": int(st.samples),
+           "image_alpha_mean": float(out[..., 3].mean()),
+           "roofline": roofline(st.sample_steps, st.samples, mean, p.integrator, "f16", True, W * H, ceiling,
+                                f"c2/f16/{args.sampler}/{args.c2_size}/{args.c2_image}")}
+    variants = {"f16": {"gss": res["gss"], "ms": mean}}
+    for storage in ("f32", "bf16"):
+        vid2 = ctx.upload_field(w.field, storage=storage)
+        timed(torch, stream, flush, lambda: frame(vid2))
+        ms2 = timed(torch, stream, flush, lambda: frame(vid2))
+        s2 = ctx.stats()
+        variants[storage] = {"gss": s2.sample_steps / (ms2 / 1e3) / 1e9, "ms": ms2}
+        ctx.free_volume(vid2)
+    variants["bf16"]["note"] = ("bf16 texels via their f16 texture copy: the texture and hybrid samplers read a "
+                                "half4 texture, so this is the f16 kernel on bf16-valued data")
+    res["storage_variants"] = variants
+    ctx.free_volume(vid)
+    return res
+
+
+def bench_c4(ctx, torch, stream, flush, args):
     """C4: 128^3 vortex field, dense noise, Heun L=30 (61 taps), 512^2 x 4 views, L2 loss to a
     target rendered from a hidden seeded TF; gradients w.r.t. TF (256x4), opacity (256) and the
     61 taps.  Times the plain forward, the recording forward and the adjoint per view."""
     from vectorvisualization_gb300 import capi, workloads as wl
 
     w = wl.c4()
-    w.storage = args.storage
+    w.storage = "f16"
     vid = wl.setup_context(ctx, w)
     L = w.params.steps_forward
-    taps, inv_area = ctx.filter_taps()
     W, H = w.width, w.height
     p = w.params
     p.sampler = capi.SAMPLER[args.sampler]
     p.schedule = capi.SCHEDULE[args.schedule]
     sh = stream.cuda_stream
     img = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
-    # the hidden target: the same views rendered with another seeded TF
-    ctx.set_tf(*wl.random_tf(seed=4040))
+    ctx.set_tf(*wl.random_tf(seed=4040))  # the hidden target TF
     ctx.set_params(p)
     targets = []
     for v in w.views:
@@ -263,38 +386,25 @@ def bench_adjoint(ctx, torch, stream, flush, args):
     d_op = torch.empty(256, dtype=torch.float32, device="cuda")
     d_taps = torch.empty(2 * L + 1, dtype=torch.float32, device="cuda")
     g = torch.empty_like(img)
-
-    def timed(fn):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        with torch.cuda.stream(stream):
-            flush.zero_()
-            e0.record(stream)
-            fn()
-            e1.record(stream)
-        torch.cuda.synchronize()
-        return e0.elapsed_time(e1)
-
     fwd_ms, rec_ms, adj_ms, steps = 0.0, 0.0, 0.0, 0
-    for rep in range(2):  # first pass warms up
+    for rep in range(2):  # the first pass warms up
         f_ms = r_ms = a_ms = 0.0
         for v, tgt in zip(w.views, targets):
             ctx.set_view(v)
             p.record_tape = 0
             ctx.set_params(p)
-            f_ms += timed(lambda: ctx.render_device(vid, img.data_ptr(), W, H, None, sh))
+            f_ms += timed(torch, stream, flush, lambda: ctx.render_device(vid, img.data_ptr(), W, H, None, sh))
             steps_v = ctx.stats().sample_steps
             p.record_tape = 1
             ctx.set_params(p)
-            r_ms += timed(lambda: ctx.render_device(vid, img.data_ptr(), W, H, None, sh))
+            r_ms += timed(torch, stream, flush, lambda: ctx.render_device(vid, img.data_ptr(), W, H, None, sh))
             torch.mul(img - tgt, 2.0, out=g)
-
-            def adj():
-                ctx.render_adjoint(vid, g.data_ptr(), W, H, d_tf.data_ptr(), d_op.data_ptr(), d_taps.data_ptr(), sh)
-
-            a_ms += timed(adj)
+            a_ms += timed(torch, stream, flush, lambda: ctx.render_adjoint(
+                vid, g.data_ptr(), W, H, d_tf.data_ptr(), d_op.data_ptr(), d_taps.data_ptr(), sh))
             if rep == 1:
                 steps += steps_v
         fwd_ms, rec_ms, adj_ms = f_ms, r_ms, a_ms
+    flags = ctx.stats().check_flags
     p.record_tape = 0
     ctx.set_params(p)
     ctx.free_volume(vid)
@@ -305,173 +415,81 @@ def bench_adjoint(ctx, torch, stream, flush, args):
         "fwd_plus_adjoint_over_fwd": (rec_ms + adj_ms) / fwd_ms,
         "gss_fwd": steps / (fwd_ms / 1e3) / 1e9,
         "gss_fwd_adjoint": steps / ((rec_ms + adj_ms) / 1e3) / 1e9,
+        "tape_overflow": bool(flags & capi.CHECK_TAPE_OVERFLOW),
         "grad_norms": {"tf": float(d_tf.norm()), "opacity": float(d_op.norm()), "taps": float(d_taps.norm())},
     }
 
 
-def bench_batch(ctx, torch, stream, flush, args):
+def bench_batch(ctx, torch, stream, flush, args, dist):
     """C3: 64 volumes with per-axis dims from {64, 80, ..., 192} (ABC or vortex, own seeds), 1-8
     random views each at 512^2, filters mixed box / triangle / cos^2, L in [15, 60], FP16
-    storage, Heun; one persistent launch per batch, replayed from a CUDA graph."""
+    storage, Heun; one persistent launch per batch, replayed from a CUDA graph.  Under N ranks
+    every rank renders its cost-balanced share of the jobs (replicas, no exchange)."""
     from vectorvisualization_gb300 import capi, workloads as wl
+    from vectorvisualization_gb300.replicas import shard_by_cost
 
     t0 = time.perf_counter()
     vols, noise, base = wl.c3(volumes=args.c3_volumes)
     gen_s = time.perf_counter() - t0
+    specs = [(bv, v) for bv in vols for v in bv.views]
+    # cost estimate per job: pixels x taps (the chord length is similar across the random views)
+    mine = shard_by_cost([512 * 512 * (2 * bv.L + 1) for bv, _ in specs], dist.rank, dist.world)
     ctx.upload_noise(noise)
     ctx.set_tf(*wl.default_tf())
-    jobs, outs = [], []
-    voxels = 0
-    for bv in vols:
-        vid = ctx.upload_field(bv.field, storage=args.storage)
-        voxels += bv.field.shape[0] * bv.field.shape[1] * bv.field.shape[2]
-        table = capi.make_filter_table(bv.filter_kind, 256)
-        for v in bv.views:
+
+    def make_jobs(c, storage, sampler, outs):
+        vids, jobs = {}, []
+        for k, i in enumerate(mine):
+            bv, v = specs[i]
+            if id(bv) not in vids:
+                vids[id(bv)] = c.upload_field(bv.field, storage=storage)
             p = capi.Params.from_buffer_copy(base)
             p.steps_forward = p.steps_backward = bv.L
-            p.sampler = capi.SAMPLER[args.sampler]
-            out = torch.empty((512, 512, 4), dtype=torch.float32, device="cuda")
-            outs.append(out)
-            jobs.append(capi.make_job(vid, out.data_ptr(), 512, 512, v, p, table))
+            p.sampler = capi.SAMPLER[sampler]
+            jobs.append(capi.make_job(vids[id(bv)], outs[k].data_ptr(), 512, 512, v, p,
+                                      capi.make_filter_table(bv.filter_kind, 256)))
+        return jobs, vids
+
+    outs = [torch.empty((512, 512, 4), dtype=torch.float32, device="cuda") for _ in mine]
+    jobs, vids = make_jobs(ctx, "f16", args.sampler, outs)
+    voxels = sum(int(np.prod(bv.field.shape[:3])) for bv in vols if id(bv) in vids)
     sh = stream.cuda_stream
     tw, smp, tune_ms = ctx.batch_autotune(jobs, sh)
     ctx.batch_render(jobs, sh)  # capture with the tuned shape
     stream.synchronize()
-    times = []
-    for _ in range(2):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        with torch.cuda.stream(stream):
-            flush.zero_()
-            e0.record(stream)
-            ctx.batch_render(jobs, sh)
-            e1.record(stream)
-        torch.cuda.synchronize()
-        times.append(e0.elapsed_time(e1))
+    dist.barrier()
+    ms = min(timed(torch, stream, flush, lambda: ctx.batch_render(jobs, sh)) for _ in range(2))
     st = ctx.stats()
-    ms = min(times)
-    # cacheless model for the unlit Heun batch: 8 (2 s_F + 1) B per sample-step
-    sF = bytes_per_texel(args.storage)
-    alg = st.sample_steps * 8 * (2 * sF + 1) + st.samples * 8 * sF + len(jobs) * 512 * 512 * 16
-    peak, peak_kind = load_peaks()
-    achieved = alg / (ms / 1e3) / 1e9
-    # the plain FP32 form: the same jobs from FP32 texels with the gather sampler, one launch
-    plain_ms = None
-    with capi.Context(torch.cuda.current_device()) as pctx:
-        pctx.upload_noise(noise)
-        pctx.set_tf(*wl.default_tf())
-        pjobs = []
-        k = 0
-        for bv in vols:
-            pvid = pctx.upload_field(bv.field, storage="f32")
-            table = capi.make_filter_table(bv.filter_kind, 256)
-            for v in bv.views:
-                p = capi.Params.from_buffer_copy(base)
-                p.steps_forward = p.steps_backward = bv.L
-                p.sampler = capi.SAMPLER["gather"]
-                pjobs.append(capi.make_job(pvid, outs[k].data_ptr(), 512, 512, v, p, table))
-                k += 1
-        pctx.batch_render(pjobs, sh)
-        stream.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        with torch.cuda.stream(stream):
-            flush.zero_()
-            e0.record(stream)
-            pctx.batch_render(pjobs, sh)
-            e1.record(stream)
-        torch.cuda.synchronize()
-        plain_ms = e0.elapsed_time(e1)
-    return {
-        "workload": f"C3 {len(vols)} volumes (dims 64..192 per axis), {len(jobs)} views at 512^2, L 15..60, "
-                    f"mixed box/triangle/cos2, {args.storage}",
-        "jobs": len(jobs), "voxels": voxels, "ms_per_batch": ms, "frames_per_s": len(jobs) / (ms / 1e3),
-        "gss": st.sample_steps / (ms / 1e3) / 1e9, "sample_steps": int(st.sample_steps),
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_kind": peak_kind, "algorithmic_bytes_per_batch": alg},
-        "plain_f32_gather_ms": plain_ms, "speedup_vs_plain_f32": plain_ms / ms,
+    ms_all = dist.max(ms)
+    steps_all = dist.sum(float(st.sample_steps))
+    jobs_all = int(dist.sum(float(len(jobs))))
+    res = {
+        "workload": f"C3 {len(vols)} volumes (dims 64..192 per axis), {len(specs)} views at 512^2, L 15..60, "
+                    f"mixed box/triangle/cos2, f16",
+        "jobs": jobs_all, "jobs_this_rank": len(jobs), "voxels_this_rank": voxels, "ms_per_batch": ms_all,
+        "frames_per_s": jobs_all / (ms_all / 1e3), "gss": steps_all / (ms_all / 1e3) / 1e9,
+        "sample_steps": int(steps_all), "sharding": f"shard_by_cost over {dist.world} rank(s)",
         "autotune": {"tile": f"{tw}x{32 // tw}", "sampler": [k for k, v in capi.SAMPLER.items() if v == smp][0],
                      "best_ms": tune_ms},
         "cuda_graph": True, "generation_s": gen_s,
     }
+    # the plain FP32 form: the same jobs from FP32 texels with the gather sampler, one launch
+    with capi.Context(torch.cuda.current_device()) as pctx:
+        pctx.upload_noise(noise)
+        pctx.set_tf(*wl.default_tf())
+        pjobs, _ = make_jobs(pctx, "f32", "gather", outs)
+        pctx.batch_render(pjobs, sh)
+        stream.synchronize()
+        plain_ms = timed(torch, stream, flush, lambda: pctx.batch_render(pjobs, sh))
+    res["plain_f32_gather_ms"] = dist.max(plain_ms)
+    res["speedup_vs_plain_f32"] = res["plain_f32_gather_ms"] / ms_all
+    return res
 
 
-def bench_orbit(ctx, torch, stream, flush, args, dist):
-    """C5: 512^3 FP16 solenoidal spectral field, dense gradient noise, RK4 L=60, step 1/512,
-    2048^2, gradient lighting; `--c5-frames` frames of the 64-frame orbit per GPU (frames dealt
-    round-robin over the ranks, each holding its own copy of the inputs), one launch each, L2
-    flushed between frames (the 1.5 GiB field + noise working set exceeds L2 anyway)."""
+def bench_orbit_adjoint(ctx, torch, stream, flush, w, vid, out, frame):
+    """Forward (recording) + adjoint of one lit orbit frame: L2 loss to the same frame rendered
+    with another transfer function; gradients for the TF, opacity and 121 taps."""
     from vectorvisualization_gb300 import capi, workloads as wl
-
-    t0 = time.perf_counter()
-    w = wl.c5(size=args.c5_size, image=args.c5_image, frames=64, device="cuda")
-    gen_s = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    vid = wl.setup_context(ctx, w)
-    p = w.params
-    p.sampler = capi.SAMPLER[args.sampler]
-    p.schedule = capi.SCHEDULE[args.schedule]
-    ctx.set_params(p)
-    setup_s = time.perf_counter() - t0
-    W, H = w.width, w.height
-    out = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
-    sh = stream.cuda_stream
-    per_rank = max(1, min(args.c5_frames, 64 // dist.world))
-    mine = dist.shard(per_rank * dist.world)
-    frames = len(mine)
-    with torch.cuda.stream(stream):
-        ctx.render_device(vid, out.data_ptr(), W, H, None, sh)  # warm-up (cell layouts, tables)
-    stream.synchronize()
-    ms, steps, samples = [], 0, 0
-    clocks = Clocks(torch.cuda.current_device())
-    clocks.start()
-    dist.barrier()
-    for f in mine:
-        ctx.set_view(w.views[f])
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        with torch.cuda.stream(stream):
-            flush.zero_()
-            e0.record(stream)
-            ctx.render_device(vid, out.data_ptr(), W, H, None, sh)
-            e1.record(stream)
-        torch.cuda.synchronize()
-        ms.append(e0.elapsed_time(e1))
-        st = ctx.stats()
-        steps += int(st.sample_steps)
-        samples += int(st.samples)
-    clk = clocks.stop()
-    adjoint = None
-    if not args.no_adjoint:
-        adjoint = orbit_adjoint(ctx, torch, stream, flush, w, vid, out, mine[0])
-    total_ms = dist.max(sum(ms))
-    steps, samples = dist.sum(float(steps)), dist.sum(float(samples))
-    frames = per_rank * dist.world
-    peak, peak_kind = load_peaks()
-
-    class _S:
-        pass
-
-    agg = _S()
-    agg.sample_steps, agg.samples = steps, samples
-    alg = algorithmic_bytes(agg, p, w.storage, True, W * H * frames)
-    achieved = alg / (total_ms / 1e3) / 1e9 / dist.world  # per GPU, against one GPU's peak
-    key = f"c5/{w.storage}/{args.sampler}/{args.c5_size}/{args.c5_image}"
-    traffic = load_traffic(key)
-    return {
-        "workload": w.name, "frames": frames, "ms_per_frame": total_ms / frames,
-        "frames_per_s": frames / (total_ms / 1e3), "gss": steps / (total_ms / 1e3) / 1e9,
-        "sample_steps_per_frame": steps / frames, "samples_per_frame": samples / frames,
-        "sampler": args.sampler, "storage": w.storage,
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "peak_kind": peak_kind, "algorithmic_bytes_per_frame": alg / frames},
-        "clocks": clk, "generation_s": gen_s, "setup_s": setup_s,
-        "image_alpha_mean": float(out[..., 3].mean()),
-        "fwd_adjoint": adjoint,
-    }
-
-
-def orbit_adjoint(ctx, torch, stream, flush, w, vid, out, frame):
-    """Forward (recording) + adjoint of one lit C5 frame: L2 loss to the same frame rendered with
-    another transfer function; gradients for the TF, opacity and 121 taps."""
-    from vectorvisualization_gb300 import workloads as wl
 
     W, H = w.width, w.height
     sh = stream.cuda_stream
@@ -487,33 +505,24 @@ def orbit_adjoint(ctx, torch, stream, flush, w, vid, out, frame):
     d_op = torch.empty(256, dtype=torch.float32, device="cuda")
     d_taps = torch.empty(ntaps, dtype=torch.float32, device="cuda")
     g = torch.empty_like(out)
-
-    def timed(fn):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        with torch.cuda.stream(stream):
-            flush.zero_()
-            e0.record(stream)
-            fn()
-            e1.record(stream)
-        torch.cuda.synchronize()
-        return e0.elapsed_time(e1)
-
     p.record_tape = 0
     ctx.set_params(p)
-    fwd_ms = timed(lambda: ctx.render_device(vid, out.data_ptr(), W, H, None, sh))
+    fwd_ms = timed(torch, stream, flush, lambda: ctx.render_device(vid, out.data_ptr(), W, H, None, sh))
     steps = ctx.stats().sample_steps
     p.record_tape = 1
     ctx.set_params(p)
-    rec_ms = timed(lambda: ctx.render_device(vid, out.data_ptr(), W, H, None, sh))
+    rec_ms = timed(torch, stream, flush, lambda: ctx.render_device(vid, out.data_ptr(), W, H, None, sh))
     with torch.cuda.stream(stream):
         torch.mul(out - target, 2.0, out=g)
-    adj_ms = timed(lambda: ctx.render_adjoint(vid, g.data_ptr(), W, H, d_tf.data_ptr(), d_op.data_ptr(),
-                                              d_taps.data_ptr(), sh))
+    adj_ms = timed(torch, stream, flush, lambda: ctx.render_adjoint(
+        vid, g.data_ptr(), W, H, d_tf.data_ptr(), d_op.data_ptr(), d_taps.data_ptr(), sh))
+    flags = ctx.stats().check_flags
     p.record_tape = 0
     ctx.set_params(p)
     return {"frame": frame, "fwd_ms": fwd_ms, "fwd_recording_ms": rec_ms, "adjoint_ms": adj_ms,
             "fwd_plus_adjoint_over_fwd": (rec_ms + adj_ms) / fwd_ms,
             "gss_fwd": steps / (fwd_ms / 1e3) / 1e9, "gss_fwd_adjoint": steps / ((rec_ms + adj_ms) / 1e3) / 1e9,
+            "tape_overflow": bool(flags & capi.CHECK_TAPE_OVERFLOW),
             "finite": bool(torch.isfinite(d_tf).all() and torch.isfinite(d_taps).all()),
             "grad_norms": {"tf": float(d_tf.norm()), "opacity": float(d_op.norm()), "taps": float(d_taps.norm())}}
 
@@ -526,65 +535,74 @@ def run_ours(args, dist):
     build.build()
     dev = dist.local
     torch.cuda.set_device(dev)
-    w = make_workload(args)
-    lit = w.params.illum == capi.ILLUM_GRADIENT
+    ceiling = None if args.no_ceiling else capi.measure_fetch_ceiling(dev, 1)
+
+    t0 = time.perf_counter()
+    w = wl.c5(size=args.size, image=args.image, frames=ORBIT_FRAMES, device="cuda")
+    gen_s = time.perf_counter() - t0
     ctx = capi.Context(dev)
+    t0 = time.perf_counter()
     vid = wl.setup_context(ctx, w)
     p = w.params
     p.sampler = capi.SAMPLER[args.sampler]
     p.schedule = capi.SCHEDULE[args.schedule]
     ctx.set_params(p)
+    setup_s = time.perf_counter() - t0
     stream = torch.cuda.Stream(device=dev)
     sh = stream.cuda_stream
     W, H = w.width, w.height
     out = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    frames = orbit_frames(args.steps, dist.world, dist.rank)
 
-    def frame():
+    def frame(f):
+        ctx.set_view(w.views[f])
         ctx.render_device(vid, out.data_ptr(), W, H, None, sh)
 
-    with torch.cuda.stream(stream):
-        for _ in range(args.warmup):
-            frame()
-    stream.synchronize()
-    st0 = ctx.stats()
+    for i in range(args.warmup):
+        timed(torch, stream, flush, lambda: frame(frames[i % len(frames)]))
 
+    # timed region: K frames, each bracketed by events on the render stream, L2 flushed between
     clocks = Clocks(dev)
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    starts = [torch.cuda.Event(enable_timing=True) for _ in frames]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in frames]
+    steps_f, samples_f = [], []
     dist.barrier()
     torch.cuda.synchronize()
     clocks.start()
     t_wall0 = time.perf_counter()
-    with torch.cuda.stream(stream):
-        for k in range(args.steps):
-            flush.zero_()  # L2 flush between frames, outside the event pair
+    for k, f in enumerate(frames):
+        ctx.set_view(w.views[f])
+        with torch.cuda.stream(stream):
+            flush.zero_()
             starts[k].record(stream)
-            frame()
+            ctx.render_device(vid, out.data_ptr(), W, H, None, sh)
             ends[k].record(stream)
+        st = ctx.stats()  # waits for this frame; counts of its samples
+        steps_f.append(int(st.sample_steps))
+        samples_f.append(int(st.samples))
     torch.cuda.synchronize()
     t_wall = time.perf_counter() - t_wall0
     dist.barrier()
     clk = clocks.stop()
     times = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    st = ctx.stats()
-    assert st.sample_steps == st0.sample_steps
     kernel_ms = sum(times)
-    steps_rank = st.sample_steps * args.steps
-    total_steps = dist.sum(float(steps_rank))
     max_ms = dist.max(kernel_ms)
+    total_steps = dist.sum(float(sum(steps_f)))
+    total_samples = dist.sum(float(sum(samples_f)))
     value = total_steps / (max_ms / 1e3) / 1e9
     ms_per_step = max_ms / args.steps
-
-    peak, peak_kind = load_peaks()
-    alg = algorithmic_bytes(st, p, w.storage, lit, W * H)
-    achieved = alg / (ms_per_step / 1e3) / 1e9
-    key = f"c2/{w.storage}/{args.sampler}/{args.size}/{args.image}"
-    traffic = load_traffic(key)
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": traffic, "peak_kind": peak_kind,
-                "algorithmic_bytes_per_launch": alg,
-                "model": "8*(k*s_F+s_N) B per sample-step + 8*s_F per sample + 16 B per pixel"}
+    roof = roofline(sum(steps_f), sum(samples_f), kernel_ms, p.integrator, w.storage, True, W * H * len(frames),
+                    ceiling, f"c5/{w.storage}/{args.sampler}/{args.size}/{args.image}")
+    # per launch figures (the roofline's traffic is per launch)
+    roof["per_launch"] = {kk: v / len(frames) for kk, v in roof["per_launch"].items()}
+    if roof["traffic"] is not None:
+        roof["hbm"]["dram_gbs"] = roof["traffic"] / (kernel_ms / len(frames) / 1e3) / 1e9
+        roof["hbm"]["dram_frac"] = roof["hbm"]["dram_gbs"] / roof["hbm"]["peak_gbs"]
+    roof["hbm"]["cacheless_model_bytes_per_launch"] /= len(frames)
+    if ceiling:
+        roof["ceiling"] = {"tex_per_s": ceiling["tex_per_s"], "ld256_per_s": ceiling["ld256_per_s"],
+                           "group_per_s": ceiling["group_per_s"], "spread_texels": ceiling["spread_texels"]}
 
     line = {
         "metric": METRIC,
@@ -594,116 +612,100 @@ def run_ours(args, dist):
         "steps": args.steps,
         "warmup": args.warmup,
         "ms_per_step": ms_per_step,
-        "frames_per_s": 1e3 / ms_per_step * dist.world,
+        "frames_per_s": len(frames) * dist.world / (max_ms / 1e3),
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32",
-        "data": "synthetic (seeded SplitMix64 vortex field and noise; the reference ships no datasets)",
-        "config": {**w.describe(), "sampler": args.sampler, "schedule": args.schedule,
-                   "l2": "flushed between frames (256 MiB write); inputs > L2",
-                   "sample_steps_per_frame": int(st.sample_steps), "samples_per_frame": int(st.samples),
-                   "rays": int(st.rays), "parallelism": f"replicas x{dist.world}"},
+        "data": "synthetic (seeded SplitMix64 spectral field and noise; the reference ships no datasets)",
+        "config": {**w.describe(), "sampler": args.sampler, "schedule": args.schedule, "frames": frames,
+                   "l2": "inputs > L2 (1 GiB field texture, 4.3 GB noise cells); L2 also flushed between frames "
+                         "(256 MiB write)",
+                   "sample_steps_per_frame": sum(steps_f) / len(frames),
+                   "samples_per_frame": sum(samples_f) / len(frames),
+                   "parallelism": f"replicas x{dist.world}", "generation_s": gen_s, "setup_s": setup_s},
         "wall_ms_per_step": t_wall / args.steps * 1e3,
         "image_alpha_mean": float(out[..., 3].mean()),
-        "roofline": roofline,
+        "roofline": roof,
         # per frame: the queue schedule's tile order (cost, bucket scan, scatter) + the ray-cast
         "gpu_launches": args.steps * (4 if args.schedule == "queue" else 1),
         "clocks": clk,
     }
+    del total_samples
 
-    # reduced / full precision storage alongside (same frame, same sampler)
-    if not args.no_variants and dist.rank == 0:
-        variants = {}
-        for storage in ("f32", "f16", "bf16"):
-            if storage == w.storage:
-                variants[storage] = {"gss": value / dist.world, "ms": ms_per_step}
-                continue
-            vid2 = ctx.upload_field(w.field, storage=storage)
-            with torch.cuda.stream(stream):
-                frame2 = lambda: ctx.render_device(vid2, out.data_ptr(), W, H, None, sh)  # noqa: E731
-                frame2()
-                stream.synchronize()
-                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                flush.zero_()
-                e0.record(stream)
-                frame2()
-                e1.record(stream)
-            torch.cuda.synchronize()
-            ms = e0.elapsed_time(e1)
-            s2 = ctx.stats()
-            variants[storage] = {"gss": s2.sample_steps / (ms / 1e3) / 1e9, "ms": ms}
-            ctx.free_volume(vid2)
-        line["storage_variants"] = variants
-
-    # forward + adjoint on the differentiable-fit configuration (unlit; 4 views)
-    if not args.no_adjoint and dist.rank == 0:
-        with capi.Context(dev) as actx:
-            line["fwd_adjoint"] = bench_adjoint(actx, torch, stream, flush, args)
-    if args.c3 and dist.rank == 0:
-        with capi.Context(dev) as bctx:
-            line["batch"] = bench_batch(bctx, torch, stream, flush, args)
-    if args.c5:
-        with capi.Context(dev) as octx:
-            orbit = bench_orbit(octx, torch, stream, flush, args, dist)
-        if dist.rank == 0:
-            line["orbit"] = orbit
-
-    # end to end through the C ABI with host buffers
+    # end to end through the C ABI with host buffers (every step: field + noise from pinned host
+    # memory, encode, noise gradients, layout rebuilds, render, image download)
     if not args.no_e2e:
+        lib = capi.load()
         field_h = torch.from_numpy(np.ascontiguousarray(w.field)).pin_memory()
         noise_h = torch.from_numpy(np.ascontiguousarray(w.noise)).pin_memory()
         img_h = torch.empty((H, W, 4), dtype=torch.float32).pin_memory()
-        lib = capi.load()
         nz, ny, nx = w.field.shape[:3]
         mz, my, mx = w.noise.shape
-        e2e_steps = max(1, min(args.steps, 3))
-        e2e_vid = None
 
-        def e2e_step():
-            # the animation path (a new field and noise every frame): the first step creates the
-            # volume, later steps rewrite it in place (vvlic_update_field; the same-shape noise
-            # upload is in place too); every step copies both from pinned host memory, encodes,
-            # recomputes the noise gradients and cell / texture layouts, renders and downloads
-            nonlocal e2e_vid
-            if e2e_vid is None:
-                v = capi._I(0)
-                ctx._check(lib.vvlic_upload_field(ctx.h, field_h.data_ptr(), capi.DTYPE_FLOAT32, nx, ny, nz, None,
-                                                  capi.STORAGE[w.storage], capi.C.byref(v)), "upload_field")
-                e2e_vid = v.value
-            else:
-                ctx._check(lib.vvlic_update_field(ctx.h, e2e_vid, field_h.data_ptr(), capi.DTYPE_FLOAT32, nx, ny, nz),
-                           "update_field")
+        def e2e_step(f):
+            ctx._check(lib.vvlic_update_field(ctx.h, vid, field_h.data_ptr(), capi.DTYPE_FLOAT32, nx, ny, nz),
+                       "update_field")
             ctx._check(lib.vvlic_upload_noise(ctx.h, noise_h.data_ptr(), mx, my, mz, w.noise_mode), "upload_noise")
-            ctx._check(lib.vvlic_render(ctx.h, e2e_vid, img_h.data_ptr(), W, H), "render")
+            ctx.set_view(w.views[f])
+            ctx._check(lib.vvlic_render(ctx.h, vid, img_h.data_ptr(), W, H), "render")
 
-        e2e_step()
+        e2e_step(frames[0])
         dist.barrier()
+        torch.cuda.synchronize()
         t0 = time.perf_counter()
-        for _ in range(e2e_steps):
-            e2e_step()
-        t = time.perf_counter() - t0
-        t = dist.max(t)
-        s3 = ctx.stats()
-        line["e2e"] = {"value": dist.sum(float(s3.sample_steps * e2e_steps)) / t / 1e9, "unit": UNIT,
+        for f in frames:
+            e2e_step(f)
+        torch.cuda.synchronize()
+        t = dist.max(time.perf_counter() - t0)
+        last = ctx.stats()
+        line["e2e"] = {"value": total_steps / t / 1e9, "unit": UNIT,
                        "h2d_bytes_per_step": int(field_h.numel() * 4 + noise_h.numel()),
                        "d2h_bytes_per_step": int(img_h.numel() * 4),
-                       "ms_per_step": t / e2e_steps * 1e3,
+                       "ms_per_step": t / args.steps * 1e3,
+                       "same_sample_steps_as_device_timed": int(last.sample_steps) == steps_f[-1],
                        "includes": "field upload+encode (in place), noise upload+gradients, cell and texture "
-                                   "layout rebuilds, render, image download"}
-        ctx.free_volume(e2e_vid)
+                                   "layout rebuilds, view, render, image download; the same frames as the "
+                                   "device-timed steps"}
 
-    # CPU baseline (rank 0, N=1 only): the FP32 OpenMP restatement on a bounded sample
+    if not args.no_adjoint and dist.rank == 0:
+        line["orbit_adjoint"] = bench_orbit_adjoint(ctx, torch, stream, flush, w, vid, out, frames[0])
+
+    # CPU baseline (rank 0, N=1 only): the FP32 OpenMP restatement on a bounded row sample of
+    # the last timed frame, compared with the GPU's rows of that frame
     if not args.no_cpu and dist.rank == 0 and dist.world == 1:
-        res = cpu_sample(w, args.cpu_seconds)
-        gpu_rows = out.cpu().numpy()[res["rows"]]
+        ctx.set_view(w.views[frames[-1]])
+        ctx.render_device(vid, out.data_ptr(), W, H, None, sh)
+        stream.synchronize()
+        gpu_img = out.cpu().numpy()
+        t0 = time.perf_counter()
+        sc = cpu_scene(w)
+        prep_s = time.perf_counter() - t0
+        res = cpu_sample(sc, w, w.views[frames[-1]], args.cpu_seconds)
+        gpu_rows = gpu_img[res["rows"]]
         line["cpu_baseline"] = {
             "value": res["rate"], "unit": UNIT, "cores": res["threads"], "kind": "port",
-            "sample": f"{len(res['rows'])} stratified rows of the {W}x{H} frame ({res['seconds']:.1f} s, "
-                      f"FP32 OpenMP restatement of the reference GLSL path)",
+            "sample": f"{len(res['rows'])} stratified rows of orbit frame {frames[-1]} ({W}x{H}; "
+                      f"{res['seconds']:.1f} s; FP32 OpenMP restatement of the reference GLSL path)",
             "rmse_gpu_vs_cpu_rows": float(np.sqrt(np.mean((gpu_rows.astype(np.float64) - res["img"]) ** 2))),
+            "input_build_s": prep_s,
         }
+        del sc
+    ctx.free_volume(vid)
     ctx.close()
+    del w
+
+    if not args.no_c2 and dist.rank == 0:
+        with capi.Context(dev) as c2ctx:
+            line["c2"] = bench_c2(c2ctx, torch, stream, flush, args, ceiling)
+    if not args.no_c4 and dist.rank == 0:
+        with capi.Context(dev) as actx:
+            line["fwd_adjoint"] = bench_c4(actx, torch, stream, flush, args)
+    if not args.no_c3:
+        with capi.Context(dev) as bctx:
+            batch = bench_batch(bctx, torch, stream, flush, args, dist)
+        if dist.rank == 0:
+            line["batch"] = batch
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
     return 0

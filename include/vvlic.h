@@ -544,6 +544,27 @@ vvlic_status vvlic_noise_gradients_device(const uint8_t* d_noise, int32_t mx, in
                                           int32_t mz, int32_t mode, const float* slice_dist,
                                           uint8_t* d_rgba, void* stream);
 
+/* ---- diagnostics (no reference counterpart) ------------------------------------------- */
+
+/* Measured L1TEX fetch ceiling of one GPU (vvlic_measure_fetch_ceiling). */
+typedef struct vvlic_fetch_ceiling {
+  double tex_per_s;       /* tex3D<float4> trilinear fetches per second from an L1-resident half4 texture */
+  double ld256_per_s;     /* 256-bit ld.global.nc loads per second that hit L1 */
+  double group_per_s[3];  /* groups of k fetches + one 256-bit load per second, k = 1, 2, 4: the
+                             fetches of one Euler, Heun and RK4 streamline step of the HYBRID
+                             sampler (field through the texture unit, one noise cell load) */
+  float ms[5];            /* best kernel time of each measurement (tex, ld256, k = 1, 2, 4) */
+  int32_t num_sms;
+  int32_t spread4;        /* lane spacing of the 8x4 lane tile the kernels use, in quarter texels */
+} vvlic_fetch_ceiling;
+
+/* Times five small kernels on `device` (about 50 ms in all; allocates and frees ~50 KB) whose
+ * warps fetch like the ray-cast kernels' warps — an 8x4 lane tile `spread4` quarter texels
+ * apart, advancing about a quarter texel per iteration — from data that stays in L1.  The
+ * rates are the ceiling the render kernels' fetch rate is compared with (their DRAM traffic is
+ * a few percent of HBM bandwidth, so HBM does not bound them). */
+vvlic_status vvlic_measure_fetch_ceiling(int32_t device, int32_t spread4, vvlic_fetch_ceiling* out);
+
 /* Largest noise (voxels) vvlic_noise_gradients_device_noalloc accepts: its fixed 12 MiB
  * gradient scratch holds three floats per voxel. */
 #define VVLIC_NOALLOC_MAX_VOXELS (1u << 20)

@@ -1364,8 +1364,12 @@ template <class R> static inline void adjoint(const Inputs& in, const vvlic_para
 #pragma omp for schedule(dynamic, 1)
 #endif
     for (int py = 0; py < H; ++py)
-      for (int px = 0; px < W; ++px)
-        adjoint_pixel<R>(in, p, u, rc, px, py, g_img + 4 * ((size_t)py * W + px), mine);
+      for (int px = 0; px < W; ++px) {
+        const float* g = g_img + 4 * ((size_t)py * W + px);
+        /* a zero cotangent contributes exactly zero: rows outside a checked subset cost nothing */
+        if (g[0] == 0.0f && g[1] == 0.0f && g[2] == 0.0f && g[3] == 0.0f) continue;
+        adjoint_pixel<R>(in, p, u, rc, px, py, g, mine);
+      }
   }
   for (int t = 0; t < nt; ++t) {
     const double* b = acc.data() + (size_t)t * (1024 + 256 + ntaps);

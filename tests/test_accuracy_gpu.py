@@ -6,8 +6,8 @@ Two oracle references per storage:
   * "same"  — the oracle reads the field rounded to the same storage precision (FP16 is what the
               reference itself stores, dataset.cpp:326-331), isolating the kernel's arithmetic;
   * "exact" — the oracle reads the unrounded FP32 encoding (the storage error included).
-Bar: RMSE <= 1e-3.  The TEXTURE sampler (hardware trilinear with 8-bit fractional weights) is
-measured and reported; it must stay within 1e-2.
+Bar: RMSE <= 1e-3 for every storage x sampler, against both references (the TEXTURE and
+HYBRID samplers' hardware trilinear with 8-bit fractional weights included).
 Run with -s to print the table.
 """
 import json
@@ -35,7 +35,7 @@ def c2_full(oracle):
     refs = {}
     for st in ("f32", "f16", "bf16", "u8"):
         rgba = enc if st == "f32" else oracle.round_storage(enc, st)
-        sc = oracle.Scene(rgba, noise_rgba, w.tf_rgba, w.tf_opac, filter_table=w.filter_table)
+        sc = oracle.Scene(rgba, noise_rgba, w.tf_rgba, w.tf_opac, filter_table=oracle.filter_table(w.filter_kind, 256))
         refs[st] = sc.render(w.params, w.views[0], w.width, w.height, rows=ROWS)[0]
     return w, refs
 
@@ -65,9 +65,6 @@ def test_accuracy_table(ctx, c2_full):
         with open(out, "w") as fh:
             json.dump({"workload": w.describe(), "rows": ROWS, "errors": table}, fh, indent=1)
     for key, e in table.items():
-        st, sm = key.split("/")
-        if sm in ("texture", "hybrid"):
-            assert e["rmse_same_storage"] <= 1e-2, (key, e)
-        else:
-            assert e["rmse_same_storage"] <= 1e-3, (key, e)
-        assert e["rmse_exact_field"] <= 1e-2, (key, e)
+        assert e["rmse_same_storage"] <= 1e-3, (key, e)
+        assert e["rmse_exact_field"] <= 1e-3, (key, e)
+        assert e["maxabs_same_storage"] <= 0.25, (key, e)

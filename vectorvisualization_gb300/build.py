@@ -48,8 +48,7 @@ def _cxx() -> str:
     raise RuntimeError("no C++ compiler found")
 
 
-def _digest(extra: str) -> str:
-    h = hashlib.sha256(extra.encode())
+def _hash_sources(h):
     for d in (CSRC, INCLUDE):
         for f in sorted(os.listdir(d)):
             p = os.path.join(d, f)
@@ -57,7 +56,17 @@ def _digest(extra: str) -> str:
                 h.update(f.encode())
                 with open(p, "rb") as fh:
                     h.update(fh.read())
-    return h.hexdigest()
+    return h
+
+
+def _digest(extra: str) -> str:
+    return _hash_sources(hashlib.sha256(extra.encode())).hexdigest()
+
+
+def source_digest() -> str:
+    """Digest of the kernel and ABI sources alone (no flags, no machine): identifies the code a
+    profile was captured with, so a committed measurement can be matched to the current build."""
+    return _hash_sources(hashlib.sha256()).hexdigest()[:16]
 
 
 def build(force: bool = False, verbose: bool = False, jobs: int | None = None, extra: list[str] | None = None,

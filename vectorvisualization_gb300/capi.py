@@ -147,6 +147,17 @@ class Stats(C.Structure):
     ]
 
 
+class FetchCeiling(C.Structure):
+    _fields_ = [
+        ("tex_per_s", C.c_double),
+        ("ld256_per_s", C.c_double),
+        ("group_per_s", C.c_double * 3),
+        ("ms", C.c_float * 5),
+        ("num_sms", C.c_int32),
+        ("spread4", C.c_int32),
+    ]
+
+
 _P = C.c_void_p
 _I = C.c_int32
 _SIGS = {
@@ -207,6 +218,7 @@ _SIGS = {
     "vvlic_noise_gradients_device_noalloc": (_I, [_P, _I, _I, _I, _I, _P, _P, _P]),
     "vvlic_download_field": (_I, [_P, _I, _P, C.c_uint64]),
     "vvlic_download_noise": (_I, [_P, _P, C.c_uint64]),
+    "vvlic_measure_fetch_ceiling": (_I, [_I, _I, C.POINTER(FetchCeiling)]),
 }
 
 _lib = None
@@ -583,6 +595,17 @@ class Context:
         s = Stats()
         self._check(self._lib.vvlic_get_stats(self.h, C.byref(s)), "get_stats")
         return s
+
+
+def measure_fetch_ceiling(device: int = 0, spread4: int = 1) -> dict:
+    """vvlic_measure_fetch_ceiling as a dict of rates (per second)."""
+    f = FetchCeiling()
+    st = load().vvlic_measure_fetch_ceiling(device, spread4, C.byref(f))
+    if st:
+        raise VVLICError(st, "measure_fetch_ceiling")
+    return {"tex_per_s": f.tex_per_s, "ld256_per_s": f.ld256_per_s,
+            "group_per_s": {"euler": f.group_per_s[0], "heun": f.group_per_s[1], "rk4": f.group_per_s[2]},
+            "ms": list(f.ms), "num_sms": f.num_sms, "spread_texels": f.spread4 / 4.0}
 
 
 def noise_gradients_device(d_noise: int, dims, mode: int, d_rgba: int, slice_dist=None, stream: int = 0):
