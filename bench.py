@@ -57,7 +57,6 @@ def parse():
     ap.add_argument("--c2-size", type=int, default=256)
     ap.add_argument("--c2-image", type=int, default=1024)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
-    ap.add_argument("--no-c2", action="store_true", help="skip the mid-size lit frame and its storage variants")
     ap.add_argument("--no-c3", action="store_true", help="skip the 64-volume batch")
     ap.add_argument("--no-c4", action="store_true", help="skip the differentiable-fit forward+adjoint")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the orbit's forward+adjoint")
@@ -65,6 +64,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-ceiling", action="store_true", help="skip the L1TEX fetch-ceiling measurement")
     ap.add_argument("--c3-volumes", type=int, default=64)
+    ap.add_argument("--only", default="all", choices=["all", "c5", "c2", "c3", "c4"],
+                    help="run one section alone (profiling); its results are the only keys printed")
     return ap.parse_args()
 
 
@@ -230,24 +231,27 @@ def cpu_scene(w):
     return pyoracle.Scene(rgba, noise, w.tf_rgba, w.tf_opac, filter_table=w.filter_table)
 
 
-def cpu_sample(sc, w, view, seconds: float, threads: int = 0, rows_offset: int = 0, probe_row=None):
-    """FP32 OpenMP CPU restatement on a stratified row subset sized to ~`seconds`."""
+def cpu_sample(sc, w, view, seconds: float, threads: int = 0, rows_offset: int = 0, row_seconds=None):
+    """FP32 OpenMP CPU restatement on about `seconds` of stratified rows: evenly spaced over the
+    whole frame (the k-th of n rows at (k + f) H / n, f shifted per call by the golden ratio), so
+    that dense centre rows and sparse edge rows enter in their proportion.  `row_seconds` is the
+    time of one central row (measured here when not given)."""
     from oracle import pyoracle
 
     H = w.height
-    probe = [probe_row if probe_row is not None else H // 2 + rows_offset % max(1, H // 4)]
-    t0 = time.perf_counter()
-    _, s = sc.render(w.params, view, w.width, H, rows=probe, precision=32, threads=threads)
-    dt = max(time.perf_counter() - t0, 1e-3)
-    nrows = int(max(1, min(H, seconds / dt)))
-    stride = max(1, H // nrows)
-    rows = list(range(rows_offset % stride, H, stride))[:nrows]
+    if row_seconds is None:
+        t0 = time.perf_counter()
+        sc.render(w.params, view, w.width, H, rows=[H // 2], precision=32, threads=threads)
+        row_seconds = max(time.perf_counter() - t0, 1e-3)
+    nrows = int(max(1, min(H, seconds / row_seconds)))
+    f = (0.5 + 0.6180339887 * rows_offset) % 1.0
+    rows = sorted({min(H - 1, int((k + f) * H / nrows)) for k in range(nrows)})
     t0 = time.perf_counter()
     img, smp = sc.render(w.params, view, w.width, H, rows=rows, precision=32, threads=threads)
     dt = time.perf_counter() - t0
     steps = float(smp.astype(np.float64).sum()) * (w.params.steps_forward + w.params.steps_backward)
     return {"rate": steps / dt / 1e9, "seconds": dt, "rows": rows, "img": img, "sample_steps": steps,
-            "threads": pyoracle.max_threads() if threads <= 0 else threads}
+            "row_seconds": row_seconds, "threads": pyoracle.max_threads() if threads <= 0 else threads}
 
 
 def run_reference(args, dist):
@@ -265,12 +269,14 @@ def run_reference(args, dist):
     frames = orbit_frames(args.steps, 1, 0)
     # the whole run stays within a few minutes: about 120 s of timed CPU work in all
     per_step = max(1.0, min(args.cpu_seconds, 120.0 / max(1, args.steps)))
+    row_s = None
     for i in range(args.warmup):
-        cpu_sample(sc, w, w.views[frames[i % len(frames)]], per_step / 4, rows_offset=i)
+        row_s = cpu_sample(sc, w, w.views[frames[i % len(frames)]], per_step / 4, rows_offset=i,
+                           row_seconds=row_s)["row_seconds"]
     secs, steps, rows = 0.0, 0.0, 0
     res = None
     for i, f in enumerate(frames):
-        res = cpu_sample(sc, w, w.views[f], per_step, rows_offset=i + args.warmup)
+        res = cpu_sample(sc, w, w.views[f], per_step, rows_offset=i + args.warmup, row_seconds=row_s)
         secs += res["seconds"]
         steps += res["sample_steps"]
         rows += len(res["rows"])
@@ -431,9 +437,8 @@ def bench_batch(ctx, torch, stream, flush, args, dist):
     t0 = time.perf_counter()
     vols, noise, base = wl.c3(volumes=args.c3_volumes)
     gen_s = time.perf_counter() - t0
-    specs = [(bv, v) for bv in vols for v in bv.views]
-    # cost estimate per job: pixels x taps (the chord length is similar across the random views)
-    mine = shard_by_cost([512 * 512 * (2 * bv.L + 1) for bv, _ in specs], dist.rank, dist.world)
+    specs, costs = wl.c3_jobs(vols)
+    mine = shard_by_cost(costs, dist.rank, dist.world)
     ctx.upload_noise(noise)
     ctx.set_tf(*wl.default_tf())
 
@@ -530,12 +535,36 @@ def bench_orbit_adjoint(ctx, torch, stream, flush, w, vid, out, frame):
 def run_ours(args, dist):
     import torch
 
-    from vectorvisualization_gb300 import build, capi, workloads as wl
+    from vectorvisualization_gb300 import build, capi
 
     build.build()
     dev = dist.local
     torch.cuda.set_device(dev)
     ceiling = None if args.no_ceiling else capi.measure_fetch_ceiling(dev, 1)
+    stream = torch.cuda.Stream(device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    line = headline(args, dist, torch, stream, flush, ceiling) if args.only in ("all", "c5") else {}
+    if args.only in ("all", "c2") and dist.rank == 0:
+        with capi.Context(dev) as c2ctx:
+            line["c2"] = bench_c2(c2ctx, torch, stream, flush, args, ceiling)
+    if args.only in ("all", "c4") and not args.no_c4 and dist.rank == 0:
+        with capi.Context(dev) as actx:
+            line["fwd_adjoint"] = bench_c4(actx, torch, stream, flush, args)
+    if args.only in ("all", "c3") and not args.no_c3:
+        with capi.Context(dev) as bctx:
+            batch = bench_batch(bctx, torch, stream, flush, args, dist)
+        if dist.rank == 0:
+            line["batch"] = batch
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def headline(args, dist, torch, stream, flush, ceiling) -> dict:
+    """The orbit frames: device-timed steps, e2e steps, the orbit's adjoint, the CPU baseline."""
+    from vectorvisualization_gb300 import capi, workloads as wl
+
+    dev = dist.local
 
     t0 = time.perf_counter()
     w = wl.c5(size=args.size, image=args.image, frames=ORBIT_FRAMES, device="cuda")
@@ -548,11 +577,9 @@ def run_ours(args, dist):
     p.schedule = capi.SCHEDULE[args.schedule]
     ctx.set_params(p)
     setup_s = time.perf_counter() - t0
-    stream = torch.cuda.Stream(device=dev)
     sh = stream.cuda_stream
     W, H = w.width, w.height
     out = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
-    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
     frames = orbit_frames(args.steps, dist.world, dist.rank)
 
     def frame(f):
@@ -693,22 +720,7 @@ def run_ours(args, dist):
         del sc
     ctx.free_volume(vid)
     ctx.close()
-    del w
-
-    if not args.no_c2 and dist.rank == 0:
-        with capi.Context(dev) as c2ctx:
-            line["c2"] = bench_c2(c2ctx, torch, stream, flush, args, ceiling)
-    if not args.no_c4 and dist.rank == 0:
-        with capi.Context(dev) as actx:
-            line["fwd_adjoint"] = bench_c4(actx, torch, stream, flush, args)
-    if not args.no_c3:
-        with capi.Context(dev) as bctx:
-            batch = bench_batch(bctx, torch, stream, flush, args, dist)
-        if dist.rank == 0:
-            line["batch"] = batch
-    if dist.rank == 0:
-        print(json.dumps(line), flush=True)
-    return 0
+    return line
 
 
 def main():

@@ -1360,11 +1360,14 @@ template <class R> static inline void adjoint(const Inputs& in, const vvlic_para
 #endif
     double* base = acc.data() + (size_t)tid * (1024 + 256 + ntaps);
     AdjointOut mine{base, base + 1024, base + 1280};
+    const int kChunk = 16;  /* runs of pixels: a few nonzero rows still occupy every core */
+    const int per_row = (W + kChunk - 1) / kChunk;
 #if defined(_OPENMP)
 #pragma omp for schedule(dynamic, 1)
 #endif
-    for (int py = 0; py < H; ++py)
-      for (int px = 0; px < W; ++px) {
+    for (long long t = 0; t < (long long)H * per_row; ++t)
+      for (int py = (int)(t / per_row), px = (int)(t % per_row) * kChunk, pe = std::min(W, px + kChunk); px < pe;
+           ++px) {
         const float* g = g_img + 4 * ((size_t)py * W + px);
         /* a zero cotangent contributes exactly zero: rows outside a checked subset cost nothing */
         if (g[0] == 0.0f && g[1] == 0.0f && g[2] == 0.0f && g[3] == 0.0f) continue;
@@ -1385,13 +1388,18 @@ template <class R> static inline void render(const Inputs& in, const vvlic_param
                                              int threads, const double* slicing = nullptr) {
   Uniforms<R> u = uniforms<R>(in, p);
   int nr = rows ? nrows : H;
+  /* threads take runs of kChunk pixels, so that a few rows still occupy every core */
+  const int kChunk = 16;
+  const int per_row = (W + kChunk - 1) / kChunk;
+  const long long items = (long long)nr * per_row;
 #if defined(_OPENMP)
   if (threads > 0) omp_set_num_threads(threads);
 #pragma omp parallel for schedule(dynamic, 1)
 #endif
-  for (int r = 0; r < nr; ++r) {
-    int py = rows ? rows[r] : r;
-    for (int px = 0; px < W; ++px) {
+  for (long long t = 0; t < items; ++t) {
+    const int r = (int)(t / per_row), x0 = (int)(t % per_row) * kChunk;
+    const int py = rows ? rows[r] : r;
+    for (int px = x0; px < std::min(W, x0 + kChunk); ++px) {
       uint32_t s = render_pixel<R>(in, p, u, rc, px, py, out + 4 * ((size_t)r * W + px), slicing);
       if (samples) samples[(size_t)r * W + px] = s;
     }

@@ -86,3 +86,60 @@ def test_two_gloo_ranks_render_the_orbit_like_one_process(tmp_path):
     for r in range(world):
         n, total, slowest = open(tmp_path / f"rank{r}.txt").read().split()
         assert int(n) == 3 and float(total) == steps and float(slowest) == world
+
+
+def _batch():
+    from oracle import pyoracle
+    from vectorvisualization_gb300 import workloads as wl
+
+    vols, noise, base = wl.c3(volumes=5, max_views=3, dims=(8, 12, 16), defaults=pyoracle.DEFAULTS)
+    specs, costs = wl.c3_jobs(vols, image=8)
+    return vols, noise, base, specs, costs
+
+
+def _render_job(spec, noise, base):
+    from oracle import pyoracle
+    from vectorvisualization_gb300 import capi, workloads as wl
+
+    bv, v = spec
+    p = capi.Params.from_buffer_copy(base)
+    p.steps_forward = p.steps_backward = max(2, bv.L // 10)
+    rgba, op = wl.default_tf()
+    sc = pyoracle.Scene(pyoracle.round_storage(pyoracle.encode_field(bv.field), "f16"), noise, rgba, op,
+                        filter_table=pyoracle.filter_table(bv.filter_kind, 8))
+    return sc.render(p, v, 8, 8, threads=1)[0]
+
+
+def _batch_rank_main(rank, world, port, out_dir):
+    os.environ.update(RANK=str(rank), WORLD_SIZE=str(world), LOCAL_RANK=str(rank), MASTER_ADDR="127.0.0.1",
+                      MASTER_PORT=str(port))
+    from vectorvisualization_gb300.replicas import Replicas
+
+    rep = Replicas(backend="gloo")
+    vols, noise, base, specs, costs = _batch()
+    mine = shard_by_cost(costs, rep.rank, rep.world)
+    for i in mine:
+        np.save(os.path.join(out_dir, f"job{i}_rank{rank}.npy"), _render_job(specs[i], noise, base))
+    total = rep.sum(float(len(mine)))
+    with open(os.path.join(out_dir, f"batch_rank{rank}.txt"), "w") as fh:
+        fh.write(f"{len(mine)} {total}\n")
+    rep.close()
+
+
+def test_two_gloo_ranks_split_the_batch_like_one_process(tmp_path):
+    """The batch dealt by cost over two ranks: every job rendered by exactly one rank, the union
+    equal to the single-process batch."""
+    import torch.multiprocessing as mp
+
+    world = 2
+    mp.start_processes(_batch_rank_main, args=(world, _free_port(), str(tmp_path)), nprocs=world,
+                       start_method="spawn")
+    vols, noise, base, specs, costs = _batch()
+    assert len(specs) >= 4
+    for i, spec in enumerate(specs):
+        owners = [r for r in range(world) if (tmp_path / f"job{i}_rank{r}.npy").exists()]
+        assert len(owners) == 1, (i, owners)
+        np.testing.assert_array_equal(np.load(tmp_path / f"job{i}_rank{owners[0]}.npy"),
+                                      _render_job(spec, noise, base))
+    counts = [open(tmp_path / f"batch_rank{r}.txt").read().split() for r in range(world)]
+    assert sum(int(c[0]) for c in counts) == len(specs) and all(float(c[1]) == len(specs) for c in counts)

@@ -396,12 +396,17 @@ vvlic_status make_schedule(vvlic_ctx* c, const RenderArgs& a, const Geometry& gm
   return VVLIC_OK;
 }
 
-// Tape buffers for a recording render: per ray `stride` samples (the longest chord / spacing,
-// capped by the two loop bounds) and a checkpoint every kSegment samples.
-vvlic_status prepare_tape(vvlic_ctx* c, const Geometry& gm, int w, int h, RenderArgs& a, cudaStream_t s) {
-  const double diag = std::sqrt((double)gm.extent[0] * gm.extent[0] + (double)gm.extent[1] * gm.extent[1] +
-                                (double)gm.extent[2] * gm.extent[2]);
-  double bound = std::min(diag / a.step_size + 3.0, (double)a.num_iter * (double)a.num_iter);
+// Tape buffers for a recording render: per ray `stride` samples (the longest march / spacing,
+// capped by the two loop bounds) and a checkpoint every kSegment samples.  A ray marches in
+// texture space through [0, tex_max] by step_size * |normalize(d) * scaleVol| per sample, and
+// that step is at least step_size * min(scaleVol): the bound holds whatever scaleVol the
+// shader receives (with VVLIC_QUIRK_UNIFORM_SCALE_BUG it is scaleInv, and rays run past the
+// object box until they leave [0, tex_max]).
+vvlic_status prepare_tape(vvlic_ctx* c, int w, int h, RenderArgs& a, cudaStream_t s) {
+  const double diag = std::sqrt((double)a.tex_max[0] * a.tex_max[0] + (double)a.tex_max[1] * a.tex_max[1] +
+                                (double)a.tex_max[2] * a.tex_max[2]);
+  const double min_sv = std::max(1e-6, (double)std::min(std::min(a.scale_vol[0], a.scale_vol[1]), a.scale_vol[2]));
+  double bound = std::min(diag / (a.step_size * min_sv) + 3.0, (double)a.num_iter * (double)a.num_iter);
   if (c->params.tape_max_samples > 0) bound = std::min(bound, (double)c->params.tape_max_samples);
   const int stride = std::max(1, (int)std::ceil(bound));
   const int nck = (stride + kSegment - 1) / kSegment;
@@ -486,7 +491,7 @@ extern "C" vvlic_status vvlic_render_device(vvlic_ctx* c, int32_t vol_id, float*
   const bool record = c->params.record_tape != 0;
   if (record) {
     c->tape_valid = false;
-    if ((st = prepare_tape(c, it->second.geom, w, h, a, s))) return st;
+    if ((st = prepare_tape(c, w, h, a, s))) return st;
   }
   Schedule sch;
   sch.num_sms = c->num_sms;

@@ -418,6 +418,13 @@ def c3(volumes: int = 64, image: int = 512, seed: int = 3, max_views: int = 8, d
     return out, dense_noise(128, seed=seed * 10), p
 
 
+def c3_jobs(vols, image: int = 512):
+    """The batch's jobs in order, (volume, view) pairs, with a cost estimate per job for
+    dealing them over replicas: pixels x taps (the random views' chords are alike)."""
+    jobs = [(bv, v) for bv in vols for v in bv.views]
+    return jobs, [image * image * (2 * bv.L + 1) for bv, _ in jobs]
+
+
 def c5(size: int = 512, image: int = 2048, frames: int = 64, device: str | None = None,
        defaults=LIBRARY) -> Workload:
     """Large turbulence orbit (spectral field via torch.fft on `device`, numpy otherwise)."""
