@@ -16,7 +16,8 @@ and downloads the image.  `roofline` compares the kernel's fetch rate with the m
 fetch ceiling of the GPU (vvlic_measure_fetch_ceiling); DRAM figures are reported beside it.
 Extra keys: the mid-size lit frame with FP32/FP16/BF16 storage (`c2`), the 64-volume batch
 (`batch`), the differentiable-fit forward+adjoint (`fwd_adjoint`), the orbit's forward+adjoint
-(`orbit_adjoint`).
+(`orbit_adjoint`), the TMA-staged brick sampler against the texture and gather samplers
+(`brick_ab`).
 
 `--impl reference` times the CPU restatement of the reference's path (the reference itself is
 GLSL and runs only through OpenGL) on all host cores, on stratified rows of the same orbit
@@ -64,7 +65,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-ceiling", action="store_true", help="skip the L1TEX fetch-ceiling measurement")
     ap.add_argument("--c3-volumes", type=int, default=64)
-    ap.add_argument("--only", default="all", choices=["all", "c5", "c2", "c3", "c4"],
+    ap.add_argument("--only", default="all", choices=["all", "c5", "c2", "c3", "c4", "brick"],
                     help="run one section alone (profiling); its results are the only keys printed")
     return ap.parse_args()
 
@@ -363,6 +364,35 @@ def bench_c2(ctx, torch, stream, flush, args, ceiling):
     return res
 
 
+def bench_brick(ctx, torch, stream, flush, args):
+    """The BRICK sampler (field and noise bricks staged in shared memory by TMA) against the
+    hardware-trilinear texture path and the gathers, on the configurations where a brick holds
+    a segment's streamline reach (the plain 64^3 case: Euler L = 20 reaches 4 texels) and where
+    it does not (the fit's 128^3 Heun L = 30 frame: 12 texels each way)."""
+    from vectorvisualization_gb300 import capi, workloads as wl
+
+    res = {}
+    for name, w, storage in (("C1 64^3 f32 Euler L=20 box 256^2 ortho", wl.c1(), "f32"),
+                             ("C4 128^3 f16 Heun L=30 512^2 view 0", wl.c4(), "f16")):
+        vid = wl.setup_context(ctx, w, storage=storage)
+        W, H = w.width, w.height
+        out = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+        row = {}
+        for sampler in ("brick", "gather", "cell", "texture", "hybrid"):
+            p = capi.Params.from_buffer_copy(w.params)
+            p.sampler = capi.SAMPLER[sampler]
+            p.schedule = capi.SCHEDULE["static" if sampler == "brick" else args.schedule]
+            ctx.set_params(p)
+            frame = lambda: ctx.render_device(vid, out.data_ptr(), W, H, None, stream.cuda_stream)  # noqa: E731
+            timed(torch, stream, flush, frame)
+            ms = min(timed(torch, stream, flush, frame) for _ in range(5))
+            st = ctx.stats()
+            row[sampler] = {"ms": ms, "gss": st.sample_steps / (ms / 1e3) / 1e9, "check_flags": int(st.check_flags)}
+        res[name] = row
+        ctx.free_volume(vid)
+    return res
+
+
 def bench_c4(ctx, torch, stream, flush, args):
     """C4: 128^3 vortex field, dense noise, Heun L=30 (61 taps), 512^2 x 4 views, L2 loss to a
     target rendered from a hidden seeded TF; gradients w.r.t. TF (256x4), opacity (256) and the
@@ -550,6 +580,9 @@ def run_ours(args, dist):
     if args.only in ("all", "c4") and not args.no_c4 and dist.rank == 0:
         with capi.Context(dev) as actx:
             line["fwd_adjoint"] = bench_c4(actx, torch, stream, flush, args)
+    if args.only in ("all", "brick") and dist.rank == 0:
+        with capi.Context(dev) as bctx:
+            line["brick_ab"] = bench_brick(bctx, torch, stream, flush, args)
     if args.only in ("all", "c3") and not args.no_c3:
         with capi.Context(dev) as bctx:
             batch = bench_batch(bctx, torch, stream, flush, args, dist)

@@ -65,8 +65,20 @@ enum { VVLIC_STORAGE_F32 = 0, VVLIC_STORAGE_F16 = 1, VVLIC_STORAGE_BF16 = 2, VVL
  *             filter weights); a BF16 field's texture is a half4 copy of its BF16 texels
  *             (exact for the encoded texel values down to 2^-14);
  *   HYBRID  - field through the texture unit, noise from corner-packed cells through the
- *             load/store path, splitting the gathers over both L1 data pipes. */
-enum { VVLIC_SAMPLER_GATHER = 0, VVLIC_SAMPLER_CELL = 1, VVLIC_SAMPLER_TEXTURE = 2, VVLIC_SAMPLER_HYBRID = 3 };
+ *             load/store path, splitting the gathers over both L1 data pipes;
+ *   BRICK   - field and noise texels staged per 16x8 ray tile into shared memory by TMA
+ *             (cp.async.bulk.tensor), one brick pair per segment of 8 samples covering the
+ *             samples' streamline reach; GATHER's arithmetic from shared memory, global memory
+ *             for fetches outside the bricks.  RAYCAST renders only (no tape, no batch), static
+ *             schedule; needs field rows (nx * texel bytes) and noise rows (mx * channels) that
+ *             are multiples of 16 bytes (else VVLIC_ERR_UNSUPPORTED). */
+enum {
+  VVLIC_SAMPLER_GATHER = 0,
+  VVLIC_SAMPLER_CELL = 1,
+  VVLIC_SAMPLER_TEXTURE = 2,
+  VVLIC_SAMPLER_HYBRID = 3,
+  VVLIC_SAMPLER_BRICK = 4
+};
 
 /* Noise texture preparation (NoiseDataSet::createTexture, dataset.cpp:1176-1344).
  *   SCALAR  - noise value only (the reference without -g, read as the noise value, see quirks);
@@ -217,7 +229,10 @@ enum {
   VVLIC_CHECK_IMAGE = 1u << 4,
   /* a ray of the last recording render had more samples than its tape holds
      (vvlic_params.tape_max_samples): that render's adjoint gradients are NaN */
-  VVLIC_CHECK_TAPE_OVERFLOW = 1u << 5
+  VVLIC_CHECK_TAPE_OVERFLOW = 1u << 5,
+  /* a BRICK render gave up waiting for a brick copy (or could not align its bricks) and read
+     global memory instead */
+  VVLIC_CHECK_BRICK = 1u << 6
 };
 
 /* ---- defaults and helpers (no device work) ------------------------------------------- */

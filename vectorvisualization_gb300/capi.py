@@ -21,7 +21,7 @@ OK, ERR_INVALID_ARGUMENT, ERR_OUT_OF_MEMORY, ERR_CUDA, ERR_NO_DEVICE, ERR_NOT_RE
 ERR_TIMEOUT, ERR_UNSUPPORTED, ERR_BAD_HANDLE, ERR_IO, ERR_FORMAT = 6, 7, 8, 9, 10
 DTYPE_FLOAT32, DTYPE_UINT8 = 0, 1
 STORAGE = {"f32": 0, "f16": 1, "bf16": 2, "u8": 3}
-SAMPLER = {"gather": 0, "cell": 1, "texture": 2, "hybrid": 3}
+SAMPLER = {"gather": 0, "cell": 1, "texture": 2, "hybrid": 3, "brick": 4}
 SCHEDULE = {"queue": 0, "static": 1}
 TECHNIQUE = {"volume": 0, "raycast": 1, "slicing": 2, "licvolume": 3}
 NOISE_SCALAR, NOISE_GRAD_SOBEL, NOISE_GRAD_CENTRAL = 0, 1, 2
@@ -33,7 +33,7 @@ FILTER = {"box": 0, "triangle": 1, "cos2": 2, "gaussian": 3}
 PERSPECTIVE, ORTHOGRAPHIC = 0, 1
 QUIRK_LUMINANCE_NOISE, QUIRK_UNIFORM_SCALE_BUG, QUIRK_GRAD_NOISE_NO_FREQ, QUIRK_ZOECKLER_LUMINANCE = 1, 2, 4, 8
 QUIRKS_REFERENCE = QUIRK_UNIFORM_SCALE_BUG | QUIRK_GRAD_NOISE_NO_FREQ | QUIRK_ZOECKLER_LUMINANCE
-CHECK_FIELD, CHECK_NOISE, CHECK_SCALAR, CHECK_TAPE, CHECK_IMAGE, CHECK_TAPE_OVERFLOW = 1, 2, 4, 8, 16, 32
+CHECK_FIELD, CHECK_NOISE, CHECK_SCALAR, CHECK_TAPE, CHECK_IMAGE, CHECK_TAPE_OVERFLOW, CHECK_BRICK = 1, 2, 4, 8, 16, 32, 64
 
 _f3 = C.c_float * 3
 

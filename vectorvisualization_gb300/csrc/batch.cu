@@ -152,6 +152,8 @@ vvlic_status prepare_batch(vvlic_ctx* c, const vvlic_job* jobs, int n, int tw, i
       return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "batch: job %d: bad image", j);
     vvlic_params p = jb.params;
     if (sampler_override >= 0) p.sampler = sampler_override;
+    if (p.sampler == VVLIC_SAMPLER_BRICK)
+      return fail(c, VVLIC_ERR_UNSUPPORTED, "batch: job %d: the BRICK sampler renders single images only", j);
     p.record_tape = 0;
     const vvlic_params& p0 = jobs[0].params;
     const int smp0 = sampler_override >= 0 ? sampler_override : p0.sampler;

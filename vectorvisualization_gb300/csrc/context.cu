@@ -845,7 +845,7 @@ static vvlic_status check_params(vvlic_ctx* c, const vvlic_params& p) {
     return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "params: illum %d", p.illum);
   if (p.tf_index != VVLIC_TF_INDEX_DIR_Z && p.tf_index != VVLIC_TF_INDEX_MAGNITUDE)
     return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "params: tf_index %d", p.tf_index);
-  if (p.sampler < VVLIC_SAMPLER_GATHER || p.sampler > VVLIC_SAMPLER_HYBRID)
+  if (p.sampler < VVLIC_SAMPLER_GATHER || p.sampler > VVLIC_SAMPLER_BRICK)
     return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "params: sampler %d", p.sampler);
   if (p.schedule != VVLIC_SCHEDULE_QUEUE && p.schedule != VVLIC_SCHEDULE_STATIC)
     return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "params: schedule %d", p.schedule);

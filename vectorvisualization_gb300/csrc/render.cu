@@ -9,11 +9,19 @@
 #include <thread>
 
 #include "../../include/vvlic.h"
+#include "brick.cuh"
 #include "vvlic_device.cuh"
 #include "vvlic_host.hpp"
 #include "vvlic_launch.hpp"
 
 using namespace vvlic;
+
+// Queue schedule: log2 of the tile cost-class width beyond the finest one that fits the longest
+// chord into the 1024 classes (0: finest).  Coarser classes keep more neighbouring tiles in
+// raster order within a class.
+#ifndef VVLIC_QUEUE_COARSEN
+#define VVLIC_QUEUE_COARSEN 0
+#endif
 
 namespace {
 
@@ -185,6 +193,7 @@ vvlic_status build_render_args_ex(vvlic_ctx* c, Volume& v, int W, int H, cudaStr
   a.n[2] = v.n[2];
   switch (p.sampler) {
     case VVLIC_SAMPLER_GATHER:
+    case VVLIC_SAMPLER_BRICK:  // bricks are staged from the texel arrays; fetches outside them gather
       a.field = v.d_texels;
       a.noise = c->noise.d_texels;
       break;
@@ -206,6 +215,11 @@ vvlic_status build_render_args_ex(vvlic_ctx* c, Volume& v, int W, int H, cudaStr
       a.tex = v.tex;
       a.noise = c->noise.d_cells;
       break;
+  }
+  if (VVLIC_RK4_CELL_EVAL && p.integrator == VVLIC_RK4 &&
+      (p.sampler == VVLIC_SAMPLER_TEXTURE || p.sampler == VVLIC_SAMPLER_HYBRID)) {
+    if ((st = ensure_cells(c, v, s))) return st;
+    a.field = v.d_cells;  // the RK4 evaluation taken from cells
   }
   for (int i = 0; i < 3; ++i) {
     a.m[i] = c->noise.m[i];
@@ -386,6 +400,8 @@ vvlic_status make_schedule(vvlic_ctx* c, const RenderArgs& a, const Geometry& gm
   const double maxcost = diag / a.step_size + 2.0;
   int shift = 0;
   while ((maxcost / (double)(1u << shift)) >= 1024.0 && shift < 31) ++shift;
+  // coarser cost classes keep more neighbouring tiles in raster order within a class
+  shift = std::min(31, shift + VVLIC_QUEUE_COARSEN);
   unsigned* scratch = c->d_sched;
   cudaError_t e = launch_tile_order(a, ntiles, tiles_x, shift, scratch, s);
   sch.order = scratch + ntiles;
@@ -458,6 +474,9 @@ extern "C" vvlic_status vvlic_render_device(vvlic_ctx* c, int32_t vol_id, float*
   if (st) return st;
   a.out = d_out;
   a.samples = d_samples;
+  if (c->params.sampler == VVLIC_SAMPLER_BRICK &&
+      (c->params.technique != VVLIC_TECHNIQUE_RAYCAST || c->params.record_tape))
+    return fail(c, VVLIC_ERR_UNSUPPORTED, "render: the BRICK sampler renders the RAYCAST technique without a tape");
   if (c->params.technique != VVLIC_TECHNIQUE_RAYCAST) {
     if (c->params.record_tape)
       return fail(c, VVLIC_ERR_UNSUPPORTED, "render: the adjoint tape is recorded by the RAYCAST technique only");
@@ -495,14 +514,18 @@ extern "C" vvlic_status vvlic_render_device(vvlic_ctx* c, int32_t vol_id, float*
   }
   Schedule sch;
   sch.num_sms = c->num_sms;
+  const bool grad = c->params.illum == VVLIC_ILLUM_GRADIENT;
+  const bool brick = c->params.sampler == VVLIC_SAMPLER_BRICK;
+  BrickArgs bargs;
+  if (brick && (st = prepare_brick(c, it->second, a, grad, bargs))) return st;
   cudaError_t e = cudaMemsetAsync(c->d_counters, 0, 4 * sizeof(unsigned long long), s);
   if (e != cudaSuccess) return cuda_fail(c, e, "render");
-  if (c->params.schedule == VVLIC_SCHEDULE_QUEUE && (st = make_schedule(c, a, it->second.geom, w, h, s, sch)))
+  if (!brick && c->params.schedule == VVLIC_SCHEDULE_QUEUE && (st = make_schedule(c, a, it->second.geom, w, h, s, sch)))
     return st;
   e = cudaEventRecord(c->ev0, s);
   if (e == cudaSuccess)
-    e = launch_raycast(a, it->second.storage, c->params.sampler, c->params.integrator,
-                       c->params.illum == VVLIC_ILLUM_GRADIENT, sch, s);
+    e = brick ? launch_brick(it->second.storage, a, bargs, c->params.integrator, grad, s)
+              : launch_raycast(a, it->second.storage, c->params.sampler, c->params.integrator, grad, sch, s);
   if (e == cudaSuccess) e = cudaEventRecord(c->ev1, s);
   if (e != cudaSuccess) return cuda_fail(c, e, "render launch");
   c->stats_pending = true;
@@ -657,6 +680,8 @@ extern "C" vvlic_status vvlic_compute_lic_volume(vvlic_ctx* c, int32_t vol_id, i
   if (it == c->vols.end()) return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "compute_lic_volume: unknown volume %d", vol_id);
   if (nx < 1 || ny < 1 || nz < 1 || nx > 2048 || ny > 2048 || nz > 2048)
     return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "compute_lic_volume: dims");
+  if (c->params.sampler == VVLIC_SAMPLER_BRICK)
+    return fail(c, VVLIC_ERR_UNSUPPORTED, "compute_lic_volume: the BRICK sampler renders the RAYCAST technique only");
   DeviceGuard g(c->device);
   Volume& v = it->second;
   cudaStream_t s = c->stream;

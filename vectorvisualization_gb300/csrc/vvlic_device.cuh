@@ -9,6 +9,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "../../include/vvlic.h"
 
 namespace vvlic {
@@ -495,11 +497,18 @@ __device__ __forceinline__ float3 slope_h(float4 f, float h) {
   return f3(fmaf(f.x, h2, -h), fmaf(f.y, h2, -h), fmaf(f.z, h2, -h));
 }
 
+// RK4 evaluations taken from the corner-packed cells (load/store path) instead of the texture
+// unit when the field is sampled through textures: 0 or 1 (the third evaluation).
+#ifndef VVLIC_RK4_CELL_EVAL
+#define VVLIC_RK4_CELL_EVAL 0
+#endif
+
 // One streamline step; replaces `step` with the field value at the new position (the
 // first-same-as-last reuse of the reference's `step` in/out argument).
 template <int ST, int FL, int INTEG>
 __device__ __forceinline__ float3 lic_step(const RenderArgs& a, float3 p, float4& step, float dirs) {
   using F = Field<ST, FL>;
+  using F3 = typename std::conditional<(VVLIC_RK4_CELL_EVAL != 0 && FL == kTexture), Field<ST, kCell>, F>::type;
   const float hs = a.sof ? a.h_eff * dirs * step.w : a.h_eff * dirs;
   float3 k1 = INTEG == VVLIC_RK4 ? scl3(slope(step), hs) : slope_h(step, hs);
   if (INTEG == VVLIC_EULER) {
@@ -509,7 +518,7 @@ __device__ __forceinline__ float3 lic_step(const RenderArgs& a, float3 p, float4
     p = add3(p, scl3(add3(k1, k2), 0.5f));
   } else {
     float3 k2 = scl3(slope(F::sample(a, add3(p, scl3(k1, 0.5f)))), hs);
-    float3 k3 = scl3(slope(F::sample(a, add3(p, scl3(k2, 0.5f)))), hs);
+    float3 k3 = scl3(slope(F3::sample(a, add3(p, scl3(k2, 0.5f)))), hs);
     float3 k4 = scl3(slope(F::sample(a, add3(p, k3))), hs);
     p = add3(p, scl3(add3(add3(k1, scl3(k2, 2.0f)), add3(scl3(k3, 2.0f), k4)), 1.0f / 6.0f));
   }

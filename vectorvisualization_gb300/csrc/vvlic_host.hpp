@@ -1,6 +1,7 @@
 // Host-side state of a vvlic context (opaque to callers of the C ABI).
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -33,6 +34,8 @@ struct Volume {
   float* d_licvol = nullptr;      // precomputed LIC volume (vvlic_compute_lic_volume)
   int ln[3] = {0, 0, 0};
   bool licvol_valid = false;      // false after a field update until the next precompute
+  CUtensorMap brick_map;          // BRICK sampler: TMA map of the texels for bricks of brick_box
+  int brick_box[3] = {0, 0, 0};   // (0: no map encoded)
 };
 
 struct NoiseTex {
@@ -43,6 +46,8 @@ struct NoiseTex {
   uint8_t* d_cells = nullptr;     // m^3 cells of 8 corners, built on first CELL render
   cudaArray_t array = nullptr;    // texture copy, built on first TEXTURE render
   cudaTextureObject_t tex = 0;
+  CUtensorMap brick_map;          // BRICK sampler: TMA map of the texels for bricks of brick_box
+  int brick_box[3] = {0, 0, 0};
 };
 
 class DeviceGuard {

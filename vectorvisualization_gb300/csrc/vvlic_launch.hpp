@@ -102,6 +102,12 @@ cudaError_t launch_batch_order(const RenderArgs* jobs, const BatchScratch& b, in
 cudaError_t launch_tile_order(const RenderArgs& a, int ntiles, int tiles_x, int shift, unsigned* scratch,
                               cudaStream_t s);
 
+// BRICK sampler (brick.cu): brick shapes and TMA maps for a render of volume v, and its launch.
+struct BrickArgs;
+struct Volume;
+vvlic_status prepare_brick(vvlic_ctx* c, Volume& v, const RenderArgs& a, bool grad, BrickArgs& b);
+cudaError_t launch_brick(int storage, const RenderArgs& a, const BrickArgs& b, int integ, bool grad, cudaStream_t s);
+
 // Preprocessing (preprocess.cu, compiled without FMA contraction so results match the
 // reference's CPU arithmetic bit for bit).
 // Field encoding of fillTexDataFloatInterp into `storage` texels; d_maxbits is a 4-byte
