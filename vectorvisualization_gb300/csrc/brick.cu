@@ -21,9 +21,8 @@
 namespace vvlic {
 namespace {
 
-constexpr int kTfOff = kBrickStateBytes;                             // 5 * 256 floats
-constexpr int kFieldOff = kBrickStateBytes + 5 * VVLIC_TF_ENTRIES * 4;  // 5504: 128-byte aligned
-static_assert(kFieldOff % 128 == 0, "TMA destinations must be 128-byte aligned");
+constexpr int kTfOff = kBrickTfOff;
+constexpr int kFieldOff = kBrickFieldOff;
 constexpr unsigned kWaitPolls = 1u << 22;  // mbarrier polls before a wait gives up
 
 __host__ __device__ constexpr unsigned round128(unsigned b) { return (b + 127u) & ~127u; }

@@ -13,9 +13,8 @@
 // contractions in the two kernels.
 //
 // The tensor maps cover this GPU's own memory only and use no cluster multicast.  Every wait on
-// the mbarrier is bounded: a wait that runs out records VVLIC_CHECK_BRICK_TIMEOUT in the
-// render's stats (VVLIC_CHECK_BRICK) and the CTA waits (bounded again) for its copy before it
-// returns.
+// the mbarrier is bounded: a wait that runs out records VVLIC_CHECK_BRICK in the render's
+// stats and the CTA waits (bounded again) for its copy before it returns.
 #pragma once
 
 #include <cuda.h>
@@ -51,13 +50,17 @@ struct BrickState {
   int lo[4][6];            // per-warp lower box corners: field xyz, noise xyz (texels)
   int hi[4][6];            // per-warp upper box corners
 };
+// Dynamic shared memory: [BrickState][TF table: 5 x 256 floats][field brick][noise brick].
 constexpr int kBrickStateBytes = 384;  // sizeof(BrickState) rounded up to a multiple of 128
 static_assert(sizeof(BrickState) <= kBrickStateBytes, "brick state");
+constexpr int kBrickTfOff = kBrickStateBytes;
+constexpr int kBrickFieldOff = kBrickTfOff + 5 * VVLIC_TF_ENTRIES * 4;  // 5504
+static_assert(kBrickFieldOff % 128 == 0, "TMA destinations must be 128-byte aligned");
 
 extern __shared__ __align__(128) unsigned char vvlic_brick_smem[];
 
 __device__ __forceinline__ BrickState& brick_state() { return *reinterpret_cast<BrickState*>(vvlic_brick_smem); }
-__device__ __forceinline__ const unsigned char* brick_field_smem() { return vvlic_brick_smem + kBrickStateBytes; }
+__device__ __forceinline__ const unsigned char* brick_field_smem() { return vvlic_brick_smem + kBrickFieldOff; }
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 

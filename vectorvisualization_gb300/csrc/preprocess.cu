@@ -11,6 +11,7 @@
 #include <type_traits>
 
 #include "../../include/vvlic.h"
+#include "vvlic_device.cuh"
 #include "vvlic_launch.hpp"
 
 namespace vvlic {
@@ -238,8 +239,10 @@ __global__ void field_cells_kernel(const void* texels, int nx, int ny, int nz, v
 // noise cell i per axis covers texels i and (i+1) mod m (REPEAT): m^3 cells
 __global__ void noise_cells_kernel(const uint8_t* texels, int mx, int my, int mz, int ch, uint8_t* cells) {
   const size_t count = (size_t)mx * my * mz;
-  for (size_t a = blockIdx.x * (size_t)blockDim.x + threadIdx.x; a < count; a += (size_t)gridDim.x * blockDim.x) {
-    const int x = (int)(a % mx), y = (int)((a / mx) % my), z = (int)(a / ((size_t)mx * my));
+  const int m[3] = {mx, my, mz};
+  for (size_t v = blockIdx.x * (size_t)blockDim.x + threadIdx.x; v < count; v += (size_t)gridDim.x * blockDim.x) {
+    const int x = (int)(v % mx), y = (int)((v / mx) % my), z = (int)(v / ((size_t)mx * my));
+    const size_t a = noise_cell_index(x, y, z, m);
     const int xs[2] = {x, x + 1 == mx ? 0 : x + 1}, ys[2] = {y, y + 1 == my ? 0 : y + 1},
               zs[2] = {z, z + 1 == mz ? 0 : z + 1};
     // the cell is assembled in registers and written with 16-byte (RGBA: 32-byte cells) or one

@@ -39,7 +39,7 @@ vvlic_status ensure_cells(vvlic_ctx* c, Volume& v, cudaStream_t s) {
 
 vvlic_status ensure_noise_cells(vvlic_ctx* c, NoiseTex& n, cudaStream_t s) {
   if (n.d_cells) return VVLIC_OK;
-  const size_t bytes = (size_t)n.m[0] * n.m[1] * n.m[2] * 8 * n.ch;
+  const size_t bytes = noise_cell_count(n.m) * 8 * n.ch;
   cudaError_t e = cudaMalloc(&n.d_cells, bytes);
   if (e != cudaSuccess) return cuda_fail(c, e, "noise cell allocation");
   e = launch_build_noise_cells(n.d_texels, n.m, n.ch, n.d_cells, s);

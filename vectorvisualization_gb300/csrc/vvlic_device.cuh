@@ -380,6 +380,31 @@ __device__ __forceinline__ void repeat_axis_fast(float s, int m, int& i0, int& i
 //     corner and channel.  The accumulator then carries 8 bits below a noise step: the filtered
 //     value is within 0.011 of a step (RMS 0.002, no bias) of the exact trilinear.  The texture
 //     unit's 8-bit filter weights allow up to about 1.5 steps.
+// Order of the noise cells in memory.  0: x fastest (cell (x, y, z) at (z*my + y)*mx + x).
+// 1: 2x2x2 blocks of cells, blocks x fastest, so that the four cells of a 128-byte line are a
+// 2x2 square in (x, y) and the next line holds the z+1 square.
+#ifndef VVLIC_NOISE_CELL_BLOCK
+#define VVLIC_NOISE_CELL_BLOCK 0
+#endif
+__host__ __device__ __forceinline__ size_t noise_cell_index(int x, int y, int z, const int m[3]) {
+#if VVLIC_NOISE_CELL_BLOCK
+  const int bx = (m[0] + 1) >> 1, by = (m[1] + 1) >> 1;
+  return ((((size_t)(z >> 1) * by + (size_t)(y >> 1)) * bx + (size_t)(x >> 1)) << 3) |
+         (size_t)(((z & 1) << 2) | ((y & 1) << 1) | (x & 1));
+#else
+  // 32-bit arithmetic (noises up to 2^32 cells, 1625^3)
+  return (size_t)(((unsigned)z * (unsigned)m[1] + (unsigned)y) * (unsigned)m[0] + (unsigned)x);
+#endif
+}
+// Cells allocated for an m[0] x m[1] x m[2] noise (the blocked order pads odd extents).
+__host__ __device__ __forceinline__ size_t noise_cell_count(const int m[3]) {
+#if VVLIC_NOISE_CELL_BLOCK
+  return (size_t)((m[0] + 1) >> 1) * ((m[1] + 1) >> 1) * ((m[2] + 1) >> 1) * 8;
+#else
+  return (size_t)m[0] * m[1] * m[2];
+#endif
+}
+
 template <bool EXACT> struct NoiseCells {
   static __device__ __forceinline__ float corner(uint32_t w, int k) {
     return EXACT ? byte_as_float(w, k) : byte_biased(w, k);
@@ -395,11 +420,12 @@ template <bool EXACT> struct NoiseCells {
     const float bx = 1.0f - ax, by = 1.0f - ay, bz = 1.0f - az;
     const float w00 = by * bz, w10 = ay * bz, w01 = by * az, w11 = ay * az;
     const float w[8] = {bx * w00, ax * w00, bx * w10, ax * w10, bx * w01, ax * w01, bx * w11, ax * w11};
-    int cidx = (z0 * a.m[1] + y0) * a.m[0] + x0;
-    if (VVLIC_BOUNDS_CHECK && !in_range(a, cidx, (long long)a.m[0] * a.m[1] * a.m[2], VVLIC_CHECK_NOISE)) cidx = 0;
+    size_t cidx = noise_cell_index(x0, y0, z0, a.m);
+    if (VVLIC_BOUNDS_CHECK && !in_range(a, (long long)cidx, (long long)noise_cell_count(a.m), VVLIC_CHECK_NOISE))
+      cidx = 0;
     if (RGBA) {
       uint32_t t[8];
-      ldg256(reinterpret_cast<const uint4*>(a.noise) + 2 * (size_t)cidx, t);
+      ldg256(reinterpret_cast<const uint4*>(a.noise) + 2 * cidx, t);
       float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
       for (int i = 0; i < 8; ++i) {
