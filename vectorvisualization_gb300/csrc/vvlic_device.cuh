@@ -446,6 +446,19 @@ template <bool EXACT> struct NoiseCells {
     return make_float4(0.f, 0.f, 0.f, (v - bias) * k);
   }
 };
+// Prefetch into L1 of the cell a later NoiseCells::sample at p reads (same index arithmetic).
+template <bool GRADC> __device__ __forceinline__ void noise_cell_prefetch(const RenderArgs& a, float3 p, bool rgba) {
+  int x0, x1, y0, y1, z0, z1;
+  float ax, ay, az;
+  repeat_axis_fast(p.x, GRADC ? a.nscale_grad[0] : a.nscale[0], a.m[0], x0, x1, ax);
+  repeat_axis_fast(p.y, GRADC ? a.nscale_grad[1] : a.nscale[1], a.m[1], y0, y1, ay);
+  repeat_axis_fast(p.z, GRADC ? a.nscale_grad[2] : a.nscale[2], a.m[2], z0, z1, az);
+  size_t cidx = noise_cell_index(x0, y0, z0, a.m);
+  if (VVLIC_BOUNDS_CHECK && cidx >= noise_cell_count(a.m)) cidx = 0;
+  const void* addr = a.noise + cidx * (rgba ? 32 : 8);
+  asm volatile("prefetch.global.L1 [%0];" ::"l"(addr));
+}
+
 template <> struct Noise<kCell> : NoiseCells<true> {};
 template <> struct Noise<kCellFast> : NoiseCells<false> {};
 
@@ -563,6 +576,19 @@ template <int NL, bool GRAD> __device__ __forceinline__ float4 noise_tap(const R
   return make_float4(0.f, 0.f, 0.f, noise_value<NL>(a, p));
 }
 
+// Noise taps of compute_lic are prefetched as soon as their streamline position is known and
+// read one streamline step later, so that a cell's load latency overlaps the other chain's step
+// instead of stalling the sum (1; 0 reads each tap right after its step).  The sums add the same
+// terms in the same order either way.
+#ifndef VVLIC_NOISE_PREFETCH
+#define VVLIC_NOISE_PREFETCH 1
+#endif
+template <int NL, bool GRAD> __device__ __forceinline__ void noise_prefetch(const RenderArgs& a, float3 p) {
+  if (VVLIC_NOISE_PREFETCH && (NL == kCell || NL == kCellFast) && !a.gate &&
+      !(a.quirks & VVLIC_QUIRK_LUMINANCE_NOISE && !GRAD))
+    noise_cell_prefetch<GRAD>(a, p, GRAD || a.noise_ch == 4);
+}
+
 template <bool GRAD> __device__ __forceinline__ void accumulate(float4& acc, float4 n, float w) {
   if (GRAD) {
     acc.x = fmaf(n.x, w, acc.x);
@@ -587,13 +613,26 @@ __device__ __forceinline__ float4 compute_lic(const RenderArgs& a, float3 pos, f
   float3 pb = pos, pf = pos;
   float4 sb = f0, sf = f0;
   int i = 1;
-  for (; i <= both; ++i) {
-    pb = lic_step<ST, FL, INTEG>(a, pb, sb, -1.0f);
-    pf = lic_step<ST, FL, INTEG>(a, pf, sf, 1.0f);
-    float4 nb = noise_tap<NL, GRAD>(a, pb);
-    float4 nf = noise_tap<NL, GRAD>(a, pf);
-    accumulate<GRAD>(accb, nb, a.taps[lb - i]);
-    accumulate<GRAD>(accf, nf, a.taps[lb + i]);
+  if (VVLIC_NOISE_PREFETCH && both > 0) {
+    // each chain's tap is read after the other chain's next step (the noise_prefetch note)
+    for (; i <= both; ++i) {
+      pb = lic_step<ST, FL, INTEG>(a, pb, sb, -1.0f);
+      noise_prefetch<NL, GRAD>(a, pb);
+      if (i > 1) accumulate<GRAD>(accf, noise_tap<NL, GRAD>(a, pf), a.taps[lb + i - 1]);
+      pf = lic_step<ST, FL, INTEG>(a, pf, sf, 1.0f);
+      noise_prefetch<NL, GRAD>(a, pf);
+      accumulate<GRAD>(accb, noise_tap<NL, GRAD>(a, pb), a.taps[lb - i]);
+    }
+    accumulate<GRAD>(accf, noise_tap<NL, GRAD>(a, pf), a.taps[lb + both]);
+  } else {
+    for (; i <= both; ++i) {
+      pb = lic_step<ST, FL, INTEG>(a, pb, sb, -1.0f);
+      pf = lic_step<ST, FL, INTEG>(a, pf, sf, 1.0f);
+      float4 nb = noise_tap<NL, GRAD>(a, pb);
+      float4 nf = noise_tap<NL, GRAD>(a, pf);
+      accumulate<GRAD>(accb, nb, a.taps[lb - i]);
+      accumulate<GRAD>(accf, nf, a.taps[lb + i]);
+    }
   }
   for (int j = i; j <= lb; ++j) {
     pb = lic_step<ST, FL, INTEG>(a, pb, sb, -1.0f);
