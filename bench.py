@@ -52,7 +52,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--sampler", default="hybrid", choices=["gather", "cell", "texture", "hybrid"])
-    ap.add_argument("--schedule", default="queue", choices=["queue", "static"])
+    ap.add_argument("--schedule", default="auto", choices=["auto", "queue", "static"],
+                    help="auto: the schedule measured faster per workload (static for the orbit frames, "
+                         "queue for the others)")
     ap.add_argument("--size", type=int, default=512, help="orbit field size per axis")
     ap.add_argument("--image", type=int, default=2048, help="orbit image size")
     ap.add_argument("--c2-size", type=int, default=256)
@@ -68,6 +70,16 @@ def parse():
     ap.add_argument("--only", default="all", choices=["all", "c5", "c2", "c3", "c4", "brick"],
                     help="run one section alone (profiling); its results are the only keys printed")
     return ap.parse_args()
+
+
+def schedule(args, workload: str) -> str:
+    """The work distribution of a section.  Measured on one GB300 (ms per frame): the orbit's
+    2048^2 RK4 frames run about 3 % faster on the static raster grid (1230 / 1419 / 1491 against
+    1268 / 1455 / 1540 for frames 0 / 16 / 40), the lit 1024^2 Heun frame about 3 % faster on
+    the longest-first queue; `auto` takes the faster per workload."""
+    if args.schedule != "auto":
+        return args.schedule
+    return "static" if workload == "orbit" else "queue"
 
 
 def orbit_frames(steps: int, world: int, rank: int) -> list[int]:
@@ -332,7 +344,7 @@ def bench_c2(ctx, torch, stream, flush, args, ceiling):
     vid = wl.setup_context(ctx, w)
     p = w.params
     p.sampler = capi.SAMPLER[args.sampler]
-    p.schedule = capi.SCHEDULE[args.schedule]
+    p.schedule = capi.SCHEDULE[schedule(args, "c2")]
     ctx.set_params(p)
     W, H = w.width, w.height
     out = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
@@ -381,7 +393,7 @@ def bench_brick(ctx, torch, stream, flush, args):
         for sampler in ("brick", "gather", "cell", "texture", "hybrid"):
             p = capi.Params.from_buffer_copy(w.params)
             p.sampler = capi.SAMPLER[sampler]
-            p.schedule = capi.SCHEDULE["static" if sampler == "brick" else args.schedule]
+            p.schedule = capi.SCHEDULE["static" if sampler == "brick" else schedule(args, "brick_ab")]
             ctx.set_params(p)
             frame = lambda: ctx.render_device(vid, out.data_ptr(), W, H, None, stream.cuda_stream)  # noqa: E731
             timed(torch, stream, flush, frame)
@@ -406,7 +418,7 @@ def bench_c4(ctx, torch, stream, flush, args):
     W, H = w.width, w.height
     p = w.params
     p.sampler = capi.SAMPLER[args.sampler]
-    p.schedule = capi.SCHEDULE[args.schedule]
+    p.schedule = capi.SCHEDULE[schedule(args, "c4")]
     sh = stream.cuda_stream
     img = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
     ctx.set_tf(*wl.random_tf(seed=4040))  # the hidden target TF
@@ -607,7 +619,7 @@ def headline(args, dist, torch, stream, flush, ceiling) -> dict:
     vid = wl.setup_context(ctx, w)
     p = w.params
     p.sampler = capi.SAMPLER[args.sampler]
-    p.schedule = capi.SCHEDULE[args.schedule]
+    p.schedule = capi.SCHEDULE[schedule(args, "orbit")]
     ctx.set_params(p)
     setup_s = time.perf_counter() - t0
     sh = stream.cuda_stream
@@ -678,7 +690,7 @@ def headline(args, dist, torch, stream, flush, ceiling) -> dict:
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded SplitMix64 spectral field and noise; the reference ships no datasets)",
-        "config": {**w.describe(), "sampler": args.sampler, "schedule": args.schedule, "frames": frames,
+        "config": {**w.describe(), "sampler": args.sampler, "schedule": schedule(args, "orbit"), "frames": frames,
                    "l2": "inputs > L2 (1 GiB field texture, 4.3 GB noise cells); L2 also flushed between frames "
                          "(256 MiB write)",
                    "sample_steps_per_frame": sum(steps_f) / len(frames),
@@ -687,8 +699,8 @@ def headline(args, dist, torch, stream, flush, ceiling) -> dict:
         "wall_ms_per_step": t_wall / args.steps * 1e3,
         "image_alpha_mean": float(out[..., 3].mean()),
         "roofline": roof,
-        # per frame: the queue schedule's tile order (cost, bucket scan, scatter) + the ray-cast
-        "gpu_launches": args.steps * (4 if args.schedule == "queue" else 1),
+        # per frame: the ray-cast (+ the queue schedule's tile order: cost, bucket scan, scatter)
+        "gpu_launches": args.steps * (4 if schedule(args, "orbit") == "queue" else 1),
         "clocks": clk,
     }
     del total_samples

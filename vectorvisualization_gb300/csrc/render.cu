@@ -16,13 +16,6 @@
 
 using namespace vvlic;
 
-// Queue schedule: log2 of the tile cost-class width beyond the finest one that fits the longest
-// chord into the 1024 classes (0: finest).  Coarser classes keep more neighbouring tiles in
-// raster order within a class.
-#ifndef VVLIC_QUEUE_COARSEN
-#define VVLIC_QUEUE_COARSEN 0
-#endif
-
 namespace {
 
 vvlic_status ensure_cells(vvlic_ctx* c, Volume& v, cudaStream_t s) {
@@ -216,11 +209,7 @@ vvlic_status build_render_args_ex(vvlic_ctx* c, Volume& v, int W, int H, cudaStr
       a.noise = c->noise.d_cells;
       break;
   }
-  if (VVLIC_RK4_CELL_EVAL && p.integrator == VVLIC_RK4 &&
-      (p.sampler == VVLIC_SAMPLER_TEXTURE || p.sampler == VVLIC_SAMPLER_HYBRID)) {
-    if ((st = ensure_cells(c, v, s))) return st;
-    a.field = v.d_cells;  // the RK4 evaluation taken from cells
-  }
+
   for (int i = 0; i < 3; ++i) {
     a.m[i] = c->noise.m[i];
     a.sn[i] = c->sn[i];
@@ -400,8 +389,6 @@ vvlic_status make_schedule(vvlic_ctx* c, const RenderArgs& a, const Geometry& gm
   const double maxcost = diag / a.step_size + 2.0;
   int shift = 0;
   while ((maxcost / (double)(1u << shift)) >= 1024.0 && shift < 31) ++shift;
-  // coarser cost classes keep more neighbouring tiles in raster order within a class
-  shift = std::min(31, shift + VVLIC_QUEUE_COARSEN);
   unsigned* scratch = c->d_sched;
   cudaError_t e = launch_tile_order(a, ntiles, tiles_x, shift, scratch, s);
   sch.order = scratch + ntiles;

@@ -63,22 +63,10 @@ __device__ __forceinline__ void flush_counters(const RenderArgs& a, uint32_t sam
   }
 }
 
-// Transfer-function tables of the render kernels: 0 staged into shared memory per CTA; 1 read
-// from global memory through L1, with the launch asking for the largest L1 share.
-#ifndef VVLIC_TF_IN_L1
-#define VVLIC_TF_IN_L1 0
-#endif
-#if VVLIC_TF_IN_L1
-#define VVLIC_RENDER_TF const float* s_tf = a.tf;
-#else
-#define VVLIC_RENDER_TF                                      \
-  __shared__ __align__(16) float s_tf[5 * VVLIC_TF_ENTRIES]; \
-  load_tf(a, s_tf);
-#endif
-
 template <int ST, int FL, int NL, int INTEG, bool GRAD>
 __global__ void __launch_bounds__(kThreads, min_blocks<INTEG, GRAD>()) raycast_kernel(const __grid_constant__ RenderArgs a) {
-  VVLIC_RENDER_TF
+  __shared__ __align__(16) float s_tf[5 * VVLIC_TF_ENTRIES];
+  load_tf(a, s_tf);
   const int px = blockIdx.x * kTileW + (threadIdx.x % kTileW);
   const int py = blockIdx.y * kTileH + (threadIdx.x / kTileW);
   uint32_t samples = 0, hit = 0;
@@ -93,7 +81,8 @@ template <int ST, int FL, int NL, int INTEG, bool GRAD>
 __global__ void __launch_bounds__(kThreads, min_blocks<INTEG, GRAD>()) raycast_queue_kernel(const __grid_constant__ RenderArgs a,
                                                                  const uint32_t* __restrict__ order, int ntiles,
                                                                  unsigned* __restrict__ next) {
-  VVLIC_RENDER_TF
+  __shared__ __align__(16) float s_tf[5 * VVLIC_TF_ENTRIES];
+  load_tf(a, s_tf);
   const int lane = threadIdx.x & 31;
   const int tiles_x = (a.W + kWarpTileW - 1) / kWarpTileW;
   uint32_t samples_acc = 0, hits_acc = 0;
@@ -124,10 +113,6 @@ static cudaError_t launch_one(const RenderArgs& a, const Schedule& sch, cudaStre
     return cudaGetLastError();
   }
   auto kern = raycast_queue_kernel<ST, FL, NL, INTEG, GRAD>;
-  if (VVLIC_TF_IN_L1) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
-    if (e != cudaSuccess) return e;
-  }
   int per_sm = 0;
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, 0);
   if (e != cudaSuccess) return e;

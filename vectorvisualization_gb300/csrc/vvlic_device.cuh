@@ -9,8 +9,6 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
-#include <type_traits>
-
 #include "../../include/vvlic.h"
 
 namespace vvlic {
@@ -380,30 +378,12 @@ __device__ __forceinline__ void repeat_axis_fast(float s, int m, int& i0, int& i
 //     corner and channel.  The accumulator then carries 8 bits below a noise step: the filtered
 //     value is within 0.011 of a step (RMS 0.002, no bias) of the exact trilinear.  The texture
 //     unit's 8-bit filter weights allow up to about 1.5 steps.
-// Order of the noise cells in memory.  0: x fastest (cell (x, y, z) at (z*my + y)*mx + x).
-// 1: 2x2x2 blocks of cells, blocks x fastest, so that the four cells of a 128-byte line are a
-// 2x2 square in (x, y) and the next line holds the z+1 square.
-#ifndef VVLIC_NOISE_CELL_BLOCK
-#define VVLIC_NOISE_CELL_BLOCK 0
-#endif
+// Noise cells in memory: cell (x, y, z) at (z*my + y)*mx + x, in 32-bit arithmetic (noises up
+// to 2^32 cells, 1625^3).  (A 2x2x2-blocked order measured within 1 % on the 512^3 orbit.)
 __host__ __device__ __forceinline__ size_t noise_cell_index(int x, int y, int z, const int m[3]) {
-#if VVLIC_NOISE_CELL_BLOCK
-  const int bx = (m[0] + 1) >> 1, by = (m[1] + 1) >> 1;
-  return ((((size_t)(z >> 1) * by + (size_t)(y >> 1)) * bx + (size_t)(x >> 1)) << 3) |
-         (size_t)(((z & 1) << 2) | ((y & 1) << 1) | (x & 1));
-#else
-  // 32-bit arithmetic (noises up to 2^32 cells, 1625^3)
   return (size_t)(((unsigned)z * (unsigned)m[1] + (unsigned)y) * (unsigned)m[0] + (unsigned)x);
-#endif
 }
-// Cells allocated for an m[0] x m[1] x m[2] noise (the blocked order pads odd extents).
-__host__ __device__ __forceinline__ size_t noise_cell_count(const int m[3]) {
-#if VVLIC_NOISE_CELL_BLOCK
-  return (size_t)((m[0] + 1) >> 1) * ((m[1] + 1) >> 1) * ((m[2] + 1) >> 1) * 8;
-#else
-  return (size_t)m[0] * m[1] * m[2];
-#endif
-}
+__host__ __device__ __forceinline__ size_t noise_cell_count(const int m[3]) { return (size_t)m[0] * m[1] * m[2]; }
 
 template <bool EXACT> struct NoiseCells {
   static __device__ __forceinline__ float corner(uint32_t w, int k) {
@@ -446,19 +426,6 @@ template <bool EXACT> struct NoiseCells {
     return make_float4(0.f, 0.f, 0.f, (v - bias) * k);
   }
 };
-// Prefetch into L1 of the cell a later NoiseCells::sample at p reads (same index arithmetic).
-template <bool GRADC> __device__ __forceinline__ void noise_cell_prefetch(const RenderArgs& a, float3 p, bool rgba) {
-  int x0, x1, y0, y1, z0, z1;
-  float ax, ay, az;
-  repeat_axis_fast(p.x, GRADC ? a.nscale_grad[0] : a.nscale[0], a.m[0], x0, x1, ax);
-  repeat_axis_fast(p.y, GRADC ? a.nscale_grad[1] : a.nscale[1], a.m[1], y0, y1, ay);
-  repeat_axis_fast(p.z, GRADC ? a.nscale_grad[2] : a.nscale[2], a.m[2], z0, z1, az);
-  size_t cidx = noise_cell_index(x0, y0, z0, a.m);
-  if (VVLIC_BOUNDS_CHECK && cidx >= noise_cell_count(a.m)) cidx = 0;
-  const void* addr = a.noise + cidx * (rgba ? 32 : 8);
-  asm volatile("prefetch.global.L1 [%0];" ::"l"(addr));
-}
-
 template <> struct Noise<kCell> : NoiseCells<true> {};
 template <> struct Noise<kCellFast> : NoiseCells<false> {};
 
@@ -536,18 +503,11 @@ __device__ __forceinline__ float3 slope_h(float4 f, float h) {
   return f3(fmaf(f.x, h2, -h), fmaf(f.y, h2, -h), fmaf(f.z, h2, -h));
 }
 
-// RK4 evaluations taken from the corner-packed cells (load/store path) instead of the texture
-// unit when the field is sampled through textures: 0 or 1 (the third evaluation).
-#ifndef VVLIC_RK4_CELL_EVAL
-#define VVLIC_RK4_CELL_EVAL 0
-#endif
-
 // One streamline step; replaces `step` with the field value at the new position (the
 // first-same-as-last reuse of the reference's `step` in/out argument).
 template <int ST, int FL, int INTEG>
 __device__ __forceinline__ float3 lic_step(const RenderArgs& a, float3 p, float4& step, float dirs) {
   using F = Field<ST, FL>;
-  using F3 = typename std::conditional<(VVLIC_RK4_CELL_EVAL != 0 && FL == kTexture), Field<ST, kCell>, F>::type;
   const float hs = a.sof ? a.h_eff * dirs * step.w : a.h_eff * dirs;
   float3 k1 = INTEG == VVLIC_RK4 ? scl3(slope(step), hs) : slope_h(step, hs);
   if (INTEG == VVLIC_EULER) {
@@ -557,7 +517,7 @@ __device__ __forceinline__ float3 lic_step(const RenderArgs& a, float3 p, float4
     p = add3(p, scl3(add3(k1, k2), 0.5f));
   } else {
     float3 k2 = scl3(slope(F::sample(a, add3(p, scl3(k1, 0.5f)))), hs);
-    float3 k3 = scl3(slope(F3::sample(a, add3(p, scl3(k2, 0.5f)))), hs);
+    float3 k3 = scl3(slope(F::sample(a, add3(p, scl3(k2, 0.5f)))), hs);
     float3 k4 = scl3(slope(F::sample(a, add3(p, k3))), hs);
     p = add3(p, scl3(add3(add3(k1, scl3(k2, 2.0f)), add3(scl3(k3, 2.0f), k4)), 1.0f / 6.0f));
   }
@@ -574,19 +534,6 @@ template <int NL, bool GRAD> __device__ __forceinline__ float4 noise_tap(const R
   }
   if (a.quirks & VVLIC_QUIRK_LUMINANCE_NOISE) return make_float4(0.f, 0.f, 0.f, 1.0f);
   return make_float4(0.f, 0.f, 0.f, noise_value<NL>(a, p));
-}
-
-// Noise taps of compute_lic are prefetched as soon as their streamline position is known and
-// read one streamline step later, so that a cell's load latency overlaps the other chain's step
-// instead of stalling the sum (1; 0 reads each tap right after its step).  The sums add the same
-// terms in the same order either way.
-#ifndef VVLIC_NOISE_PREFETCH
-#define VVLIC_NOISE_PREFETCH 1
-#endif
-template <int NL, bool GRAD> __device__ __forceinline__ void noise_prefetch(const RenderArgs& a, float3 p) {
-  if (VVLIC_NOISE_PREFETCH && (NL == kCell || NL == kCellFast) && !a.gate &&
-      !(a.quirks & VVLIC_QUIRK_LUMINANCE_NOISE && !GRAD))
-    noise_cell_prefetch<GRAD>(a, p, GRAD || a.noise_ch == 4);
 }
 
 template <bool GRAD> __device__ __forceinline__ void accumulate(float4& acc, float4 n, float w) {
@@ -613,26 +560,13 @@ __device__ __forceinline__ float4 compute_lic(const RenderArgs& a, float3 pos, f
   float3 pb = pos, pf = pos;
   float4 sb = f0, sf = f0;
   int i = 1;
-  if (VVLIC_NOISE_PREFETCH && both > 0) {
-    // each chain's tap is read after the other chain's next step (the noise_prefetch note)
-    for (; i <= both; ++i) {
-      pb = lic_step<ST, FL, INTEG>(a, pb, sb, -1.0f);
-      noise_prefetch<NL, GRAD>(a, pb);
-      if (i > 1) accumulate<GRAD>(accf, noise_tap<NL, GRAD>(a, pf), a.taps[lb + i - 1]);
-      pf = lic_step<ST, FL, INTEG>(a, pf, sf, 1.0f);
-      noise_prefetch<NL, GRAD>(a, pf);
-      accumulate<GRAD>(accb, noise_tap<NL, GRAD>(a, pb), a.taps[lb - i]);
-    }
-    accumulate<GRAD>(accf, noise_tap<NL, GRAD>(a, pf), a.taps[lb + both]);
-  } else {
-    for (; i <= both; ++i) {
-      pb = lic_step<ST, FL, INTEG>(a, pb, sb, -1.0f);
-      pf = lic_step<ST, FL, INTEG>(a, pf, sf, 1.0f);
-      float4 nb = noise_tap<NL, GRAD>(a, pb);
-      float4 nf = noise_tap<NL, GRAD>(a, pf);
-      accumulate<GRAD>(accb, nb, a.taps[lb - i]);
-      accumulate<GRAD>(accf, nf, a.taps[lb + i]);
-    }
+  for (; i <= both; ++i) {
+    pb = lic_step<ST, FL, INTEG>(a, pb, sb, -1.0f);
+    pf = lic_step<ST, FL, INTEG>(a, pf, sf, 1.0f);
+    float4 nb = noise_tap<NL, GRAD>(a, pb);
+    float4 nf = noise_tap<NL, GRAD>(a, pf);
+    accumulate<GRAD>(accb, nb, a.taps[lb - i]);
+    accumulate<GRAD>(accf, nf, a.taps[lb + i]);
   }
   for (int j = i; j <= lb; ++j) {
     pb = lic_step<ST, FL, INTEG>(a, pb, sb, -1.0f);
