@@ -23,12 +23,11 @@ constexpr int kThreads = 128;
 #ifndef VVLIC_MIN_BLOCKS
 #define VVLIC_MIN_BLOCKS 7
 #endif
-// The same for the RK4 kernels, which hold four slopes per step: at 73 registers the lit RK4
-// kernel spills 40 B; at 6 CTAs (80 registers, 8 B) the 512^3 RK4 frame ran 1.5 % faster
-// (110.5 vs 108.9 Gsample-steps/s, two alternations).  8 CTAs (64 registers) for every kernel
-// measured the same as 7 on the lit 1024^2 frame.
+// The same for the RK4 kernels, which hold four slopes per step and trace two samples per pass
+// (trace_ray): 4 CTAs, 128 registers.  With one sample per pass, 6 CTAs (80 registers) was
+// best: 7 and 8 CTAs spilled and ran 1.5-3 % slower on the 512^3 RK4 orbit frames.
 #ifndef VVLIC_RK4_MIN_BLOCKS
-#define VVLIC_RK4_MIN_BLOCKS 6
+#define VVLIC_RK4_MIN_BLOCKS 4
 #endif
 // Unlit (and line-lit) Euler / Heun kernels: no noise gradients to carry.
 #ifndef VVLIC_UNLIT_MIN_BLOCKS

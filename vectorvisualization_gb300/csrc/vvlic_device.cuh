@@ -933,14 +933,22 @@ __device__ __forceinline__ float4 trace_pixel2(const RenderArgs& a, const float*
 }
 
 // Samples whose LIC one thread computes together: 1 (trace_pixel) or 2 (trace_pixel2, twice the
-// independent gather chains per thread at more registers per thread).
+// independent gather chains per thread at more registers per thread).  RK4 kernels, whose four
+// serial fetches per step leave a thread mostly waiting, take two: on the 512^3 / 2048^2 RK4
+// orbit frames 106.0 against 103.3 Gsample-steps/s at 128 registers (4 CTAs/SM; 102 registers
+// measured 105.7).  Euler and Heun kernels take one (two measured +1 % on the lit 1024^2 Heun
+// frame with the texture field, -9 % with the cell field).
 #ifndef VVLIC_SAMPLES_PER_PASS
 #define VVLIC_SAMPLES_PER_PASS 1
+#endif
+#ifndef VVLIC_RK4_SAMPLES_PER_PASS
+#define VVLIC_RK4_SAMPLES_PER_PASS 2
 #endif
 template <int ST, int FL, int NL, int INTEG, bool GRAD>
 __device__ __forceinline__ float4 trace_ray(const RenderArgs& a, const float* s_tf, int px, int py,
                                             uint32_t& samples, uint32_t& hit) {
-  if constexpr (VVLIC_SAMPLES_PER_PASS == 2) return trace_pixel2<ST, FL, NL, INTEG, GRAD>(a, s_tf, px, py, samples, hit);
+  constexpr int spp = INTEG == VVLIC_RK4 ? VVLIC_RK4_SAMPLES_PER_PASS : VVLIC_SAMPLES_PER_PASS;
+  if constexpr (spp == 2) return trace_pixel2<ST, FL, NL, INTEG, GRAD>(a, s_tf, px, py, samples, hit);
   else return trace_pixel<ST, FL, NL, INTEG, GRAD>(a, s_tf, px, py, samples, hit);
 }
 
