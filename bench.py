@@ -705,29 +705,34 @@ def headline(args, dist, torch, stream, flush, ceiling) -> dict:
     }
     del total_samples
 
-    # end to end through the C ABI with host buffers (every step: field + noise from pinned host
-    # memory, encode, noise gradients, layout rebuilds, render, image download)
+    # end to end through the C ABI with host buffers.  Every step copies the field and the noise
+    # from pinned host memory, re-encodes the field, recomputes the noise gradients and layouts,
+    # renders and downloads the image.  `e2e` runs the steps as the stream-ordered animation
+    # step (vvlic_update_field_async, vvlic_upload_noise_async, vvlic_render_to_host_async on
+    # one stream, one wait at the end), so each step's host copies overlap the previous render;
+    # `e2e_synchronous` runs the first steps with the synchronous calls for comparison.
     if not args.no_e2e:
-        lib = capi.load()
         field_h = torch.from_numpy(np.ascontiguousarray(w.field)).pin_memory()
         noise_h = torch.from_numpy(np.ascontiguousarray(w.noise)).pin_memory()
         img_h = torch.empty((H, W, 4), dtype=torch.float32).pin_memory()
         nz, ny, nx = w.field.shape[:3]
         mz, my, mx = w.noise.shape
+        lib = capi.load()
 
-        def e2e_step(f):
-            ctx._check(lib.vvlic_update_field(ctx.h, vid, field_h.data_ptr(), capi.DTYPE_FLOAT32, nx, ny, nz),
-                       "update_field")
-            ctx._check(lib.vvlic_upload_noise(ctx.h, noise_h.data_ptr(), mx, my, mz, w.noise_mode), "upload_noise")
+        def step_async(f):
+            ctx.update_field_async(vid, field_h.data_ptr(), (nx, ny, nz), sh)
+            ctx.upload_noise_async(noise_h.data_ptr(), (mx, my, mz), w.noise_mode, sh)
             ctx.set_view(w.views[f])
-            ctx._check(lib.vvlic_render(ctx.h, vid, img_h.data_ptr(), W, H), "render")
+            ctx.render_to_host_async(vid, img_h.data_ptr(), W, H, sh)
 
-        e2e_step(frames[0])
+        step_async(frames[0])
+        stream.synchronize()
         dist.barrier()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for f in frames:
-            e2e_step(f)
+            step_async(f)
+        ctx._check(lib.vvlic_synchronize(ctx.h, sh, 600000), "synchronize")
         torch.cuda.synchronize()
         t = dist.max(time.perf_counter() - t0)
         last = ctx.stats()
@@ -736,9 +741,24 @@ def headline(args, dist, torch, stream, flush, ceiling) -> dict:
                        "d2h_bytes_per_step": int(img_h.numel() * 4),
                        "ms_per_step": t / args.steps * 1e3,
                        "same_sample_steps_as_device_timed": int(last.sample_steps) == steps_f[-1],
-                       "includes": "field upload+encode (in place), noise upload+gradients, cell and texture "
-                                   "layout rebuilds, view, render, image download; the same frames as the "
-                                   "device-timed steps"}
+                       "includes": "per step: field copy from pinned host memory + in-place encode, noise copy + "
+                                   "gradients, cell and texture layout rebuilds, view, render, image copy to pinned "
+                                   "host memory; stream-ordered calls, the next step's copies overlapping the "
+                                   "render; the same frames as the device-timed steps"}
+        # the same steps with the synchronous calls (each returns when its work is done)
+        ns = min(len(frames), 4)
+        t0 = time.perf_counter()
+        steps_sync = 0
+        for f in frames[:ns]:
+            ctx._check(lib.vvlic_update_field(ctx.h, vid, field_h.data_ptr(), capi.DTYPE_FLOAT32, nx, ny, nz),
+                       "update_field")
+            ctx._check(lib.vvlic_upload_noise(ctx.h, noise_h.data_ptr(), mx, my, mz, w.noise_mode), "upload_noise")
+            ctx.set_view(w.views[f])
+            ctx._check(lib.vvlic_render(ctx.h, vid, img_h.data_ptr(), W, H), "render")
+            steps_sync += ctx.stats().sample_steps
+        t = time.perf_counter() - t0
+        line["e2e_synchronous"] = {"value": steps_sync / t / 1e9, "unit": UNIT, "steps": ns,
+                                   "ms_per_step": t / ns * 1e3}
 
     if not args.no_adjoint and dist.rank == 0:
         line["orbit_adjoint"] = bench_orbit_adjoint(ctx, torch, stream, flush, w, vid, out, frames[0])

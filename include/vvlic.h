@@ -293,6 +293,20 @@ vvlic_status vvlic_upload_field_device(vvlic_ctx* ctx, const float* d_xyz,
  * Waits for the device's in-flight work, then returns when the update is complete. */
 vvlic_status vvlic_update_field(vvlic_ctx* ctx, int32_t vol_id, const void* xyz, int32_t dtype,
                                 int32_t nx, int32_t ny, int32_t nz);
+/* vvlic_update_field ordered on `stream` instead of on the host (no counterpart in the
+ * reference, whose animation step idle() re-creates the texture synchronously, 3DLIC.cpp:129-145).
+ * The host copy runs on the context's copy stream into a staging buffer of its own; the
+ * re-encoding and layout rebuild run on `stream` after that copy and after everything already
+ * enqueued on `stream`.  The call returns at once, so the copy for the next frame overlaps the
+ * render of the current one.
+ *   - `xyz` must stay unchanged until the copy has run (after the next operation on `stream`
+ *     has completed, e.g. vvlic_synchronize).
+ *   - Renders of this volume must be enqueued on `stream` too: work on other streams is not
+ *     ordered against the rewrite.
+ *   - Back-to-back calls are ordered among themselves: a copy waits until the previous update's
+ *     encoding has consumed the staging buffer. */
+vvlic_status vvlic_update_field_async(vvlic_ctx* ctx, int32_t vol_id, const void* xyz, int32_t dtype,
+                                      int32_t nx, int32_t ny, int32_t nz, void* stream);
 /* The same with the time interpolation of vvlic_upload_field_interp. */
 vvlic_status vvlic_update_field_interp(vvlic_ctx* ctx, int32_t vol_id, const void* xyz0, const void* xyz1,
                                        int32_t dtype, int32_t nx, int32_t ny, int32_t nz,
@@ -316,6 +330,13 @@ vvlic_status vvlic_volume_bytes(const vvlic_ctx* ctx, int32_t vol_id, uint64_t* 
  * recorded adjoint tape is dropped. */
 vvlic_status vvlic_upload_noise(vvlic_ctx* ctx, const uint8_t* noise,
                                 int32_t mx, int32_t my, int32_t mz, int32_t mode);
+/* vvlic_upload_noise of a noise with the current noise's extent and channel count, ordered on
+ * `stream` like vvlic_update_field_async (host copy on the copy stream, gradients and layout
+ * rebuild on `stream`); returns at once.  A noise of another extent returns
+ * VVLIC_ERR_NOT_READY: upload it with vvlic_upload_noise first.  `noise` must stay unchanged
+ * until the copy has run.  No counterpart in the reference. */
+vvlic_status vvlic_upload_noise_async(vvlic_ctx* ctx, const uint8_t* noise, int32_t mx, int32_t my, int32_t mz,
+                                      int32_t mode, void* stream);
 /* Noise with precomputed gradients: mx*my*mz RGBA texels (quantised gradient x, y, z, noise)
  * as vvlic_upload_noise builds them; `mode` (SOBEL or CENTRAL) records their kind. */
 vvlic_status vvlic_upload_noise_rgba(vvlic_ctx* ctx, const uint8_t* rgba, int32_t mx, int32_t my, int32_t mz,
@@ -393,6 +414,13 @@ vvlic_status vvlic_view_rays(const vvlic_ctx* ctx, int32_t vol_id, int32_t w, in
 /* Renderer::render -> raycastVolume (renderer.cpp:126-312, 1093-1120): one LIC ray per pixel.
  * `out_rgba` is HOST memory (w*h*4 floats); the call copies the image back and synchronises. */
 vvlic_status vvlic_render(vvlic_ctx* ctx, int32_t vol_id, float* out_rgba, int32_t w, int32_t h);
+/* vvlic_render into HOST memory, asynchronous on `stream`: the render and the copy of the
+ * image into `out_rgba` (pinned memory lets the copy overlap other work) are enqueued and the
+ * call returns; the image is in `out_rgba` once `stream` has completed.  Consecutive calls
+ * share one device image buffer, so they must use the same stream.  No counterpart in the
+ * reference (its render draws into the window). */
+vvlic_status vvlic_render_to_host_async(vvlic_ctx* ctx, int32_t vol_id, float* out_rgba, int32_t w, int32_t h,
+                                        void* stream);
 /* Same into DEVICE memory, asynchronous on `stream`.  `d_samples` (optional, w*h uint32) gets
  * the number of LIC samples of each ray. */
 vvlic_status vvlic_render_device(vvlic_ctx* ctx, int32_t vol_id, float* d_out_rgba,

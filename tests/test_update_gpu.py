@@ -202,3 +202,57 @@ def test_repeated_updates_allocate_nothing(ctx):
     torch.cuda.synchronize()
     assert abs(torch.cuda.mem_get_info()[0] - free0) < (1 << 20)
     ctx.free_volume(vid)
+
+
+@pytest.mark.parametrize("lit", [False, True])
+def test_stream_ordered_animation_equals_synchronous_steps(ctx, lit):
+    """vvlic_update_field_async + vvlic_upload_noise_async + vvlic_render_to_host_async on one
+    stream, all frames enqueued before a single wait, give the images of the synchronous
+    update / upload / render sequence bit for bit (every copy overlaps the previous render)."""
+    import torch
+
+    w = small()
+    if lit:
+        w.params.illum = capi.ILLUM_GRADIENT
+        w.noise_mode = capi.NOISE_GRAD_CENTRAL
+    fields = [other_field(w, seed=s) for s in (11, 12, 13)]
+    noises = [wl.dense_noise(w.noise.shape[::-1], seed=s) for s in (21, 22, 23)]
+    views = [wl.perspective_view(wl.quat_axis_angle((0, 1, 0), a), distance=2.2) for a in (0.0, 40.0, 80.0)]
+    W, H = w.width, w.height
+    vid = wl.setup_context(ctx, w, storage="f16")
+    p = w.params
+    p.sampler = capi.SAMPLER["hybrid"]
+    ctx.set_params(p)
+    want = []
+    for f, n, v in zip(fields, noises, views):
+        ctx.update_field(vid, f)
+        ctx.upload_noise(n, w.noise_mode)
+        ctx.set_view(v)
+        want.append(ctx.render(vid, W, H))
+    ctx.update_field(vid, w.field)  # back to the first state
+    hf = [torch.from_numpy(np.ascontiguousarray(f)).pin_memory() for f in fields]
+    hn = [torch.from_numpy(np.ascontiguousarray(n)).pin_memory() for n in noises]
+    out = [torch.empty((H, W, 4), dtype=torch.float32).pin_memory() for _ in fields]
+    stream = torch.cuda.Stream()
+    nz, ny, nx = w.field.shape[:3]
+    for k, v in enumerate(views):
+        ctx.update_field_async(vid, hf[k].data_ptr(), (nx, ny, nz), stream.cuda_stream)
+        ctx.upload_noise_async(hn[k].data_ptr(), noises[k].shape[::-1], w.noise_mode, stream.cuda_stream)
+        ctx.set_view(v)
+        ctx.render_to_host_async(vid, out[k].data_ptr(), W, H, stream.cuda_stream)
+    assert ctx.synchronize(stream.cuda_stream, timeout_ms=120000)
+    for k in range(len(views)):
+        np.testing.assert_array_equal(out[k].numpy(), want[k], err_msg=f"frame {k}")
+    ctx.free_volume(vid)
+
+
+def test_async_noise_needs_a_same_shape_noise(ctx):
+    import torch
+
+    w = small()
+    wl.setup_context(ctx, w, storage="f16")
+    other = wl.dense_noise((8, 8, 8), seed=3)
+    h = torch.from_numpy(other).pin_memory()
+    with pytest.raises(capi.VVLICError) as e:
+        ctx.upload_noise_async(h.data_ptr(), (8, 8, 8), capi.NOISE_SCALAR, 0)
+    assert e.value.status == capi.ERR_NOT_READY

@@ -193,6 +193,9 @@ _SIGS = {
     "vvlic_upload_field_interp": (_I, [_P, _P, _P, _I, _I, _I, _I, _P, _I, _I, _I, C.POINTER(_I)]),
     "vvlic_update_field": (_I, [_P, _I, _P, _I, _I, _I, _I]),
     "vvlic_update_field_interp": (_I, [_P, _I, _P, _P, _I, _I, _I, _I, _I, _I]),
+    "vvlic_update_field_async": (_I, [_P, _I, _P, _I, _I, _I, _I, _P]),
+    "vvlic_upload_noise_async": (_I, [_P, _P, _I, _I, _I, _I, _P]),
+    "vvlic_render_to_host_async": (_I, [_P, _I, _P, _I, _I, _P]),
     "vvlic_free_volume": (_I, [_P, _I]),
     "vvlic_volume_bytes": (_I, [_P, _I, C.POINTER(C.c_uint64)]),
     "vvlic_upload_noise": (_I, [_P, _P, _I, _I, _I, _I]),
@@ -568,6 +571,21 @@ class Context:
         """Gradients of the last recording render (params.record_tape = 1) into device buffers."""
         self._check(self._lib.vvlic_render_adjoint(self.h, vid, d_grad_img, w, h, d_tf, d_opac, d_taps, stream or None),
                     "render_adjoint")
+
+    # -- stream-ordered animation step (pointers must stay valid until the stream has run) --
+    def update_field_async(self, vid: int, h_xyz: int, dims, stream: int, dtype: int = DTYPE_FLOAT32):
+        nx, ny, nz = dims
+        self._check(self._lib.vvlic_update_field_async(self.h, vid, h_xyz, dtype, nx, ny, nz, stream or None),
+                    "update_field_async")
+
+    def upload_noise_async(self, h_noise: int, dims, mode: int, stream: int):
+        mx, my, mz = dims
+        self._check(self._lib.vvlic_upload_noise_async(self.h, h_noise, mx, my, mz, mode, stream or None),
+                    "upload_noise_async")
+
+    def render_to_host_async(self, vid: int, h_out: int, w: int, h: int, stream: int):
+        self._check(self._lib.vvlic_render_to_host_async(self.h, vid, h_out, w, h, stream or None),
+                    "render_to_host_async")
 
     def compute_lic_volume(self, vid: int, dims) -> None:
         nx, ny, nz = dims

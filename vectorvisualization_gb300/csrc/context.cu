@@ -370,7 +370,7 @@ static void free_noise(NoiseTex& n) {
 extern "C" vvlic_status vvlic_destroy(vvlic_ctx* c) {
   if (!c) return VVLIC_ERR_BAD_HANDLE;
   DeviceGuard g(c->device);
-  if (c->stream) cudaStreamSynchronize(c->stream);
+  cudaDeviceSynchronize();  // renders and stream-ordered updates on any stream
   for (auto& kv : c->vols) free_volume(kv.second);
   free_noise(c->noise);
   if (c->d_scalar) cudaFree(c->d_scalar);
@@ -380,6 +380,12 @@ extern "C" vvlic_status vvlic_destroy(vvlic_ctx* c) {
   if (c->d_scratch_word) cudaFree(c->d_scratch_word);
   if (c->d_image) cudaFree(c->d_image);
   if (c->d_upload) cudaFree(c->d_upload);
+  if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
+  if (c->d_field_stage) cudaFree(c->d_field_stage);
+  if (c->d_noise_stage) cudaFree(c->d_noise_stage);
+  for (cudaEvent_t ev : {c->ev_field_copied, c->ev_field_used, c->ev_noise_copied, c->ev_noise_used})
+    if (ev) cudaEventDestroy(ev);
+  if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
   if (c->d_sched) cudaFree(c->d_sched);
   if (c->d_tape) cudaFree(c->d_tape);
   if (c->d_tape_flag) cudaFree(c->d_tape_flag);
@@ -570,6 +576,53 @@ extern "C" vvlic_status vvlic_update_field_interp(vvlic_ctx* c, int32_t vol_id, 
   return reencode_volume(c, vol_id, *v, base + 2 * slot, dtype);
 }
 
+// Copy stream and events of the stream-ordered updates, created on first use.
+static vvlic_status ensure_async(vvlic_ctx* c) {
+  if (c->copy_stream) return VVLIC_OK;
+  cudaError_t e = cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking);
+  for (cudaEvent_t* ev : {&c->ev_field_copied, &c->ev_field_used, &c->ev_noise_copied, &c->ev_noise_used})
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+  if (e != cudaSuccess) return cuda_fail(c, e, "asynchronous update set-up");
+  return VVLIC_OK;
+}
+
+// A staging buffer of at least `bytes`; growing it first waits for the device (a copy or its
+// consumer may still use the old one).
+static vvlic_status grow_stage(vvlic_ctx* c, void** buf, size_t* cap, size_t bytes) {
+  if (*cap >= bytes) return VVLIC_OK;
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return cuda_fail(c, e, "staging");
+  return grow(c, buf, cap, bytes);
+}
+
+extern "C" vvlic_status vvlic_update_field_async(vvlic_ctx* c, int32_t vol_id, const void* xyz, int32_t dtype,
+                                                int32_t nx, int32_t ny, int32_t nz, void* stream) {
+  if (!c) return VVLIC_ERR_BAD_HANDLE;
+  if (!xyz) return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "update_field_async: null data");
+  Volume* v = nullptr;
+  vvlic_status st = update_target(c, vol_id, dtype, nx, ny, nz, "update_field_async", &v);
+  if (st) return st;
+  DeviceGuard g(c->device);
+  if ((st = ensure_async(c))) return st;
+  const size_t bytes = (size_t)nx * ny * nz * 3 * (dtype == VVLIC_DTYPE_FLOAT32 ? 4 : 1);
+  if ((st = grow_stage(c, &c->d_field_stage, &c->field_stage_cap, bytes))) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  // the copy overwrites the stage once the previous update's encoding has read it; the
+  // encoding on `stream` follows the copy and every render enqueued on `stream` before it
+  cudaError_t e = cudaStreamWaitEvent(c->copy_stream, c->ev_field_used, 0);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(c->d_field_stage, xyz, bytes, cudaMemcpyHostToDevice, c->copy_stream);
+  if (e == cudaSuccess) e = cudaEventRecord(c->ev_field_copied, c->copy_stream);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(s, c->ev_field_copied, 0);
+  if (e == cudaSuccess) e = launch_encode_field(c->d_field_stage, dtype, v->n, v->storage, v->d_texels, c->d_scratch_word, s);
+  if (e != cudaSuccess) return cuda_fail(c, e, "update_field_async");
+  if ((st = refresh_volume_layouts(c, *v, s))) return st;
+  e = cudaEventRecord(c->ev_field_used, s);
+  if (e != cudaSuccess) return cuda_fail(c, e, "update_field_async");
+  v->licvol_valid = false;
+  if (c->tape_vol == vol_id) c->tape_valid = false;
+  return VVLIC_OK;
+}
+
 extern "C" vvlic_status vvlic_upload_field_device(vvlic_ctx* c, const float* d_xyz, int32_t nx, int32_t ny, int32_t nz,
                                                  const float* slice_dist, int32_t storage, void* stream,
                                                  int32_t* vol_id) {
@@ -730,6 +783,51 @@ extern "C" vvlic_status vvlic_upload_noise_rgba(vvlic_ctx* c, const uint8_t* rgb
   e = cudaMemcpyAsync(n.d_texels, rgba, bytes, cudaMemcpyHostToDevice, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "upload_noise_rgba");
+  return VVLIC_OK;
+}
+
+extern "C" vvlic_status vvlic_upload_noise_async(vvlic_ctx* c, const uint8_t* noise, int32_t mx, int32_t my,
+                                                int32_t mz, int32_t mode, void* stream) {
+  if (!c) return VVLIC_ERR_BAD_HANDLE;
+  const int m[3] = {mx, my, mz};
+  if (!noise || !valid_dims(m)) return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "upload_noise_async: bad arguments");
+  if (mode < VVLIC_NOISE_SCALAR || mode > VVLIC_NOISE_GRAD_CENTRAL)
+    return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "upload_noise_async: mode %d", mode);
+  NoiseTex& n = c->noise;
+  const int ch = mode == VVLIC_NOISE_SCALAR ? 1 : 4;
+  if (!n.d_texels || n.m[0] != mx || n.m[1] != my || n.m[2] != mz || n.ch != ch)
+    return fail(c, VVLIC_ERR_NOT_READY,
+                "upload_noise_async: rewrites a noise of the same extent and channels in place; upload the first "
+                "one with vvlic_upload_noise");
+  DeviceGuard g(c->device);
+  vvlic_status st = ensure_async(c);
+  if (st) return st;
+  const size_t count = (size_t)mx * my * mz;
+  if ((st = grow_stage(c, &c->d_noise_stage, &c->noise_stage_cap,
+                       mode == VVLIC_NOISE_SCALAR ? count : noise_staging_bytes(count))))
+    return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e = cudaStreamWaitEvent(c->copy_stream, c->ev_noise_used, 0);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(c->d_noise_stage, noise, count, cudaMemcpyHostToDevice, c->copy_stream);
+  if (e == cudaSuccess) e = cudaEventRecord(c->ev_noise_copied, c->copy_stream);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(s, c->ev_noise_copied, 0);
+  if (e == cudaSuccess) {
+    if (mode == VVLIC_NOISE_SCALAR) {
+      e = cudaMemcpyAsync(n.d_texels, c->d_noise_stage, count, cudaMemcpyDeviceToDevice, s);
+    } else {
+      const float sd[3] = {1.f, 1.f, 1.f};
+      float w27[27];
+      noise_filter_weights(w27);
+      e = launch_noise_gradients((const uint8_t*)c->d_noise_stage, m, mode, sd,
+                                 (float*)((char*)c->d_noise_stage + noise_grad_offset(count)), n.d_texels, w27, s);
+    }
+  }
+  if (e != cudaSuccess) return cuda_fail(c, e, "upload_noise_async");
+  if ((st = refresh_noise_layouts(c, n, s))) return st;
+  e = cudaEventRecord(c->ev_noise_used, s);
+  if (e != cudaSuccess) return cuda_fail(c, e, "upload_noise_async");
+  n.mode = mode;
+  c->tape_valid = false;  // a recorded tape read the previous noise
   return VVLIC_OK;
 }
 

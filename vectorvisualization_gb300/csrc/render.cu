@@ -631,6 +631,30 @@ extern "C" vvlic_status vvlic_render(vvlic_ctx* c, int32_t vol_id, float* out, i
   return VVLIC_OK;
 }
 
+extern "C" vvlic_status vvlic_render_to_host_async(vvlic_ctx* c, int32_t vol_id, float* out, int32_t w, int32_t h,
+                                                  void* stream) {
+  if (!c) return VVLIC_ERR_BAD_HANDLE;
+  if (!out || w < 1 || h < 1 || w > 32768 || h > 32768)
+    return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "render_to_host_async: bad image arguments");
+  DeviceGuard g(c->device);
+  const size_t bytes = (size_t)w * h * 4 * sizeof(float);
+  if (c->image_cap < bytes) {
+    cudaError_t e = cudaDeviceSynchronize();  // a download in flight may still read the image
+    if (e != cudaSuccess) return cuda_fail(c, e, "render_to_host_async");
+    if (c->d_image) cudaFree(c->d_image);
+    c->d_image = nullptr;
+    c->image_cap = 0;
+    e = cudaMalloc(&c->d_image, bytes);
+    if (e != cudaSuccess) return cuda_fail(c, e, "image allocation");
+    c->image_cap = bytes;
+  }
+  vvlic_status st = vvlic_render_device(c, vol_id, (float*)c->d_image, w, h, nullptr, stream);
+  if (st) return st;
+  cudaError_t e = cudaMemcpyAsync(out, c->d_image, bytes, cudaMemcpyDeviceToHost, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "render_to_host_async");
+  return VVLIC_OK;
+}
+
 extern "C" vvlic_status vvlic_get_stats(vvlic_ctx* c, vvlic_stats* out) {
   if (!c) return VVLIC_ERR_BAD_HANDLE;
   if (!out) return VVLIC_ERR_INVALID_ARGUMENT;

@@ -114,6 +114,16 @@ struct vvlic_ctx {
   size_t image_cap = 0;
   void* d_upload = nullptr;
   size_t upload_cap = 0;
+  // stream-ordered updates (vvlic_update_field_async / vvlic_upload_noise_async): host copies
+  // run on copy_stream into their own staging buffers; the caller's stream waits for a copy
+  // (ev_*_copied) before consuming it, and the next copy waits until the consumer is done
+  // (ev_*_used)
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t ev_field_copied = nullptr, ev_field_used = nullptr, ev_noise_copied = nullptr, ev_noise_used = nullptr;
+  void* d_field_stage = nullptr;
+  size_t field_stage_cap = 0;
+  void* d_noise_stage = nullptr;
+  size_t noise_stage_cap = 0;
   unsigned* d_sched = nullptr;    // tile order scratch of the queue schedule
   size_t sched_cap = 0;           // in 4-byte words
   int num_sms = 1;
