@@ -467,7 +467,8 @@ typedef struct vvlic_job {
 } vvlic_job;
 
 /* Render n jobs in one persistent launch: every (job, 8x4 tile) item goes into one device work
- * queue ordered longest-first over the whole batch.  All jobs must share the field storage,
+ * queue in job-major order (jobs in submission order, each job's tiles in raster order), so the
+ * warps in flight share one or two volumes' texels in cache.  All jobs must share the field storage,
  * sampler, integrator and lighting (they are compiled variants); LIC length, step sizes,
  * filter, view, image size, TF index and the other runtime parameters may differ.  The noise,
  * scalar volume and transfer function are the context's.  The launch sequence is captured in a

@@ -1,4 +1,4 @@
-// Batched rendering: job table, longest-first (job, tile) order over the whole batch, the
+// Batched rendering: job table, job-major (job, tile) order over the whole batch, the
 // CUDA-graph-captured launch sequence and the tile-shape / sampler autotuner.
 #include <cuda_runtime.h>
 
@@ -16,8 +16,6 @@ using namespace vvlic;
 
 namespace vvlic_batch_order {
 
-constexpr int kBuckets = 1024;
-
 __device__ __forceinline__ int job_of(const unsigned* start, int njobs, unsigned g) {
   int lo = 0, hi = njobs - 1;  // largest j with start[j] <= g
   while (lo < hi) {
@@ -28,52 +26,16 @@ __device__ __forceinline__ int job_of(const unsigned* start, int njobs, unsigned
   return lo;
 }
 
-// One warp per (job, tile): cost = the tile's longest ray chord in samples.
-__global__ void batch_cost_kernel(const RenderArgs* jobs, const unsigned* start, int njobs, int ntiles, int tw,
-                                  int shift, unsigned* bucket, unsigned* hist) {
-  const int lane = threadIdx.x & 31, th = 32 / tw;
-  const int warps = gridDim.x * (blockDim.x >> 5);
-  for (int g = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); g < ntiles; g += warps) {
-    const int j = job_of(start, njobs, (unsigned)g);
-    const RenderArgs& a = jobs[j];
-    const int t = g - (int)start[j];
-    const int tiles_x = (a.W + tw - 1) / tw;
-    const int px = (t % tiles_x) * tw + lane % tw, py = (t / tiles_x) * th + lane / tw;
-    unsigned cost = 0;
-    float o[3], d[3], tn, tf;
-    if (px < a.W && py < a.H && ray_interval(a, px, py, o, d, tn, tf)) {
-      const float len = (tf - tn) * sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
-      // samples x streamline steps: jobs differ in L
-      cost = (unsigned)fminf((len / a.step_size + 1.0f) * (float)(a.lb + a.lf + 1), 4.0e9f);
-    }
-    cost = __reduce_max_sync(0xffffffffu, cost);
-    if (lane == 0) {
-      const unsigned b = kBuckets - 1 - min(cost >> shift, (unsigned)(kBuckets - 1));
-      bucket[g] = b;
-      atomicAdd(hist + b, 1u);
-    }
-  }
-}
-
-__global__ void bucket_scan_kernel(const unsigned* hist, unsigned* offsets) {
-  __shared__ unsigned s[kBuckets];
-  const int i = threadIdx.x;
-  s[i] = hist[i];
-  __syncthreads();
-  for (int d = 1; d < kBuckets; d <<= 1) {
-    unsigned v = i >= d ? s[i - d] : 0u;
-    __syncthreads();
-    s[i] += v;
-    __syncthreads();
-  }
-  offsets[i] = s[i] - hist[i];
-}
-
-__global__ void batch_scatter_kernel(const unsigned* start, int njobs, int ntiles, const unsigned* bucket,
-                                     unsigned* offsets, uint2* order) {
+// Item g of the batch: job j = the job whose tiles contain g, tile g - start[j].  Jobs run in
+// submission order and each job's tiles in raster order, so the warps in flight work on one or
+// two volumes at a time and share their texels in L1 and L2.  Measured on the 64-volume batch
+// (297 views at 512^2): 1065 ms per batch against 1252 ms for a longest-first order over all
+// (job, tile) items, which spreads the warps in flight over every volume; the tail this order
+// leaves is at most one job's last tiles.
+__global__ void batch_order_kernel(const unsigned* start, int njobs, int ntiles, uint2* order) {
   for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ntiles; g += gridDim.x * blockDim.x) {
     const int j = job_of(start, njobs, (unsigned)g);
-    order[atomicAdd(offsets + bucket[g], 1u)] = make_uint2((unsigned)j, (unsigned)g - start[j]);
+    order[g] = make_uint2((unsigned)j, (unsigned)g - start[j]);
   }
 }
 
@@ -81,16 +43,10 @@ __global__ void batch_scatter_kernel(const unsigned* start, int njobs, int ntile
 
 namespace vvlic {
 
-cudaError_t launch_batch_order(const RenderArgs* jobs, const BatchScratch& b, int njobs, int ntiles, int tw,
-                               int shift, cudaStream_t s) {
+cudaError_t launch_batch_order(const BatchScratch& b, int njobs, int ntiles, cudaStream_t s) {
   using namespace vvlic_batch_order;
-  cudaError_t e = cudaMemsetAsync(b.hist, 0, kBuckets * sizeof(unsigned), s);
-  if (e != cudaSuccess) return e;
-  const int blocks = std::max(1, std::min((ntiles + 7) / 8, 152 * 16));
-  batch_cost_kernel<<<blocks, 256, 0, s>>>(jobs, b.start, njobs, ntiles, tw, shift, b.bucket, b.hist);
-  bucket_scan_kernel<<<1, kBuckets, 0, s>>>(b.hist, b.offsets);
-  batch_scatter_kernel<<<std::max(1, std::min((ntiles + 255) / 256, 152 * 8)), 256, 0, s>>>(b.start, njobs, ntiles,
-                                                                                            b.bucket, b.offsets, b.order);
+  batch_order_kernel<<<std::max(1, std::min((ntiles + 255) / 256, 152 * 8)), 256, 0, s>>>(b.start, njobs, ntiles,
+                                                                                          b.order);
   return cudaGetLastError();
 }
 
@@ -127,7 +83,7 @@ cudaError_t launch_batch(int storage, const BatchLaunch& b, int sampler, int int
 // Validates the jobs, builds their argument blocks into the pinned staging table and the
 // per-job tile starts; returns the batch-wide variant and the tile count.
 vvlic_status prepare_batch(vvlic_ctx* c, const vvlic_job* jobs, int n, int tw, int sampler_override, cudaStream_t s,
-                           int* storage, int* sampler, int* integ, bool* grad, int* ntiles, double* maxcost,
+                           int* storage, int* sampler, int* integ, bool* grad, int* ntiles,
                            std::vector<unsigned>& start) {
   if (!jobs || n < 1 || n > 65536) return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "batch: need 1..65536 jobs");
   // the staging table may still be in flight from the previous batch
@@ -143,7 +99,6 @@ vvlic_status prepare_batch(vvlic_ctx* c, const vvlic_job* jobs, int n, int tw, i
   }
   start.assign(n + 1, 0);
   double total = 0.0;
-  *maxcost = 1.0;
   for (int j = 0; j < n; ++j) {
     const vvlic_job& jb = jobs[j];
     auto it = c->vols.find(jb.vol_id);
@@ -183,10 +138,6 @@ vvlic_status prepare_batch(vvlic_ctx* c, const vvlic_job* jobs, int n, int tw, i
     start[j] = (unsigned)total;
     total += tiles;
     if (total > 4.0e9) return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "batch: too many tiles");
-    const Geometry& gm = it->second.geom;
-    const double diag = std::sqrt((double)gm.extent[0] * gm.extent[0] + (double)gm.extent[1] * gm.extent[1] +
-                                  (double)gm.extent[2] * gm.extent[2]);
-    *maxcost = std::max(*maxcost, (diag / a.step_size + 2.0) * (a.lb + a.lf + 1));
   }
   start[n] = (unsigned)total;
   *ntiles = (int)total;
@@ -200,10 +151,9 @@ vvlic_status prepare_batch(vvlic_ctx* c, const vvlic_job* jobs, int n, int tw, i
 vvlic_status batch_render(vvlic_ctx* c, const vvlic_job* jobs, int n, cudaStream_t s, int tw, int sampler_override) {
   int storage, sampler, integ, ntiles;
   bool grad;
-  double maxcost;
   std::vector<unsigned> start;
   vvlic_status st = prepare_batch(c, jobs, n, tw, sampler_override, s, &storage, &sampler, &integ, &grad, &ntiles,
-                                  &maxcost, start);
+                                  start);
   if (st) return st;
   // device buffers; a reallocation invalidates the captured graph
   const void* old_jobs = c->d_jobs;
@@ -226,10 +176,8 @@ vvlic_status batch_render(vvlic_ctx* c, const vvlic_job* jobs, int n, cudaStream
     if (e == cudaSuccess) e = cudaEventRecord(c->ev_jobs, s);
   }
   if (e != cudaSuccess) return cuda_fail(c, e, "batch upload");
-  int shift = 0;
-  while ((maxcost / (double)(1ull << shift)) >= 1024.0 && shift < 40) ++shift;
   const uint64_t key[8] = {(uint64_t)n, (uint64_t)ntiles, (uint64_t)storage, (uint64_t)sampler, (uint64_t)integ,
-                           (uint64_t)grad, (uint64_t)tw, (uint64_t)shift};
+                           (uint64_t)grad, (uint64_t)tw, 0};
   if (!c->batch_graph || std::memcmp(key, c->batch_key, sizeof key) != 0) {
     drop_graph(c);
     // capture: counters reset, order pass, queue reset, the persistent launch
@@ -237,7 +185,7 @@ vvlic_status batch_render(vvlic_ctx* c, const vvlic_job* jobs, int n, cudaStream
     e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return cuda_fail(c, e, "batch graph capture (a non-default stream is required)");
     cudaError_t ec = cudaMemsetAsync(c->d_counters, 0, 4 * sizeof(unsigned long long), s);
-    if (ec == cudaSuccess) ec = launch_batch_order(c->d_jobs, bs, n, ntiles, tw, shift, s);
+    if (ec == cudaSuccess) ec = launch_batch_order(bs, n, ntiles, s);
     if (ec == cudaSuccess) ec = cudaMemsetAsync(bs.next, 0, sizeof(unsigned), s);
     if (ec == cudaSuccess) {
       BatchLaunch b{c->d_jobs, bs.order, ntiles, bs.next, c->d_tf, c->d_counters, tw, c->num_sms};

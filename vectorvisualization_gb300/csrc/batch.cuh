@@ -1,6 +1,6 @@
 // Batched LIC ray-cast: many render jobs (volume x view x image, each with its own LIC
 // parameters and filter) in one persistent launch.  Warps pull (job, tile) items from one
-// device work queue ordered longest-first over all jobs; on a job switch a warp copies that
+// device work queue in job-major order (batch.cu); on a job switch a warp copies that
 // job's argument block into its own shared-memory slot and traces the tile from there.  The
 // transfer function is the context's and is shared by every job.
 #pragma once

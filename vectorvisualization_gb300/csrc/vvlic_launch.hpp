@@ -92,10 +92,9 @@ inline BatchScratch batch_scratch(unsigned* base, int njobs, int ntiles) {
   b.words = s0 + nb + 2 * (size_t)ntiles + 2048 + 2;
   return b;
 }
-// Longest-first (job, tile) order over a batch (batch.cu); start[] holds njobs+1 entries
+// Job-major (job, tile) order over a batch (batch.cu); start[] holds njobs+1 entries
 // (exclusive prefix of tiles per job).
-cudaError_t launch_batch_order(const RenderArgs* jobs, const BatchScratch& b, int njobs, int ntiles, int tw,
-                               int shift, cudaStream_t s);
+cudaError_t launch_batch_order(const BatchScratch& b, int njobs, int ntiles, cudaStream_t s);
 
 // Longest-first tile order for the queue schedule (render.cu): per-tile chord cost, a
 // counting sort over 1024 cost buckets, scatter.  `scratch` holds 2*ntiles + 2048 + 1 words.
