@@ -22,10 +22,23 @@ namespace vvlic {
 
 // Minimum resident CTAs per SM requested for the adjoint kernels (register cap 65536 / (128 * n)):
 // 6 (80 registers, a few spilled bytes) measured 1786 ms against 1951 ms for 5 (93 registers)
-// on the lit 512^3 RK4 frame.
+// on the lit 512^3 RK4 frame with one sample per pass and one warp butterfly per tap sum.
 #ifndef VVLIC_ADJ_MIN_BLOCKS
 #define VVLIC_ADJ_MIN_BLOCKS 6
 #endif
+// Samples whose streamlines one thread re-walks together in the RK4 adjoint: 1 or 2 (four
+// independent gather chains, as the forward's trace_pixel2).  On frames 0 / 40 of the lit 512^3
+// RK4 orbit (2048^2) the adjoint took 1309 / 1532 ms with two samples at 6 CTAs per SM (80
+// registers, 100 spilled bytes), 1335 / 1550 ms at 5 (96 registers), 1353 / 1579 ms at 4 (127
+// registers) and 1518 / 1762 ms with one sample at 6.  Two samples per pass measured slower for
+// the Heun forward, so the other integrators keep one.
+#ifndef VVLIC_ADJ_RK4_SAMPLES_PER_PASS
+#define VVLIC_ADJ_RK4_SAMPLES_PER_PASS 2
+#endif
+
+template <int INTEG> __host__ __device__ constexpr int adj_samples_per_pass() {
+  return INTEG == VVLIC_RK4 ? VVLIC_ADJ_RK4_SAMPLES_PER_PASS : 1;
+}
 
 constexpr float kFixedScale = 1073741824.0f;  // 2^30
 constexpr int kAccTF = 0, kAccOpac = 4 * VVLIC_TF_ENTRIES, kAccTaps = 5 * VVLIC_TF_ENTRIES;
@@ -40,6 +53,19 @@ __device__ __forceinline__ void warp_fixed_add(long long* slot, float v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   if ((threadIdx.x & 31) == 0) fixed_add(slot, v);
+}
+
+// Two warp sums in five shuffles (fixed order): the first exchange leaves lanes 0-15 holding
+// pair sums of `va` and lanes 16-31 pair sums of `vb`; each half then reduces on its own.  Lane 0
+// adds the sum of `va` to slot_a (when use_a), lane 16 the sum of `vb` to slot_b (when use_b).
+__device__ __forceinline__ void warp_fixed_add2(long long* slot_a, bool use_a, float va, long long* slot_b, bool use_b,
+                                                float vb) {
+  const int lane = threadIdx.x & 31;
+  const bool lo = lane < 16;
+  float x = (lo ? va : vb) + __shfl_xor_sync(0xffffffffu, lo ? vb : va, 16);
+#pragma unroll
+  for (int o = 8; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+  if ((lane == 0 && use_a) || (lane == 16 && use_b)) fixed_add(lo ? slot_a : slot_b, x);
 }
 
 // 1D LINEAR + CLAMP_TO_EDGE lookup decomposed: entries i0, i1, weight t of i1, and whether the
@@ -184,9 +210,145 @@ __device__ __forceinline__ void tap_gradients(const RenderArgs& a, float3 pos, f
         vf = tap_dot<ST, FL, NL, INTEG, GRAD>(noise_tap<NL, GRAD>(a, pf), gI, gG);
       }
     }
-    if (i <= lb) warp_fixed_add(s_taps + lb - i, vb);
-    if (i <= lf) warp_fixed_add(s_taps + lb + i, vf);
+    warp_fixed_add2(s_taps + lb - i, i <= lb, vb, s_taps + lb + i, i <= lf, vf);
   }
+}
+
+// tap_gradients of two samples at once: four independent streamline chains per thread, and
+// per tap the two samples' contributions are added in the lane before the warp sum.  A lane
+// walks both samples' streamlines when either has a non-zero cotangent; the other sample's
+// terms are then zero (its cotangents are zero and its noise values finite).
+template <int ST, int FL, int NL, int INTEG, bool GRAD>
+__device__ __forceinline__ void tap_gradients2(const RenderArgs& a, float3 pa, float gIa, float3 gGa, float3 pc,
+                                               float gIc, float3 gGc, long long* s_taps) {
+  const bool act = gIa != 0.0f || gIc != 0.0f ||
+                   (GRAD && (gGa.x != 0.0f || gGa.y != 0.0f || gGa.z != 0.0f || gGc.x != 0.0f || gGc.y != 0.0f ||
+                             gGc.z != 0.0f));
+  const int lb = a.lb, lf = a.lf, L = max(lb, lf);
+  float4 fa = make_float4(0.f, 0.f, 0.f, 0.f), fc = fa;
+  float v0 = 0.0f;
+  if (act) {
+    fa = Field<ST, FL>::sample(a, pa);
+    fc = Field<ST, FL>::sample(a, pc);
+    v0 = tap_dot<ST, FL, NL, INTEG, GRAD>(noise_tap<NL, GRAD>(a, pa), gIa, gGa) +
+         tap_dot<ST, FL, NL, INTEG, GRAD>(noise_tap<NL, GRAD>(a, pc), gIc, gGc);
+  }
+  warp_fixed_add(s_taps + lb, v0);
+  float3 p0 = pa, p1 = pa, p2 = pc, p3 = pc;
+  float4 s0 = fa, s1 = fa, s2 = fc, s3 = fc;
+  const int both = min(lb, lf);
+  int i = 1;
+  for (; i <= both; ++i) {
+    float vb = 0.0f, vf = 0.0f;
+    if (act) {
+      p0 = lic_step<ST, FL, INTEG>(a, p0, s0, -1.0f);
+      p1 = lic_step<ST, FL, INTEG>(a, p1, s1, 1.0f);
+      p2 = lic_step<ST, FL, INTEG>(a, p2, s2, -1.0f);
+      p3 = lic_step<ST, FL, INTEG>(a, p3, s3, 1.0f);
+      vb = tap_dot<ST, FL, NL, INTEG, GRAD>(noise_tap<NL, GRAD>(a, p0), gIa, gGa) +
+           tap_dot<ST, FL, NL, INTEG, GRAD>(noise_tap<NL, GRAD>(a, p2), gIc, gGc);
+      vf = tap_dot<ST, FL, NL, INTEG, GRAD>(noise_tap<NL, GRAD>(a, p1), gIa, gGa) +
+           tap_dot<ST, FL, NL, INTEG, GRAD>(noise_tap<NL, GRAD>(a, p3), gIc, gGc);
+    }
+    warp_fixed_add2(s_taps + lb - i, true, vb, s_taps + lb + i, true, vf);
+  }
+  for (; i <= L; ++i) {
+    float vb = 0.0f, vf = 0.0f;
+    if (act) {
+      if (i <= lb) {
+        p0 = lic_step<ST, FL, INTEG>(a, p0, s0, -1.0f);
+        p2 = lic_step<ST, FL, INTEG>(a, p2, s2, -1.0f);
+        vb = tap_dot<ST, FL, NL, INTEG, GRAD>(noise_tap<NL, GRAD>(a, p0), gIa, gGa) +
+             tap_dot<ST, FL, NL, INTEG, GRAD>(noise_tap<NL, GRAD>(a, p2), gIc, gGc);
+      }
+      if (i <= lf) {
+        p1 = lic_step<ST, FL, INTEG>(a, p1, s1, 1.0f);
+        p3 = lic_step<ST, FL, INTEG>(a, p3, s3, 1.0f);
+        vf = tap_dot<ST, FL, NL, INTEG, GRAD>(noise_tap<NL, GRAD>(a, p1), gIa, gGa) +
+             tap_dot<ST, FL, NL, INTEG, GRAD>(noise_tap<NL, GRAD>(a, p3), gIc, gGc);
+      }
+    }
+    warp_fixed_add2(s_taps + lb - i, i <= lb, vb, s_taps + lb + i, i <= lf, vf);
+  }
+}
+
+// Reverse step through one sample (kk of segment seg): clamp, blend, alpha correction, opacity
+// and TF lookups and the shading, from the recomputed compositing state Dloc[kk].  Adds the TF
+// and opacity cotangents to the block accumulators, updates the image cotangent g to the one
+// before the sample and returns the cotangents of the sample's LIC intensity (gIraw, already
+// scaled by the intensity scale) and gradient sum (gG), and its position.  Samples at or past
+// cnt leave everything zero.
+template <int ST, int FL, bool GRAD>
+__device__ __forceinline__ void sample_cotangent(const RenderArgs& a, const float* s_tf, bool line, float3 dir,
+                                                 const float4* Dloc, const float3* Ploc, int px, int py, int seg,
+                                                 int kk, int cnt, float4& g, long long* s_acc, float& gIraw,
+                                                 float3& gG, float3& pk) {
+  gIraw = 0.0f;
+  gG = f3(0.f, 0.f, 0.f);
+  pk = f3(0.f, 0.f, 0.f);
+  if (kk < 0 || kk >= cnt) return;
+  const size_t idx = tape_entry_checked(a, px, py, seg * kSegment + kk);
+  const float2 rec = a.tape_is[idx];
+  const float I = rec.x;
+  Src s = unlit_source(a, s_tf, I, rec.y);
+  LitT lt;
+  float3 ld = f3(0.f, 0.f, 0.f);
+  if (GRAD) {
+    lt = lit_setup(a, tape_gradient(a, idx), Ploc[kk], dir);
+    s.col = lit_color(a, lt, s.tf, I);
+  } else if (line) {  // colour = tf.rgb * I * d + s (d, s independent of TF, taps and I)
+    float3 sf;
+    line_factors(a, Ploc[kk], dir, Field<ST, FL>::sample(a, Ploc[kk]), ld, sf);
+    s.col = f3(s.tf.x * I * ld.x + sf.x, s.tf.y * I * ld.y + sf.y, s.tf.z * I * ld.z + sf.z);
+  }
+  const float4 sv = premultiplied(s);
+  const float4 Dp = Dloc[kk];
+  pk = Ploc[kk];
+  const float om = 1.0f - Dp.w;
+  // clamp((1 - Dp.a) * s + Dp) per channel: derivative 1 on [0, 1]
+  const float ux = fmaf(om, sv.x, Dp.x), uy = fmaf(om, sv.y, Dp.y), uz = fmaf(om, sv.z, Dp.z),
+              uw = fmaf(om, sv.w, Dp.w);
+  const float gx = (ux >= 0.f && ux <= 1.f) ? g.x : 0.f, gy = (uy >= 0.f && uy <= 1.f) ? g.y : 0.f,
+              gz = (uz >= 0.f && uz <= 1.f) ? g.z : 0.f, gw = (uw >= 0.f && uw <= 1.f) ? g.w : 0.f;
+  const float4 ds = make_float4(om * gx, om * gy, om * gz, om * gw);
+  float4 gp = make_float4(gx, gy, gz, gw);
+  gp.w -= gx * sv.x + gy * sv.y + gz * sv.z + gw * sv.w;
+  // s = (col * alpha, alpha)
+  const float dcx = ds.x * s.alpha, dcy = ds.y * s.alpha, dcz = ds.z * s.alpha;
+  const float dalpha = ds.x * s.col.x + ds.y * s.col.y + ds.z * s.col.z + ds.w;
+  const float dba = s.base > 0.0f ? a.alpha_corr * powf(s.base, a.alpha_corr - 1.0f) : 0.0f;
+  const float da0 = dalpha * dba;
+  // a0 = opacity(1.3 I) * tf.a
+  const float dop = da0 * s.tf.w, dtfa = da0 * s.op;
+  fixed_add(s_acc + kAccOpac + s.lo.i0, dop * (1.0f - s.lo.t));
+  fixed_add(s_acc + kAccOpac + s.lo.i1, dop * s.lo.t);
+  const float* op = s_tf + 4 * VVLIC_TF_ENTRIES;
+  float dI = s.lo.inside ? dop * (op[s.lo.i1] - op[s.lo.i0]) * (float)VVLIC_TF_ENTRIES * 1.3f : 0.0f;
+  float dtf[4];
+  dtf[3] = dtfa;
+  if (GRAD) {
+    float dIc;
+    lit_vjp(a, lt, s.tf, I, f3(dcx, dcy, dcz), dtf, &dIc, &gG);
+    dI += dIc;
+  } else if (line) {
+    dtf[0] = dcx * I * ld.x;
+    dtf[1] = dcy * I * ld.y;
+    dtf[2] = dcz * I * ld.z;
+    dI += dcx * s.tf.x * ld.x + dcy * s.tf.y * ld.y + dcz * s.tf.z * ld.z;
+  } else {  // col = I * tf.rgb * illumScale
+    const float ci = I * a.illum_scale;
+    dtf[0] = dcx * ci;
+    dtf[1] = dcy * ci;
+    dtf[2] = dcz * ci;
+    dI += (dcx * s.tf.x + dcy * s.tf.y + dcz * s.tf.z) * a.illum_scale;
+  }
+#pragma unroll
+  for (int ch = 0; ch < 4; ++ch) {
+    fixed_add(s_acc + kAccTF + 4 * s.lt.i0 + ch, dtf[ch] * (1.0f - s.lt.t));
+    fixed_add(s_acc + kAccTF + 4 * s.lt.i1 + ch, dtf[ch] * s.lt.t);
+  }
+  gIraw = dI * a.intensity_scale;
+  g = gp;
 }
 
 template <int ST, int FL, int NL, int INTEG, bool GRAD>
@@ -256,76 +418,22 @@ __global__ void __launch_bounds__(kThreads, VVLIC_ADJ_MIN_BLOCKS) adjoint_kernel
           p = add3(p, scl3(dir, a.step_size));
         }
       }
-      for (int kk = kSegment - 1; kk >= 0; --kk) {
-        float gIraw = 0.0f;
-        float3 gG = f3(0.f, 0.f, 0.f);
-        float3 pk = f3(0.f, 0.f, 0.f);
-        if (kk < cnt) {
-          const size_t idx = tape_entry_checked(a, px, py, seg * kSegment + kk);
-          const float2 rec = a.tape_is[idx];
-          const float I = rec.x;
-          Src s = unlit_source(a, s_tf, I, rec.y);
-          LitT lt;
-          float3 ld = f3(0.f, 0.f, 0.f);
-          if (GRAD) {
-            lt = lit_setup(a, tape_gradient(a, idx), Ploc[kk], dir);
-            s.col = lit_color(a, lt, s.tf, I);
-          } else if (line) {  // colour = tf.rgb * I * d + s (d, s independent of TF, taps and I)
-            float3 sf;
-            line_factors(a, Ploc[kk], dir, Field<ST, FL>::sample(a, Ploc[kk]), ld, sf);
-            s.col = f3(s.tf.x * I * ld.x + sf.x, s.tf.y * I * ld.y + sf.y, s.tf.z * I * ld.z + sf.z);
-          }
-          const float4 sv = premultiplied(s);
-          const float4 Dp = Dloc[kk];
-          pk = Ploc[kk];
-          const float om = 1.0f - Dp.w;
-          // clamp((1 - Dp.a) * s + Dp) per channel: derivative 1 on [0, 1]
-          const float ux = fmaf(om, sv.x, Dp.x), uy = fmaf(om, sv.y, Dp.y), uz = fmaf(om, sv.z, Dp.z),
-                      uw = fmaf(om, sv.w, Dp.w);
-          const float gx = (ux >= 0.f && ux <= 1.f) ? g.x : 0.f, gy = (uy >= 0.f && uy <= 1.f) ? g.y : 0.f,
-                      gz = (uz >= 0.f && uz <= 1.f) ? g.z : 0.f, gw = (uw >= 0.f && uw <= 1.f) ? g.w : 0.f;
-          const float4 ds = make_float4(om * gx, om * gy, om * gz, om * gw);
-          float4 gp = make_float4(gx, gy, gz, gw);
-          gp.w -= gx * sv.x + gy * sv.y + gz * sv.z + gw * sv.w;
-          // s = (col * alpha, alpha)
-          const float dcx = ds.x * s.alpha, dcy = ds.y * s.alpha, dcz = ds.z * s.alpha;
-          const float dalpha = ds.x * s.col.x + ds.y * s.col.y + ds.z * s.col.z + ds.w;
-          const float dba = s.base > 0.0f ? a.alpha_corr * powf(s.base, a.alpha_corr - 1.0f) : 0.0f;
-          const float da0 = dalpha * dba;
-          // a0 = opacity(1.3 I) * tf.a
-          const float dop = da0 * s.tf.w, dtfa = da0 * s.op;
-          fixed_add(s_acc + kAccOpac + s.lo.i0, dop * (1.0f - s.lo.t));
-          fixed_add(s_acc + kAccOpac + s.lo.i1, dop * s.lo.t);
-          const float* op = s_tf + 4 * VVLIC_TF_ENTRIES;
-          float dI = s.lo.inside ? dop * (op[s.lo.i1] - op[s.lo.i0]) * (float)VVLIC_TF_ENTRIES * 1.3f : 0.0f;
-          float dtf[4];
-          dtf[3] = dtfa;
-          if (GRAD) {
-            float dIc;
-            lit_vjp(a, lt, s.tf, I, f3(dcx, dcy, dcz), dtf, &dIc, &gG);
-            dI += dIc;
-          } else if (line) {
-            dtf[0] = dcx * I * ld.x;
-            dtf[1] = dcy * I * ld.y;
-            dtf[2] = dcz * I * ld.z;
-            dI += dcx * s.tf.x * ld.x + dcy * s.tf.y * ld.y + dcz * s.tf.z * ld.z;
-          } else {  // col = I * tf.rgb * illumScale
-            const float ci = I * a.illum_scale;
-            dtf[0] = dcx * ci;
-            dtf[1] = dcy * ci;
-            dtf[2] = dcz * ci;
-            dI += (dcx * s.tf.x + dcy * s.tf.y + dcz * s.tf.z) * a.illum_scale;
-          }
-#pragma unroll
-          for (int ch = 0; ch < 4; ++ch) {
-            fixed_add(s_acc + kAccTF + 4 * s.lt.i0 + ch, dtf[ch] * (1.0f - s.lt.t));
-            fixed_add(s_acc + kAccTF + 4 * s.lt.i1 + ch, dtf[ch] * s.lt.t);
-          }
-          gIraw = dI * a.intensity_scale;
-          g = gp;
+      for (int kk = kSegment - 1; kk >= 0; kk -= adj_samples_per_pass<INTEG>()) {
+        float gIraw;
+        float3 gG, pk;
+        sample_cotangent<ST, FL, GRAD>(a, s_tf, line, dir, Dloc, Ploc, px, py, seg, kk, cnt, g, s_acc, gIraw, gG, pk);
+        bool need = gIraw != 0.0f || (GRAD && (gG.x != 0.0f || gG.y != 0.0f || gG.z != 0.0f));
+        if constexpr (adj_samples_per_pass<INTEG>() == 2) {
+          float gIraw1;
+          float3 gG1, pk1;
+          sample_cotangent<ST, FL, GRAD>(a, s_tf, line, dir, Dloc, Ploc, px, py, seg, kk - 1, cnt, g, s_acc, gIraw1,
+                                         gG1, pk1);
+          need = need || gIraw1 != 0.0f || (GRAD && (gG1.x != 0.0f || gG1.y != 0.0f || gG1.z != 0.0f));
+          if (__any_sync(0xffffffffu, need))
+            tap_gradients2<ST, FL, NL, INTEG, GRAD>(a, pk, gIraw, gG, pk1, gIraw1, gG1, s_acc + kAccTaps);
+        } else {
+          if (__any_sync(0xffffffffu, need)) tap_gradients<ST, FL, NL, INTEG, GRAD>(a, pk, gIraw, gG, s_acc + kAccTaps);
         }
-        const bool need = gIraw != 0.0f || (GRAD && (gG.x != 0.0f || gG.y != 0.0f || gG.z != 0.0f));
-        if (__any_sync(0xffffffffu, need)) tap_gradients<ST, FL, NL, INTEG, GRAD>(a, pk, gIraw, gG, s_acc + kAccTaps);
       }
     }
   }
