@@ -14,8 +14,9 @@ from vectorvisualization_gb300 import capi, workloads as wl
 pytestmark = pytest.mark.gpu
 
 
-def case(size=24, image=32, L=6, sampler="cell", storage="f32", lit=False):
+def case(size=24, image=32, L=6, sampler="cell", storage="f32", lit=False, integrator=capi.HEUN):
     w = wl.c4(size=size, image=image, views=1)
+    w.params.integrator = integrator
     w.params.steps_forward = w.params.steps_backward = L
     w.params.step_size_vol = 1.0 / 48.0
     w.params.gradient_scale = 8.0
@@ -70,8 +71,8 @@ def target_image(oracle, w, taps, storage="f32"):
                                                  ("gather", "f32", False), ("cell", "f32", "gradient"),
                                                  ("hybrid", "f16", "gradient"), ("cell", "f32", "zoeckler"),
                                                  ("cell", "f32", "mallo"), ("hybrid", "bf16", False)])
-def test_adjoint_matches_fp64_oracle(ctx, oracle, sampler, storage, lit):
-    w, taps = case(sampler=sampler, storage=storage, lit=lit)
+def test_adjoint_matches_fp64_oracle(ctx, oracle, sampler, storage, lit, integrator=capi.HEUN, L=6):
+    w, taps = case(sampler=sampler, storage=storage, lit=lit, integrator=integrator, L=L)
     target = target_image(oracle, w, taps, storage)
     vid, img, d_tf, d_op, d_taps = gpu_forward_adjoint(ctx, w, taps, target)
     enc = oracle.encode_field(w.field)
@@ -107,8 +108,19 @@ def test_adjoint_matches_fp64_oracle(ctx, oracle, sampler, storage, lit):
     assert float(np.abs(r_taps).max()) > 0 and float(np.abs(r_tf).max()) > 0
 
 
-def test_adjoint_is_deterministic(ctx, oracle):
-    w, taps = case(sampler="hybrid", storage="f16")
+# RK4 re-walks two samples' streamlines per pass in the adjoint (the other integrators one); odd
+# and even L, lit and unlit, exact and hardware-filtered samplers
+@pytest.mark.parametrize("sampler,storage,lit,integrator,L", [
+    ("cell", "f32", False, capi.RK4, 6), ("cell", "f32", "gradient", capi.RK4, 5),
+    ("hybrid", "f16", "gradient", capi.RK4, 7), ("gather", "f32", "mallo", capi.RK4, 4),
+    ("cell", "f32", False, capi.EULER, 9), ("cell", "f32", "gradient", capi.EULER, 6)])
+def test_adjoint_integrators_match_fp64_oracle(ctx, oracle, sampler, storage, lit, integrator, L):
+    test_adjoint_matches_fp64_oracle(ctx, oracle, sampler, storage, lit, integrator, L)
+
+
+@pytest.mark.parametrize("integrator", [capi.HEUN, capi.RK4])
+def test_adjoint_is_deterministic(ctx, oracle, integrator):
+    w, taps = case(sampler="hybrid", storage="f16", lit="gradient", integrator=integrator)
     target = target_image(oracle, w, taps, "f16")
     a = gpu_forward_adjoint(ctx, w, taps, target)
     b = gpu_forward_adjoint(ctx, w, taps, target)
@@ -116,11 +128,12 @@ def test_adjoint_is_deterministic(ctx, oracle):
         np.testing.assert_array_equal(x, y)
 
 
-@pytest.mark.parametrize("lit", [False, "gradient", "mallo"])
-def test_adjoint_matches_gpu_finite_differences(ctx, oracle, lit):
+@pytest.mark.parametrize("lit,integrator", [(False, capi.HEUN), ("gradient", capi.HEUN), ("mallo", capi.HEUN),
+                                             ("gradient", capi.RK4)])
+def test_adjoint_matches_gpu_finite_differences(ctx, oracle, lit, integrator):
     import torch
 
-    w, taps = case(size=32, image=40, L=8, lit=lit)
+    w, taps = case(size=32, image=40, L=8, lit=lit, integrator=integrator)
     target = target_image(oracle, w, taps)
     vid, img, d_tf, d_op, d_taps = gpu_forward_adjoint(ctx, w, taps, target)
     p = w.params

@@ -307,7 +307,7 @@ def test_row_subset_matches_full(oracle):
 # ---------------------------------------------------------------------------------------------
 # the FP64 adjoint against central finite differences of the FP64 forward
 # ---------------------------------------------------------------------------------------------
-def _adjoint_case(oracle, lit=False):
+def _adjoint_case(oracle, lit=False, integrator=capi.HEUN):
     w = wl.c1(size=12, image=14)
     w.field = wl.vortex_field((12, 12, 12), seed=6)
     w.noise = wl.dense_noise(12, seed=61)
@@ -318,7 +318,7 @@ def _adjoint_case(oracle, lit=False):
     elif lit:
         w.params.illum = {"zoeckler": capi.ILLUM_ZOECKLER, "mallo": capi.ILLUM_MALLO}[lit]
         w.params.light_pos[:] = (0.2, 1.4, 1.1)
-    w.params.integrator = capi.HEUN
+    w.params.integrator = integrator
     w.params.steps_forward = w.params.steps_backward = 4
     w.params.gradient_scale = 6.0
     w.params.step_size_vol = 1.0 / 24.0
@@ -335,9 +335,11 @@ def _adjoint_case(oracle, lit=False):
     return w, view, enc, rgba, op, taps, target, render
 
 
-@pytest.mark.parametrize("lit", [False, "gradient", "zoeckler", "mallo"])
-def test_oracle_adjoint_matches_finite_differences(oracle, lit):
-    w, view, enc, rgba, op, taps, target, render = _adjoint_case(oracle, lit)
+@pytest.mark.parametrize("lit,integrator", [(False, capi.HEUN), ("gradient", capi.HEUN), ("zoeckler", capi.HEUN),
+                                             ("mallo", capi.HEUN), (False, capi.RK4), ("gradient", capi.RK4),
+                                             ("gradient", capi.EULER)])
+def test_oracle_adjoint_matches_finite_differences(oracle, lit, integrator):
+    w, view, enc, rgba, op, taps, target, render = _adjoint_case(oracle, lit, integrator)
     img, sc = render(rgba, op, taps)
     g = (2.0 * (img - target)).astype(np.float32)
     d_tf, d_op, d_taps = oracle.adjoint(sc, w.params, view, w.width, w.height, g)
