@@ -63,6 +63,8 @@ def parse():
     ap.add_argument("--no-c3", action="store_true", help="skip the 64-volume batch")
     ap.add_argument("--no-c4", action="store_true", help="skip the differentiable-fit forward+adjoint")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the orbit's forward+adjoint")
+    ap.add_argument("--no-rows", action="store_true",
+                    help="skip the techniques and preprocessing beside the ray-cast (on the orbit's volume)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-ceiling", action="store_true", help="skip the L1TEX fetch-ceiling measurement")
@@ -574,6 +576,128 @@ def bench_orbit_adjoint(ctx, torch, stream, flush, w, vid, out, frame):
             "grad_norms": {"tf": float(d_tf.norm()), "opacity": float(d_op.norm()), "taps": float(d_taps.norm())}}
 
 
+def bench_rows(ctx, torch, stream, flush, w, vid, ceiling, frame, args):
+    """The techniques and preprocessing beside the ray-cast, on the orbit's field, noise and
+    parameters (512^3, RK4 L = 60 each way, 2048^2, orbit frame `frame`), each timed with CUDA
+    events after a warm-up and an L2 flush, against the bound that applies:
+      licvolume_precompute  vvlic_compute_lic_volume at 512^3 voxels (the reference's size): one
+                            LIC per voxel, the ray-cast's fetch groups -> L1TEX fetch ceiling;
+      licvolume_dvr         the LIC-volume ray-cast: one trilinear field fetch + one 8-load
+                            gather of the LIC volume per sample -> texture fetch rate;
+      vector_dvr            the vector-field DVR: one trilinear field fetch per sample;
+      slicing               LIC on view-aligned slices -> L1TEX fetch ceiling;
+      field_update_device   vvlic_update_field_device of the float32 field (encode + texture
+                            copy) -> HBM;
+      noise_gradients       vvlic_noise_gradients_device of the 512^3 noise -> HBM."""
+    from vectorvisualization_gb300 import capi
+
+    W, H = w.width, w.height
+    sh = stream.cuda_stream
+    p = capi.Params.from_buffer_copy(w.params)
+    peak_hbm, hbm_kind = load_peaks()
+    tex_peak = ceiling["tex_per_s"] / 1e9 if ceiling else None
+    out = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+    ctx.set_view(w.views[frame])
+    res = {"frame": frame}
+
+    def settle():
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        torch.cuda.synchronize()
+
+    # LIC-volume precompute (synchronous on the context's stream; its stats carry the kernel time)
+    n = args.size
+    ctx.set_params(p)
+    ctx.compute_lic_volume(vid, (n, n, n))
+    settle()
+    ctx.compute_lic_volume(vid, (n, n, n))
+    st = ctx.stats()
+    res["licvolume_precompute"] = {
+        "voxels": int(st.samples), "kernel_ms": st.kernel_ms,
+        "gss": st.sample_steps / (st.kernel_ms / 1e3) / 1e9,
+        "roofline": roofline(st.sample_steps, st.samples, st.kernel_ms, p.integrator, w.storage, False, 0, ceiling,
+                             "")}
+
+    def dvr(technique):
+        q = capi.Params.from_buffer_copy(p)
+        q.technique = capi.TECHNIQUE[technique]
+        ctx.set_params(q)
+        frame_fn = lambda: ctx.render_device(vid, out.data_ptr(), W, H, None, sh)  # noqa: E731
+        timed(torch, stream, flush, frame_fn)
+        ms = min(timed(torch, stream, flush, frame_fn) for _ in range(3))
+        return ms, ctx.stats()
+
+    for key, technique in (("licvolume_dvr", "licvolume"), ("vector_dvr", "volume")):
+        ms, st = dvr(technique)
+        rate = st.samples / (ms / 1e3) / 1e9
+        res[key] = {"ms": ms, "samples": int(st.samples), "gsamples_per_s": rate,
+                    "roofline": {"bound": "l1tex", "unit": "G samples/s", "achieved": rate, "peak": tex_peak,
+                                 "frac": rate / tex_peak if tex_peak else None,
+                                 "peak_kind": "measured trilinear fetch rate (vvlic_measure_fetch_ceiling)",
+                                 "note": "one trilinear field fetch per sample through the texture unit"
+                                         + (" plus an 8-load gather of the FP32 LIC volume"
+                                            if technique == "licvolume" else "")}}
+    ms, st = dvr("slicing")
+    res["slicing"] = {"ms": ms, "samples": int(st.samples), "gss": st.sample_steps / (ms / 1e3) / 1e9,
+                      "roofline": roofline(st.sample_steps, st.samples, ms, p.integrator, w.storage, True, W * H,
+                                           ceiling, "")}
+    ctx.set_params(p)
+
+    # field update from device memory: the same field, so the volume is unchanged afterwards
+    d_xyz = torch.from_numpy(np.ascontiguousarray(w.field)).cuda()
+    nz, ny, nx = w.field.shape[:3]
+    upd = lambda: ctx.update_field_device(vid, d_xyz.data_ptr(), (nx, ny, nz), sh)  # noqa: E731
+    timed(torch, stream, flush, upd)
+    ms = min(timed(torch, stream, flush, upd) for _ in range(3))
+    vox = nx * ny * nz
+    vbytes = ctx.volume_bytes(vid)
+    texels = vox * bytes_per_texel(w.storage)
+    # two passes over the float32 field, every layout of the volume written once, the texels read
+    # once more to build the derived layouts
+    alg = vox * 24 + vbytes + (texels if vbytes > texels else 0)
+    res["field_update_device"] = {
+        "ms": ms, "voxels": vox, "volume_bytes": vbytes,
+        "roofline": {"bound": "hbm", "unit": "GB/s", "achieved": alg / (ms / 1e3) / 1e9, "peak": peak_hbm,
+                     "frac": alg / (ms / 1e3) / 1e9 / peak_hbm, "peak_kind": hbm_kind, "traffic": None,
+                     "algorithmic_bytes": alg,
+                     "bytes": "24 B per voxel read (the length pass and the encode pass over float32 xyz) + "
+                              "the volume's layouts written (texels, texture copy, cells if any) + the "
+                              "texels read once to build the derived layouts"}}
+    del d_xyz
+
+    # noise gradients: 4 calls per timed region, the first untimed, so that the stream-ordered
+    # scratch of calls 2-4 comes from the pool's free list
+    mz, my, mx = w.noise.shape
+    d_noise = torch.from_numpy(np.ascontiguousarray(w.noise)).cuda()
+    d_rgba = torch.empty(mx * my * mz * 4, dtype=torch.uint8, device="cuda")
+    ng = lambda: capi.noise_gradients_device(d_noise.data_ptr(), (mx, my, mz), w.noise_mode,  # noqa: E731
+                                             d_rgba.data_ptr(), None, sh)
+    best = 1e30
+    for _ in range(3):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            ng()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(3):
+                ng()
+            e1.record(stream)
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1) / 3)
+    nvox = mx * my * mz
+    alg = nvox * 30  # raw pass: 1 B read, 12 B written; filter pass: 12 B + 1 B read, 4 B written
+    res["noise_gradients"] = {
+        "ms": best, "voxels": nvox,
+        "roofline": {"bound": "hbm", "unit": "GB/s", "achieved": alg / (best / 1e3) / 1e9, "peak": peak_hbm,
+                     "frac": alg / (best / 1e3) / 1e9 / peak_hbm, "peak_kind": hbm_kind, "traffic": None,
+                     "algorithmic_bytes": alg,
+                     "bytes": "30 B per voxel: the raw-gradient pass reads the noise byte (its 27-voxel "
+                              "stencil from L1) and writes 12 B; the filter pass reads 12 B (27-voxel "
+                              "stencil from L1) and the noise byte and writes 4 B RGBA"}}
+    del d_noise, d_rgba
+    return res
+
+
 def run_ours(args, dist):
     import torch
 
@@ -762,6 +886,9 @@ def headline(args, dist, torch, stream, flush, ceiling) -> dict:
 
     if not args.no_adjoint and dist.rank == 0:
         line["orbit_adjoint"] = bench_orbit_adjoint(ctx, torch, stream, flush, w, vid, out, frames[0])
+
+    if not args.no_rows and dist.rank == 0:
+        line["rows"] = bench_rows(ctx, torch, stream, flush, w, vid, ceiling, frames[0], args)
 
     # CPU baseline (rank 0, N=1 only): the FP32 OpenMP restatement on a bounded row sample of
     # the last timed frame, compared with the GPU's rows of that frame

@@ -307,6 +307,14 @@ vvlic_status vvlic_update_field(vvlic_ctx* ctx, int32_t vol_id, const void* xyz,
  *     encoding has consumed the staging buffer. */
 vvlic_status vvlic_update_field_async(vvlic_ctx* ctx, int32_t vol_id, const void* xyz, int32_t dtype,
                                       int32_t nx, int32_t ny, int32_t nz, void* stream);
+/* vvlic_update_field_async from a device array (float32 xyz, nx*ny*nz*3, x fastest) that a
+ * simulation or another kernel wrote on this GPU: no host copy, no staging buffer.  The
+ * re-encoding and layout rebuild run on `stream` after the work already enqueued there; `d_xyz`
+ * must stay unchanged until they have run.  The same ordering rules as vvlic_update_field_async
+ * hold for renders on other streams.  No counterpart in the reference (its fields come from
+ * files, dataset.cpp:533-635). */
+vvlic_status vvlic_update_field_device(vvlic_ctx* ctx, int32_t vol_id, const float* d_xyz, int32_t nx, int32_t ny,
+                                       int32_t nz, void* stream);
 /* The same with the time interpolation of vvlic_upload_field_interp. */
 vvlic_status vvlic_update_field_interp(vvlic_ctx* ctx, int32_t vol_id, const void* xyz0, const void* xyz1,
                                        int32_t dtype, int32_t nx, int32_t ny, int32_t nz,
@@ -446,7 +454,8 @@ vvlic_status vvlic_render_adjoint(vvlic_ctx* ctx, int32_t vol_id, const float* d
  * lic3d_volume_fragment.glsl — computeLIC * licKernel.b * gradientScale at every voxel centre of
  * an nx*ny*nz grid (the reference uses 512^3, renderer.cpp:97) with the current parameters,
  * kept with the volume (FP32; the reference's buffer is RGBA16F) for VVLIC_TECHNIQUE_LICVOLUME
- * renders.  Synchronous. */
+ * renders.  Synchronous.  vvlic_get_stats then reports the precompute: samples = voxels,
+ * sample_steps = voxels * (L_b + L_f), rays = 0 and its kernel time. */
 vvlic_status vvlic_compute_lic_volume(vvlic_ctx* ctx, int32_t vol_id, int32_t nx, int32_t ny, int32_t nz);
 /* Copy a volume's LIC volume (nx*ny*nz floats, x fastest) to host memory. */
 vvlic_status vvlic_download_lic_volume(vvlic_ctx* ctx, int32_t vol_id, float* out, uint64_t capacity);
@@ -609,8 +618,8 @@ typedef struct vvlic_fetch_ceiling {
  * a few percent of HBM bandwidth, so HBM does not bound them). */
 vvlic_status vvlic_measure_fetch_ceiling(int32_t device, int32_t spread4, vvlic_fetch_ceiling* out);
 
-/* Largest noise (voxels) vvlic_noise_gradients_device_noalloc accepts: its fixed 12 MiB
- * gradient scratch holds three floats per voxel. */
+/* Largest noise (voxels) vvlic_noise_gradients_device_noalloc accepts: its fixed 16 MiB
+ * gradient scratch holds four floats per voxel. */
 #define VVLIC_NOALLOC_MAX_VOXELS (1u << 20)
 
 /* No counterpart in the reference.  The same computation and output as
@@ -618,7 +627,7 @@ vvlic_status vvlic_measure_fetch_ceiling(int32_t device, int32_t spread4, vvlic_
  * call: applications that reserve their GPU memory budget at start-up and forbid later
  * allocations, or frame loops that cannot afford allocator latency and cudaFree's implicit
  * synchronisation.  The temporary gradients live in a fixed device array compiled into the
- * library (VVLIC_NOALLOC_MAX_VOXELS * 12 bytes, held on every GPU that loads the library until
+ * library (VVLIC_NOALLOC_MAX_VOXELS * 16 bytes, held on every GPU that loads the library until
  * the process exits); the caller still passes the input and output buffers.
  *   - Runs on the current CUDA device.  The first call on a device looks up that array's
  *     device address (cudaGetSymbolAddress) and caches it; make that first call before any

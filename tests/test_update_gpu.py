@@ -50,6 +50,57 @@ def test_update_field_equals_fresh_upload(ctx, storage):
     ctx.free_volume(vid)
 
 
+@pytest.mark.parametrize("storage", ["f32", "f16", "u8"])
+def test_update_field_device_equals_fresh_upload(ctx, storage):
+    """vvlic_update_field_device (float32 xyz already on the device, ordered on a stream) leaves
+    the volume bit for bit as a fresh upload of the same field, in every layout; the LIC volume
+    turns stale as with the host update."""
+    import torch
+
+    w = small()
+    vid = wl.setup_context(ctx, w, storage=storage)
+    for sm in SAMPLERS:
+        render(ctx, vid, w, sm)
+    ctx.compute_lic_volume(vid, (24, 24, 24))
+    new = other_field(w, seed=78)
+    d_new = torch.from_numpy(np.ascontiguousarray(new)).cuda()
+    stream = torch.cuda.Stream()
+    nz, ny, nx = new.shape[:3]
+    ctx.update_field_device(vid, d_new.data_ptr(), (nx, ny, nz), stream.cuda_stream)
+    stream.synchronize()
+    fresh = ctx.upload_field(new, storage=storage)
+    for sm in SAMPLERS:
+        np.testing.assert_array_equal(render(ctx, vid, w, sm), render(ctx, fresh, w, sm), err_msg=f"{storage}/{sm}")
+    np.testing.assert_array_equal(ctx.download_field(vid, (nx, ny, nz), storage),
+                                  ctx.download_field(fresh, (nx, ny, nz), storage))
+    p = w.params
+    p.technique = capi.TECHNIQUE["licvolume"]
+    ctx.set_params(p)
+    with pytest.raises(capi.VVLICError) as e:
+        ctx.render(vid, w.width, w.height)
+    assert e.value.status == capi.ERR_NOT_READY
+    p.technique = capi.TECHNIQUE["raycast"]
+    ctx.set_params(p)
+    with pytest.raises(capi.VVLICError) as e:
+        ctx.update_field_device(vid, d_new.data_ptr(), (nx, ny, nz + 1), stream.cuda_stream)
+    assert e.value.status == capi.ERR_INVALID_ARGUMENT
+    ctx.free_volume(fresh)
+    ctx.free_volume(vid)
+
+
+def test_lic_volume_stats(ctx):
+    """vvlic_get_stats after vvlic_compute_lic_volume: one sample per voxel, L_b + L_f steps each,
+    the kernel time."""
+    w = small()
+    vid = wl.setup_context(ctx, w)
+    ctx.compute_lic_volume(vid, (24, 20, 16))
+    st = ctx.stats()
+    assert st.samples == 24 * 20 * 16
+    assert st.sample_steps == st.samples * (w.params.steps_backward + w.params.steps_forward)
+    assert st.rays == 0 and st.kernel_ms > 0 and st.check_flags == 0
+    ctx.free_volume(vid)
+
+
 def test_update_field_interp_equals_upload_field_interp(ctx):
     w = small()
     f0, f1 = w.field, other_field(w, seed=5)

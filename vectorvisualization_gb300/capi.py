@@ -194,6 +194,7 @@ _SIGS = {
     "vvlic_update_field": (_I, [_P, _I, _P, _I, _I, _I, _I]),
     "vvlic_update_field_interp": (_I, [_P, _I, _P, _P, _I, _I, _I, _I, _I, _I]),
     "vvlic_update_field_async": (_I, [_P, _I, _P, _I, _I, _I, _I, _P]),
+    "vvlic_update_field_device": (_I, [_P, _I, _P, _I, _I, _I, _P]),
     "vvlic_upload_noise_async": (_I, [_P, _P, _I, _I, _I, _I, _P]),
     "vvlic_render_to_host_async": (_I, [_P, _I, _P, _I, _I, _P]),
     "vvlic_free_volume": (_I, [_P, _I]),
@@ -577,6 +578,11 @@ class Context:
         nx, ny, nz = dims
         self._check(self._lib.vvlic_update_field_async(self.h, vid, h_xyz, dtype, nx, ny, nz, stream or None),
                     "update_field_async")
+
+    def update_field_device(self, vid: int, d_xyz: int, dims, stream: int):
+        nx, ny, nz = dims
+        self._check(self._lib.vvlic_update_field_device(self.h, vid, d_xyz, nx, ny, nz, stream or None),
+                    "update_field_device")
 
     def upload_noise_async(self, h_noise: int, dims, mode: int, stream: int):
         mx, my, mz = dims

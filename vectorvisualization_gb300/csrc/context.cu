@@ -623,6 +623,23 @@ extern "C" vvlic_status vvlic_update_field_async(vvlic_ctx* c, int32_t vol_id, c
   return VVLIC_OK;
 }
 
+extern "C" vvlic_status vvlic_update_field_device(vvlic_ctx* c, int32_t vol_id, const float* d_xyz, int32_t nx,
+                                                 int32_t ny, int32_t nz, void* stream) {
+  if (!c) return VVLIC_ERR_BAD_HANDLE;
+  if (!d_xyz) return fail(c, VVLIC_ERR_INVALID_ARGUMENT, "update_field_device: null data");
+  Volume* v = nullptr;
+  vvlic_status st = update_target(c, vol_id, VVLIC_DTYPE_FLOAT32, nx, ny, nz, "update_field_device", &v);
+  if (st) return st;
+  DeviceGuard g(c->device);
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e = launch_encode_field(d_xyz, VVLIC_DTYPE_FLOAT32, v->n, v->storage, v->d_texels, c->d_scratch_word, s);
+  if (e != cudaSuccess) return cuda_fail(c, e, "update_field_device");
+  if ((st = refresh_volume_layouts(c, *v, s))) return st;
+  v->licvol_valid = false;
+  if (c->tape_vol == vol_id) c->tape_valid = false;
+  return VVLIC_OK;
+}
+
 extern "C" vvlic_status vvlic_upload_field_device(vvlic_ctx* c, const float* d_xyz, int32_t nx, int32_t ny, int32_t nz,
                                                  const float* slice_dist, int32_t storage, void* stream,
                                                  int32_t* vol_id) {
@@ -673,7 +690,7 @@ extern "C" vvlic_status vvlic_noise_gradients_device(const uint8_t* d_noise, int
   noise_filter_weights(w27);
   cudaStream_t s = (cudaStream_t)stream;
   float* d_grad = nullptr;
-  const size_t bytes = (size_t)mx * my * mz * 3 * sizeof(float);
+  const size_t bytes = (size_t)mx * my * mz * kNoiseGradBytes;
   cudaError_t e = cudaMallocAsync((void**)&d_grad, bytes, s);
   if (e != cudaSuccess) return e == cudaErrorMemoryAllocation ? VVLIC_ERR_OUT_OF_MEMORY : VVLIC_ERR_CUDA;
   e = launch_noise_gradients(d_noise, m, mode, sd, d_grad, d_rgba, w27, s);
@@ -683,9 +700,9 @@ extern "C" vvlic_status vvlic_noise_gradients_device(const uint8_t* d_noise, int
 }
 
 // Upload-buffer layout for noise gradients: the noise bytes, then (256-byte aligned) the raw
-// float gradients.
+// float gradients (kNoiseGradBytes per voxel).
 static size_t noise_grad_offset(size_t count) { return (count + 255) & ~(size_t)255; }
-static size_t noise_staging_bytes(size_t count) { return noise_grad_offset(count) + count * 3 * sizeof(float); }
+static size_t noise_staging_bytes(size_t count) { return noise_grad_offset(count) + count * kNoiseGradBytes; }
 
 // Noise gradients (computeGradients + filterGradients + quantizeGradients + pack) of the noise
 // bytes staged at the start of the context's upload buffer (noise_staging_bytes of capacity),

@@ -1,7 +1,7 @@
 // Noise-gradient precompute that allocates nothing.
 //
-// vvlic_noise_gradients_device needs a temporary buffer of three floats per voxel (the raw
-// gradients before smoothing) and gets it from the CUDA allocator.  Some callers cannot
+// vvlic_noise_gradients_device needs a temporary buffer of four floats per voxel (the raw
+// gradients before smoothing, padded to 16 bytes) and gets it from the CUDA allocator.  Some callers cannot
 // allocate device memory at that point: a host application that reserves its whole GPU memory
 // budget up front and forbids allocations afterwards (a render or simulation host embedding
 // this library as a plugin), or a frame loop where cudaMalloc / cudaFree would add allocator
@@ -9,7 +9,7 @@
 // the temporary buffer in a fixed device array that is part of the library's module, so the
 // call itself performs no allocation.
 //
-// The array is VVLIC_NOALLOC_MAX_VOXELS * 3 floats (12 MiB).  Every GPU that loads the library
+// The array is VVLIC_NOALLOC_MAX_VOXELS * 4 floats (16 MiB).  Every GPU that loads the library
 // holds it until the process exits.  All calls share it: two calls that run on the GPU at the
 // same time (different streams or threads) race on it, so callers must order them.  Nothing in
 // it needs to start at zero — the first kernel writes every element the second one reads — and
@@ -27,8 +27,9 @@
 
 namespace {
 
-// Fixed scratch: raw gradients (x, y, z) of up to VVLIC_NOALLOC_MAX_VOXELS voxels.
-static __device__ __align__(256) float g_noalloc_gradients[3 * (size_t)VVLIC_NOALLOC_MAX_VOXELS];
+// Fixed scratch: raw gradients (x, y, z, padding) of up to VVLIC_NOALLOC_MAX_VOXELS voxels.
+static __device__ __align__(256) float g_noalloc_gradients[vvlic::kNoiseGradBytes / sizeof(float) *
+                                                           (size_t)VVLIC_NOALLOC_MAX_VOXELS];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;

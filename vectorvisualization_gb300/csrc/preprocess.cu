@@ -103,54 +103,72 @@ __device__ __forceinline__ float nv(const uint8_t* v, int nx, int ny, int x, int
   return (float)v[((size_t)z * ny + y) * nx + x];
 }
 
+// The noise-gradient kernels run one thread per voxel on a (ceil(nx / kThreads), ny, nz) grid:
+// the voxel's coordinates come from the block and thread indices without integer division.
+inline dim3 voxel_grid(const int m[3]) { return dim3((unsigned)((m[0] + kThreads - 1) / kThreads), m[1], m[2]); }
+
 // computeGradients (gradient.cpp:190-374) for one voxel.
 __global__ void noise_grad_raw_kernel(const uint8_t* v, int nx, int ny, int nz, int mode, float sd0, float sd1,
-                                      float sd2, float* g) {
-  const size_t count = (size_t)nx * ny * nz;
-  for (size_t a = blockIdx.x * (size_t)blockDim.x + threadIdx.x; a < count; a += (size_t)gridDim.x * blockDim.x) {
-    const int x = (int)(a % nx), y = (int)((a / nx) % ny), z = (int)(a / ((size_t)nx * ny));
+                                      float sd2, float4* g) {
+  {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
+    if (x >= nx) return;
+    const size_t a = ((size_t)z * ny + y) * nx + x;
     const float sd[3] = {sd0, sd1, sd2};
     float gp[3];
     if (mode == VVLIC_NOISE_GRAD_SOBEL && x > 0 && x < nx - 1 && y > 0 && y < ny - 1 && z > 0 && z < nz - 1) {
       // weights[dir][i+1][j+1][k+1]: the 3x3x3 Sobel masks (gradient.cpp:199-224), summed in
       // the reference's i, j, k order
       const int s1[3] = {1, 3, 1}, s2[3] = {3, 6, 3};
+      // the 27 neighbours once; the three masks then run over them in the same i, j, k order
+      float nb[27];
+#pragma unroll
+      for (int i = -1; i < 2; i++)
+#pragma unroll
+        for (int j = -1; j < 2; j++)
+#pragma unroll
+          for (int k = -1; k < 2; k++) nb[((i + 1) * 3 + (j + 1)) * 3 + (k + 1)] = nv(v, nx, ny, x + i, y + j, z + k);
+#pragma unroll
       for (int d = 0; d < 3; ++d) {
         float acc = 0.0f;
+#pragma unroll
         for (int i = -1; i < 2; i++)
+#pragma unroll
           for (int j = -1; j < 2; j++)
+#pragma unroll
             for (int k = -1; k < 2; k++) {
               const int o[3] = {i, j, k};
               const int e = o[d];  // derivative axis offset
               const int p = o[(d + 1) % 3], q = o[(d + 2) % 3];
               // mask = sign(e) * w(p) * w(q) with w = (1,3,1) cross (1,3,1) pattern (1,3,1;3,6,3;1,3,1)
               int w = e == 0 ? 0 : e * ((p == 0 ? s2 : s1)[q + 1]);
-              acc += (float)w * nv(v, nx, ny, x + i, y + j, z + k);
+              acc += (float)w * nb[((i + 1) * 3 + (j + 1)) * 3 + (k + 1)];
             }
         gp[d] = acc / (2.0f * sd[d]);
       }
-    } else if (mode == VVLIC_NOISE_GRAD_SOBEL) {
-      const float c = nv(v, nx, ny, x, y, z);
-      gp[0] = (x < 1) ? (nv(v, nx, ny, x + 1, y, z) - c) / sd[0] : (c - nv(v, nx, ny, x - 1, y, z)) / sd[0];
-      gp[1] = (y < 1) ? (nv(v, nx, ny, x, y + 1, z) - c) / sd[1] : (c - nv(v, nx, ny, x, y - 1, z)) / sd[1];
-      gp[2] = (z < 1) ? (nv(v, nx, ny, x, y, z + 1) - c) / sd[2] : (c - nv(v, nx, ny, x, y, z - 1)) / sd[2];
     } else {
-      // central differences (SOBEL 0 branch); the last slice per axis uses a one-sided
-      // difference — those values are never read by the smoothing window below
-      const float c = nv(v, nx, ny, x, y, z);
+      // the voxel's neighbours along axis d lie `st[d]` bytes away
+      const uint8_t* cp = v + a;
+      const float c = (float)cp[0];
+      const size_t st[3] = {1, (size_t)nx, (size_t)nx * ny};
       const int P[3] = {x, y, z}, N[3] = {nx, ny, nz};
-      for (int d = 0; d < 3; ++d) {
-        int lo[3] = {x, y, z}, hi[3] = {x, y, z};
-        lo[d] = P[d] - 1;
-        hi[d] = P[d] + 1;
-        if (P[d] < 1) gp[d] = (nv(v, nx, ny, hi[0], hi[1], hi[2]) - c) / sd[d];
-        else if (P[d] >= N[d] - 1) gp[d] = (c - nv(v, nx, ny, lo[0], lo[1], lo[2])) / sd[d];
-        else gp[d] = (nv(v, nx, ny, hi[0], hi[1], hi[2]) - nv(v, nx, ny, lo[0], lo[1], lo[2])) / sd[d] * 0.5f;
+      if (mode == VVLIC_NOISE_GRAD_SOBEL) {
+        // one-sided differences on the border of the Sobel mode
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+          gp[d] = (P[d] < 1) ? ((float)cp[st[d]] - c) / sd[d] : (c - (float)*(cp - st[d])) / sd[d];
+      } else {
+        // central differences (SOBEL 0 branch); the last slice per axis uses a one-sided
+        // difference — those values are never read by the smoothing window below
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          if (P[d] < 1) gp[d] = ((float)cp[st[d]] - c) / sd[d];
+          else if (P[d] >= N[d] - 1) gp[d] = (c - (float)*(cp - st[d])) / sd[d];
+          else gp[d] = ((float)cp[st[d]] - (float)*(cp - st[d])) / sd[d] * 0.5f;
+        }
       }
     }
-    g[3 * a + 0] = gp[0];
-    g[3 * a + 1] = gp[1];
-    g[3 * a + 2] = gp[2];
+    g[a] = make_float4(gp[0], gp[1], gp[2], 0.0f);  // padded to 16 bytes: one vector load per filter tap
   }
 }
 
@@ -158,12 +176,33 @@ struct W27 {
   float w[27];
 };
 
+// (unsigned char)(((double)c + 1.0) / 2.0 * 255.0), quantizeGradients' conversion of a unit
+// component c (gradient.cpp:466-477), without double arithmetic for almost every input.  The
+// float t = fma(c, 127.5, 127.5) is within 2^-17 of the exact (c + 1) * 127.5 and the double
+// expression within 2^-44 of it; the exact value is an integer only at c = -1 and c = 1, so
+// when t lies more than 1e-4 from an integer both truncate to floor(t).  Inputs nearer an
+// integer (about 2 in 10^4) take the double expression itself, in a call of its own so that the
+// compiler cannot evaluate it speculatively for every voxel (GB300's FP64 rate is a small
+// fraction of its FP32 rate).
+__device__ __noinline__ unsigned char quantize_unit_double(float c) {
+  return (unsigned char)(((double)c + 1.0) / 2.0 * 255.0);
+}
+__device__ __forceinline__ unsigned char quantize_unit(float c) {
+  const float t = fmaf(c, 127.5f, 127.5f);
+  const float f = floorf(t);
+  const float r = t - f;
+  if (r > 1e-4f && r < 1.0f - 1e-4f) return (unsigned char)(int)f;
+  return quantize_unit_double(c);
+}
+
 // filterGradients + quantize8 + RGBA pack (gradient.cpp:377-478, dataset.cpp:1270-1286).
-__global__ void noise_grad_filter_kernel(const uint8_t* v, const float* g, int nx, int ny, int nz, W27 fw27,
+__global__ void noise_grad_filter_kernel(const uint8_t* v, const float4* g, int nx, int ny, int nz,
+                                         const __grid_constant__ W27 fw27,
                                          uint8_t* out) {
-  const size_t count = (size_t)nx * ny * nz;
-  for (size_t a = blockIdx.x * (size_t)blockDim.x + threadIdx.x; a < count; a += (size_t)gridDim.x * blockDim.x) {
-    const int x = (int)(a % nx), y = (int)((a / nx) % ny), z = (int)(a / ((size_t)nx * ny));
+  {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
+    if (x >= nx) return;
+    const size_t a = ((size_t)z * ny + y) * nx + x;
     int bd = min(min(min(x, nx - x - 1), min(y, ny - y - 1)), min(z, nz - z - 1));
     const int fw = min(2, bd);
     // One pass over the window with the three channel sums side by side: each channel adds its
@@ -174,13 +213,14 @@ __global__ void noise_grad_filter_kernel(const uint8_t* v, const float* g, int n
       for (int k = -2; k < 1; ++k)
 #pragma unroll
         for (int j = -2; j < 1; ++j) {
-          const float* row = g + 3 * (((size_t)(z + k) * ny + (y + j)) * nx + x);
+          const float4* row = g + ((size_t)(z + k) * ny + (y + j)) * nx + x;
 #pragma unroll
           for (int i = -2; i < 1; ++i) {
             const float w = fw27.w[((k + 2) * 3 + (j + 2)) * 3 + (i + 2)];
-            acc[0] += w * row[3 * i];
-            acc[1] += w * row[3 * i + 1];
-            acc[2] += w * row[3 * i + 2];
+            const float4 q = row[i];
+            acc[0] += w * q.x;
+            acc[1] += w * q.y;
+            acc[2] += w * q.z;
           }
         }
     } else {
@@ -191,10 +231,10 @@ __global__ void noise_grad_filter_kernel(const uint8_t* v, const float* g, int n
             // all three indices in [0, 2] are ever used
             const int wk = fw + k, wj = fw + j, wi = fw + i;
             const float w = fw27.w[(wk * 3 + wj) * 3 + wi];
-            const float* q = g + 3 * (((size_t)(z + k) * ny + (y + j)) * nx + (x + i));
-            acc[0] += w * q[0];
-            acc[1] += w * q[1];
-            acc[2] += w * q[2];
+            const float4 q = g[((size_t)(z + k) * ny + (y + j)) * nx + (x + i)];
+            acc[0] += w * q.x;
+            acc[1] += w * q.y;
+            acc[2] += w * q.z;
           }
     }
     float len = sqrtf(acc[0] * acc[0] + acc[1] * acc[1] + acc[2] * acc[2]);
@@ -206,9 +246,9 @@ __global__ void noise_grad_filter_kernel(const uint8_t* v, const float* g, int n
       acc[2] /= len;
     }
     uchar4 o;
-    o.x = (unsigned char)(((double)acc[0] + 1.0) / 2.0 * 255.0);
-    o.y = (unsigned char)(((double)acc[1] + 1.0) / 2.0 * 255.0);
-    o.z = (unsigned char)(((double)acc[2] + 1.0) / 2.0 * 255.0);
+    o.x = quantize_unit(acc[0]);
+    o.y = quantize_unit(acc[1]);
+    o.z = quantize_unit(acc[2]);
     o.w = v[a];
     reinterpret_cast<uchar4*>(out)[a] = o;
   }
@@ -331,12 +371,11 @@ cudaError_t launch_encode_field(const void* d_xyz, int dtype, const int n[3], in
 
 cudaError_t launch_noise_gradients(const uint8_t* d_noise, const int m[3], int mode, const float sd[3], float* d_grad,
                                    uint8_t* d_rgba, const float w27[27], cudaStream_t s) {
-  const size_t count = (size_t)m[0] * m[1] * m[2];
-  noise_grad_raw_kernel<<<grid_for(count), kThreads, 0, s>>>(d_noise, m[0], m[1], m[2], mode, sd[0], sd[1], sd[2],
-                                                              d_grad);
+  float4* g4 = reinterpret_cast<float4*>(d_grad);
+  noise_grad_raw_kernel<<<voxel_grid(m), kThreads, 0, s>>>(d_noise, m[0], m[1], m[2], mode, sd[0], sd[1], sd[2], g4);
   W27 w;
   for (int i = 0; i < 27; ++i) w.w[i] = w27[i];
-  noise_grad_filter_kernel<<<grid_for(count), kThreads, 0, s>>>(d_noise, d_grad, m[0], m[1], m[2], w, d_rgba);
+  noise_grad_filter_kernel<<<voxel_grid(m), kThreads, 0, s>>>(d_noise, g4, m[0], m[1], m[2], w, d_rgba);
   return cudaGetLastError();
 }
 

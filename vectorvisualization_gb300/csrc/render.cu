@@ -722,10 +722,27 @@ extern "C" vvlic_status vvlic_compute_lic_volume(vvlic_ctx* c, int32_t vol_id, i
   // lic3d_volume_fragment.glsl composes inc_lic without inc_illum: the uniform scaleVol is the
   // volume's scale whatever the shading variant
   for (int i = 0; i < 3; ++i) a.scale_vol[i] = v.geom.scale[i];
-  cudaError_t e = launch_technique(v.storage, a, t, c->params.sampler, c->params.integrator, false, s);
+  cudaError_t e = cudaMemsetAsync(c->d_counters, 0, 4 * sizeof(unsigned long long), s);
+  if (e == cudaSuccess) e = cudaEventRecord(c->ev0, s);
+  if (e == cudaSuccess) e = launch_technique(v.storage, a, t, c->params.sampler, c->params.integrator, false, s);
+  if (e == cudaSuccess) e = cudaEventRecord(c->ev1, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return cuda_fail(c, e, "compute_lic_volume");
   v.licvol_valid = true;
+  // the precompute's statistics: one LIC sample per voxel, L_b + L_f streamline steps each
+  unsigned long long h[4];
+  float ms = 0.f;
+  e = cudaMemcpy(h, c->d_counters, sizeof h, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+  if (e != cudaSuccess) return cuda_fail(c, e, "compute_lic_volume statistics");
+  c->stats.samples = count;
+  c->stats.sample_steps = count * (uint64_t)(a.lb + a.lf);
+  c->stats.rays = 0;
+  c->stats.kernel_ms = ms;
+  c->stats.check_flags = (uint32_t)h[3];
+  c->stats_pending = false;
+  c->last_was_batch = false;
+  c->tape_flag_pending = false;
   return VVLIC_OK;
 }
 

@@ -116,7 +116,9 @@ cudaError_t launch_encode_field(const void* d_xyz, int dtype, const int n[3], in
 // Time interpolation of two raw vector fields at t = interpIndex / InterpSize.
 cudaError_t launch_interp_field(const void* d_a0, const void* d_a1, int dtype, const int n[3], float t, void* d_out,
                                 cudaStream_t s);
-// Raw noise gradients (float xyz per voxel) into d_grad, then smoothing + quantisation + pack.
+// Raw noise gradients (float xyz + padding: kNoiseGradBytes per voxel, 16-byte aligned) into
+// d_grad, then smoothing + quantisation + pack.
+constexpr size_t kNoiseGradBytes = 4 * sizeof(float);
 cudaError_t launch_noise_gradients(const uint8_t* d_noise, const int m[3], int mode, const float sd[3],
                                    float* d_grad, uint8_t* d_rgba, const float w27[27], cudaStream_t s);
 // Corner-packed cell arrays (see VVLIC_SAMPLER_CELL).
