@@ -82,6 +82,15 @@ class Renderer {
   void updateDataTex(const float* xyz, int nx, int ny, int nz) {
     check(vvlic_update_field(ctx_, vol_, xyz, VVLIC_DTYPE_FLOAT32, nx, ny, nz), "updateDataTex");
   }
+  /* the same step ordered on a CUDA stream: the host copy overlaps the renders already enqueued
+   * there; `xyz` must stay unchanged until the stream has passed the update */
+  void updateDataTexAsync(const float* xyz, int nx, int ny, int nz, void* stream) {
+    check(vvlic_update_field_async(ctx_, vol_, xyz, VVLIC_DTYPE_FLOAT32, nx, ny, nz, stream), "updateDataTexAsync");
+  }
+  /* the same step from float32 xyz already in device memory (no host copy) */
+  void updateDataTexDevice(const float* d_xyz, int nx, int ny, int nz, void* stream) {
+    check(vvlic_update_field_device(ctx_, vol_, d_xyz, nx, ny, nz, stream), "updateDataTexDevice");
+  }
   /* VectorDataSet::loadData(file) + createTextureIterp: a .dat/.raw vector data set (the
    * timestep, or the first one for -1) becomes the current volume */
   int loadData(const char* datFile, int timestep = -1, int storage = VVLIC_STORAGE_F16) {
@@ -106,6 +115,13 @@ class Renderer {
   void setNoiseTex(const unsigned char* noise, int mx, int my, int mz, bool gradients,
                    int gradMode = VVLIC_NOISE_GRAD_SOBEL) {
     check(vvlic_upload_noise(ctx_, noise, mx, my, mz, gradients ? gradMode : VVLIC_NOISE_SCALAR), "setNoiseTex");
+  }
+  /* a noise of the current noise's extent and kind, ordered on a CUDA stream like
+   * updateDataTexAsync */
+  void setNoiseTexAsync(const unsigned char* noise, int mx, int my, int mz, bool gradients, void* stream,
+                        int gradMode = VVLIC_NOISE_GRAD_SOBEL) {
+    check(vvlic_upload_noise_async(ctx_, noise, mx, my, mz, gradients ? gradMode : VVLIC_NOISE_SCALAR, stream),
+          "setNoiseTexAsync");
   }
   /* VolumeDataSet + Renderer::setScalarTex (the freqSampling gate volume) */
   void setScalarTex(const float* scalar, int nx, int ny, int nz) {
@@ -191,6 +207,18 @@ class Renderer {
   /* asynchronous render into device memory on a CUDA stream */
   void renderDevice(float* d_rgba, int w, int h, void* stream = nullptr) {
     check(vvlic_render_device(ctx_, vol_, d_rgba, w, h, nullptr, stream), "renderDevice");
+  }
+  /* asynchronous render into host memory (pinned for an overlapping copy) on a CUDA stream;
+   * `rgba` holds the image once synchronize(stream) has returned true */
+  void renderToHostAsync(float* rgba, int w, int h, void* stream) {
+    check(vvlic_render_to_host_async(ctx_, vol_, rgba, w, h, stream), "renderToHostAsync");
+  }
+  /* waits for the work enqueued on `stream` (NULL: the context's stream); false on timeout */
+  bool synchronize(void* stream = nullptr, int timeoutMs = 60000) {
+    vvlic_status s = vvlic_synchronize(ctx_, stream, timeoutMs);
+    if (s == VVLIC_ERR_TIMEOUT) return false;
+    check(s, "synchronize");
+    return true;
   }
   vvlic_stats stats() {
     vvlic_stats s;

@@ -56,6 +56,18 @@ int main(int argc, char** argv) {
     r.render(img.data(), w, h);
     save_raw(argv[3], "zoeckler", img);
     std::printf("samples %llu\n", (unsigned long long)r.stats().samples);
+    // the stream-ordered animation step: the same field re-uploaded in place, then a render
+    // into host memory, one wait at the end (the image must equal the first ray-cast)
+    vvlic_dat_info info;
+    if (vvlic_dat_parse(argv[1], &info) != VVLIC_OK || info.format != VVLIC_DAT_FLOAT || info.components != 3) return 5;
+    std::vector<float> xyz((size_t)vvlic_dat_bytes(&info) / sizeof(float));
+    if (vvlic_dat_read(&info, info.timestep_begin, xyz.data(), xyz.size() * sizeof(float)) != VVLIC_OK) return 5;
+    r.loadGLSLShader("");
+    r.updateDataTexAsync(xyz.data(), info.resolution[0], info.resolution[1], info.resolution[2], nullptr);
+    std::vector<float> async_img((size_t)w * h * 4);
+    r.renderToHostAsync(async_img.data(), w, h, nullptr);
+    if (!r.synchronize(nullptr, 120000)) return 6;
+    save_raw(argv[3], "async", async_img);
   } catch (const vvlic::Error& e) {
     std::fprintf(stderr, "%s\n", e.what());
     return 1;

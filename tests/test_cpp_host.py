@@ -1,7 +1,8 @@
 """The C++ host side: tests/cpp/renderer_demo.cpp drives the library through vvlic::Renderer
 (include/vvlic_renderer.hpp) the way the reference's 3DLIC.cpp drives its Renderer.  It must
 compile and link against libvvlic.so on any machine, and on a GPU its images must equal the
-same renders made through the Python binding, and match the FP64 oracle."""
+same renders made through the Python binding, and match the FP64 oracle; its stream-ordered
+animation step (updateDataTexAsync + renderToHostAsync) must give the first ray-cast again."""
 import os
 import shutil
 import subprocess
@@ -77,6 +78,8 @@ def test_demo_images_equal_python_binding_and_match_oracle(demo, tmp_path, ctx, 
         ctx.set_params(p)
         imgs[tag] = ctx.render(vid, W, H)
         np.testing.assert_array_equal(load(tag), imgs[tag], err_msg=tag)
+    # the demo's stream-ordered step (updateDataTexAsync of the same field + renderToHostAsync)
+    np.testing.assert_array_equal(load("async"), imgs["raycast"], err_msg="async")
     rgba, op = wl.default_tf()
     sc = oracle.Scene(oracle.encode_field(field), noise, rgba, op, filter_table=capi.make_filter_table("box", 256))
     p.technique = capi.TECHNIQUE["raycast"]
