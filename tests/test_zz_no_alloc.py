@@ -47,6 +47,26 @@ def test_noalloc_matches_allocating_entry_on_consecutive_calls(vvlic_lib):
             np.testing.assert_array_equal(got.cpu().numpy(), want.cpu().numpy())
 
 
+def test_noalloc_elongated_shapes_match_the_oracle(vvlic_lib, oracle):
+    """The entry point takes any shape up to 2^20 voxels, including axes longer than the grid's
+    y / z limit (65535), which the kernels step over; the bytes equal the oracle's (the FP32
+    restatement that is pinned to the reference's own gradient code)."""
+    import torch
+
+    lib = vvlic_lib
+    for dims, mode in (((4, 2, 131072), capi.NOISE_GRAD_SOBEL), ((2, 98304, 4), capi.NOISE_GRAD_CENTRAL),
+                       ((131072, 2, 4), capi.NOISE_GRAD_CENTRAL)):
+        mx, my, mz = dims
+        noise = wl.dense_noise((mx, my, mz), seed=35)
+        assert noise.shape == (mz, my, mx)
+        d_in = torch.from_numpy(noise).cuda()
+        out = torch.full(noise.shape + (4,), 3, dtype=torch.uint8, device="cuda")
+        assert lib.vvlic_noise_gradients_device_noalloc(d_in.data_ptr(), mx, my, mz, mode, None, out.data_ptr(),
+                                                        None) == 0, dims
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(out.cpu().numpy(), oracle.noise_gradients(noise, mode), err_msg=str(dims))
+
+
 def test_noalloc_rejects_sizes_above_its_maximum(vvlic_lib):
     import torch
 

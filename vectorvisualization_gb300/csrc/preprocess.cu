@@ -3,11 +3,13 @@
 //
 // This file is compiled with -fmad=false: every float expression rounds like the reference's
 // CPU code (no fused multiply-add), so the encoded field and the quantised gradients are
-// bit-identical to the reference's own arithmetic.
+// bit-identical to the reference's own arithmetic.  The one explicit fma (quantize_unit) only
+// decides a byte where it provably equals the reference's double expression.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <type_traits>
 
 #include "../../include/vvlic.h"
@@ -103,16 +105,22 @@ __device__ __forceinline__ float nv(const uint8_t* v, int nx, int ny, int x, int
   return (float)v[((size_t)z * ny + y) * nx + x];
 }
 
-// The noise-gradient kernels run one thread per voxel on a (ceil(nx / kThreads), ny, nz) grid:
-// the voxel's coordinates come from the block and thread indices without integer division.
-inline dim3 voxel_grid(const int m[3]) { return dim3((unsigned)((m[0] + kThreads - 1) / kThreads), m[1], m[2]); }
+// The noise-gradient kernels run one thread per x voxel on a (ceil(nx / kThreads), ny, nz) grid,
+// the y and z extents capped at the grid limit (the kernels step over the rest): a voxel's
+// coordinates come from the block and thread indices without integer division.
+constexpr int kGridYZ = 65535;
+inline dim3 voxel_grid(const int m[3]) {
+  return dim3((unsigned)((m[0] + kThreads - 1) / kThreads), (unsigned)std::min(m[1], kGridYZ),
+              (unsigned)std::min(m[2], kGridYZ));
+}
 
 // computeGradients (gradient.cpp:190-374) for one voxel.
 __global__ void noise_grad_raw_kernel(const uint8_t* v, int nx, int ny, int nz, int mode, float sd0, float sd1,
                                       float sd2, float4* g) {
-  {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
-    if (x >= nx) return;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= nx) return;
+  for (int z = blockIdx.z; z < nz; z += gridDim.z)
+  for (int y = blockIdx.y; y < ny; y += gridDim.y) {
     const size_t a = ((size_t)z * ny + y) * nx + x;
     const float sd[3] = {sd0, sd1, sd2};
     float gp[3];
@@ -199,9 +207,10 @@ __device__ __forceinline__ unsigned char quantize_unit(float c) {
 __global__ void noise_grad_filter_kernel(const uint8_t* v, const float4* g, int nx, int ny, int nz,
                                          const __grid_constant__ W27 fw27,
                                          uint8_t* out) {
-  {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
-    if (x >= nx) return;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= nx) return;
+  for (int z = blockIdx.z; z < nz; z += gridDim.z)
+  for (int y = blockIdx.y; y < ny; y += gridDim.y) {
     const size_t a = ((size_t)z * ny + y) * nx + x;
     int bd = min(min(min(x, nx - x - 1), min(y, ny - y - 1)), min(z, nz - z - 1));
     const int fw = min(2, bd);
