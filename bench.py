@@ -17,7 +17,9 @@ fetch ceiling of the GPU (vvlic_measure_fetch_ceiling); DRAM figures are reporte
 Extra keys: the mid-size lit frame with FP32/FP16/BF16 storage (`c2`), the 64-volume batch
 (`batch`), the differentiable-fit forward+adjoint (`fwd_adjoint`), the orbit's forward+adjoint
 (`orbit_adjoint`), the TMA-staged brick sampler against the texture and gather samplers
-(`brick_ab`).
+(`brick_ab`), and the techniques and preprocessing beside the ray-cast on the orbit's volume —
+slicing, LIC-volume precompute and ray-cast, vector-field DVR, device field update, noise
+gradients — each against its bound (`rows`).
 
 `--impl reference` times the CPU restatement of the reference's path (the reference itself is
 GLSL and runs only through OpenGL) on all host cores, on stratified rows of the same orbit
@@ -160,7 +162,8 @@ GROUP_KEY = {0: "euler", 1: "heun", 2: "rk4"}
 
 
 def bytes_per_texel(storage: str) -> int:
-    return 16 if storage == "f32" else 8
+    """RGBA texel bytes of a field storage: FP32 16, FP16 / BF16 8, UNORM8 4."""
+    return {"f32": 16, "f16": 8, "bf16": 8, "u8": 4}[storage]
 
 
 def cacheless_bytes(sample_steps: float, samples: float, integrator: int, storage: str, lit: bool,
