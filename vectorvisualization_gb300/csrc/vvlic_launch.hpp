@@ -68,28 +68,21 @@ cudaError_t launch_batch_f32(const BatchLaunch& b, int sampler, int integ, bool 
 cudaError_t launch_batch_f16(const BatchLaunch& b, int sampler, int integ, bool grad, cudaStream_t s);
 cudaError_t launch_batch_bf16(const BatchLaunch& b, int sampler, int integ, bool grad, cudaStream_t s);
 cudaError_t launch_batch_u8(const BatchLaunch& b, int sampler, int integ, bool grad, cudaStream_t s);
-// Word layout of the batch scratch: job tile starts (njobs+1), per-tile buckets, the (job,
-// tile) order as 8-byte aligned uint2 pairs, the bucket histogram and offsets, the queue
-// counter.
+// Word layout of the batch scratch: job tile starts (njobs+1, padded to an even count), the
+// (job, tile) order as 8-byte aligned uint2 pairs, the queue counter.
 struct BatchScratch {
   unsigned* start;
-  unsigned* bucket;
   uint2* order;
-  unsigned* hist;
-  unsigned* offsets;
   unsigned* next;
   size_t words;
 };
 inline BatchScratch batch_scratch(unsigned* base, int njobs, int ntiles) {
   BatchScratch b;
-  const size_t s0 = ((size_t)njobs + 2) & ~(size_t)1, nb = ((size_t)ntiles + 1) & ~(size_t)1;
+  const size_t s0 = ((size_t)njobs + 2) & ~(size_t)1;
   b.start = base;
-  b.bucket = base ? base + s0 : nullptr;
-  b.order = base ? reinterpret_cast<uint2*>(base + s0 + nb) : nullptr;
-  b.hist = base ? base + s0 + nb + 2 * (size_t)ntiles : nullptr;
-  b.offsets = base ? b.hist + 1024 : nullptr;
-  b.next = base ? b.offsets + 1024 : nullptr;
-  b.words = s0 + nb + 2 * (size_t)ntiles + 2048 + 2;
+  b.order = base ? reinterpret_cast<uint2*>(base + s0) : nullptr;
+  b.next = base ? base + s0 + 2 * (size_t)ntiles : nullptr;
+  b.words = s0 + 2 * (size_t)ntiles + 2;
   return b;
 }
 // Job-major (job, tile) order over a batch (batch.cu); start[] holds njobs+1 entries
